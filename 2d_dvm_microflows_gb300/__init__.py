@@ -1,0 +1,267 @@
+"""GB300 (sm_103a) DVM time step behind a C ABI, and a Python host that drives it.
+
+The package loads libdvm_gpu.so (built in-tree by build.py) through ctypes; there is no
+CPU fallback: without the library every call raises. `DVMSolver` mirrors the reference
+driver's time step (solver/dvm_solver.f90:231-369 in aarthisekaran11/2D_DVM_microflows):
+compute_collision_integral, compute_convection (with the boundary conditions) and
+calculate_physical_properties, with the reference's input-deck parameter names.
+"""
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import *  # noqa: F401,F403  (constants and structs of include/dvm_gpu.h)
+from . import physics
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdvm_gpu.so")
+
+_LIB = None
+
+
+class DVMError(RuntimeError):
+    """A non-zero status from the C ABI (the reference prints and stops on these)."""
+
+    def __init__(self, status, where):
+        self.status = status
+        msg = _LIB.dvm_strerror(status).decode() if _LIB is not None else str(status)
+        super().__init__("%s: %s (status %d)" % (where, msg, status))
+
+
+def load_library(path=None):
+    """Loads the GPU library; raises if it is missing (no fallback path exists)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libdvm_gpu.so is not built (%s); run "
+                           "`python 2d_dvm_microflows_gb300/build.py`" % p)
+    lib = _abi.bind(C.CDLL(p))
+    if lib.dvm_abi_version() != _abi.DVM_ABI_VERSION:
+        raise RuntimeError("ABI version mismatch")
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(st, where):
+    if st != DVM_OK:
+        raise DVMError(st, where)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+@dataclasses.dataclass
+class DVMConfig:
+    """Input-deck keys of the time step (input_output/read_input_2D.f90:75-777)."""
+    geometry: int = DVM_GEOM_0D
+    nx_space: int = 1
+    ny_space: int = 1
+    dx: float = 1.0
+    dy: float = 1.0
+    deltat: float = 0.01
+    Kn: float = 1.0
+    mass: float = 1.0
+    omega: float = 0.5
+    alpha: float = 1.0
+    sigma: float = 1.0
+    iColl: int = DVM_COLL_VR
+    iConv: int = DVM_CONV_NONE
+    ColnRMS: float = 0.001
+    NRepl: int = 1
+    cdf_tolerance: float = 0.01
+    samples_mode: int = DVM_SAMPLES_FORMULA
+    samples_per_step: int = 0
+    bc: tuple = (DVM_BC2D_WALL, DVM_BC2D_WALL, DVM_BC2D_WALL, DVM_BC2D_WALL)
+    acc_coeff: float = 1.0
+    # per wall (left, right, bottom, top): density, u, v, w, temperature
+    walls: tuple = ((1.0, 0.0, 0.0, 0.0, 1.0),) * 4
+    pi_mode: int = DVM_PI_REFERENCE
+    seed: int = 0
+
+    def to_params(self):
+        p = dvm_params()
+        p.geometry = self.geometry
+        p.nx_space, p.ny_space = self.nx_space, self.ny_space
+        p.coll_method, p.conv_method = self.iColl, self.iConv
+        p.num_repl = self.NRepl
+        p.samples_mode = self.samples_mode
+        p.pi_mode = self.pi_mode
+        for i in range(4):
+            p.bc[i] = int(self.bc[i])
+            for q in range(5):
+                p.wall[i][q] = float(self.walls[i][q])
+        p.samples_per_step = int(self.samples_per_step)
+        p.seed = int(self.seed) & 0xFFFFFFFFFFFFFFFF
+        p.dx, p.dy, p.dt, p.Kn = self.dx, self.dy, self.deltat, self.Kn
+        p.mass, p.omega, p.alpha, p.sigma = self.mass, self.omega, self.alpha, self.sigma
+        p.coln_rms, p.cdf_tolerance = self.ColnRMS, self.cdf_tolerance
+        p.acc_coeff = self.acc_coeff
+        return p
+
+
+def make_vgrid(grid):
+    """dvm_vgrid view of a physics.VelocityGrid (the arrays must outlive the call)."""
+    vg = dvm_vgrid()
+    vg.nx, vg.ny, vg.nz = grid.nx, grid.ny, grid.nz
+    vg.x, vg.y, vg.z = _dptr(grid.x), _dptr(grid.y), _dptr(grid.z)
+    return vg
+
+
+class PairList:
+    """A recorded collision list (dvm_pairlist) built from numpy arrays.
+
+    subs[q] = dict(glA=int32[n] or None, glB=..., rA=float64[n] or None, rB=...,
+                   r_phi=float64[n*NRepl], r_cos=float64[n*NRepl])
+    """
+
+    def __init__(self, subs):
+        self._keep = []
+        self.s = dvm_pairlist()
+        for q in range(3):
+            d = subs[q] if q < len(subs) else None
+            if d is None:
+                self.s.count[q] = 0
+                continue
+            n = len(d["r_phi"]) // max(1, d.get("num_repl", 1))
+            n = int(d.get("count", n))
+            self.s.count[q] = n
+            for key, conv, dt in (("glA", _iptr, np.int32), ("glB", _iptr, np.int32),
+                                  ("rA", _dptr, np.float64), ("rB", _dptr, np.float64),
+                                  ("r_phi", _dptr, np.float64), ("r_cos", _dptr, np.float64)):
+                arr = d.get(key)
+                if arr is None:
+                    continue
+                arr = np.ascontiguousarray(arr, dtype=dt)
+                self._keep.append(arr)
+                getattr(self.s, key)[q] = conv(arr)
+
+    def ref(self):
+        return C.byref(self.s)
+
+
+class DVMSolver:
+    """Host mirror of the reference time step, running on the GPU through the C ABI."""
+
+    def __init__(self, config, grid, lib=None):
+        self.lib = lib or load_library()
+        self.config = config
+        self.grid = grid
+        self._params = config.to_params()
+        vg = make_vgrid(grid)
+        ctx = C.c_void_p()
+        _check(self.lib.dvm_create(C.byref(self._params), C.byref(vg), C.byref(ctx)), "dvm_create")
+        self.ctx = ctx
+        self.ncells = config.nx_space * config.ny_space
+        self.nv = grid.nv
+        self.ntime = 0
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.dvm_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state ---------------------------------------------------------------------------
+    def initialize_dist_func(self, f):
+        """Uploads f[cells, nv] (phi and delta_phi) and computes its properties."""
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.ncells, self.nv)
+        _check(self.lib.dvm_upload_f(self.ctx, _dptr(f)), "dvm_upload_f")
+
+    def phi(self):
+        out = np.empty((self.ncells, self.nv))
+        _check(self.lib.dvm_download_f(self.ctx, _dptr(out)), "dvm_download_f")
+        return out
+
+    def properties(self):
+        out = np.empty((self.ncells, DVM_NPROP))
+        _check(self.lib.dvm_get_properties(self.ctx, _dptr(out)), "dvm_get_properties")
+        return out
+
+    def set_properties(self, props):
+        props = np.ascontiguousarray(props, dtype=np.float64).reshape(self.ncells, DVM_NPROP)
+        _check(self.lib.dvm_set_properties(self.ctx, _dptr(props)), "dvm_set_properties")
+
+    # -- the time step -------------------------------------------------------------------
+    def compute_collision_integral(self, step=None, pairs=None):
+        step = self.ntime if step is None else step
+        ref = pairs.ref() if pairs is not None else None
+        _check(self.lib.dvm_compute_collision_integral(self.ctx, C.c_uint64(step), ref),
+               "dvm_compute_collision_integral")
+
+    def compute_convection(self):
+        _check(self.lib.dvm_compute_convection(self.ctx), "dvm_compute_convection")
+
+    def calculate_physical_properties(self):
+        _check(self.lib.dvm_calculate_physical_properties(self.ctx),
+               "dvm_calculate_physical_properties")
+
+    def solve(self, nsteps):
+        """nsteps iterations of solve()'s loop (dvm_solver.f90:299-357)."""
+        _check(self.lib.dvm_step(self.ctx, C.c_uint64(self.ntime), int(nsteps)), "dvm_step")
+        self.ntime += nsteps
+
+    def collision_count(self):
+        v = C.c_int64()
+        _check(self.lib.dvm_last_collision_count(self.ctx, C.byref(v)), "dvm_last_collision_count")
+        return v.value
+
+    def error_word(self):
+        v = C.c_uint32()
+        _check(self.lib.dvm_get_error_word(self.ctx, C.byref(v)), "dvm_get_error_word")
+        return v.value
+
+    def synchronize(self):
+        _check(self.lib.dvm_synchronize(self.ctx), "dvm_synchronize")
+
+    # -- instrumentation -----------------------------------------------------------------
+    def profile(self, enable=True):
+        _check(self.lib.dvm_profile_enable(self.ctx, int(enable)), "dvm_profile_enable")
+
+    def profile_reset(self):
+        _check(self.lib.dvm_profile_reset(self.ctx), "dvm_profile_reset")
+
+    def profile_read(self):
+        out = {}
+        for k in range(DVM_K_COUNT):
+            ms, n = C.c_double(), C.c_int64()
+            _check(self.lib.dvm_profile_read(self.ctx, k, C.byref(ms), C.byref(n)),
+                   "dvm_profile_read")
+            out[KERNEL_NAMES[k]] = (ms.value, n.value)
+        return out
+
+    def launch_count(self):
+        v = C.c_int64()
+        _check(self.lib.dvm_launch_count(self.ctx, C.byref(v)), "dvm_launch_count")
+        return v.value
+
+    def time_steps(self, nsteps):
+        ms = C.c_double()
+        _check(self.lib.dvm_time_steps(self.ctx, C.c_uint64(self.ntime), int(nsteps),
+                                       C.byref(ms)), "dvm_time_steps")
+        self.ntime += nsteps
+        return ms.value
+
+    def flush_l2(self):
+        _check(self.lib.dvm_flush_l2(self.ctx), "dvm_flush_l2")

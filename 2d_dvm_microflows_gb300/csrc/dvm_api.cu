@@ -1,0 +1,603 @@
+// dvm_api.cu -- the C ABI (include/dvm_gpu.h): context, device buffers, launch sequence.
+//
+// The context owns every device buffer (f, f_conv, properties, CDFs, ghosts), like
+// phi / delta_phi / properties in initialize_solver (solver/dvm_solver.f90:55-64). Host
+// arrays passed in are only borrowed for the duration of the call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/dvm_gpu.h"
+#include "dvm_internal.h"
+
+using namespace dvm;
+
+struct dvm_ctx {
+  dvm_params p{};
+  GridInfo g{};
+  int ncells = 0;
+  double pi = kPiReference;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  // host copies of grid metadata
+  std::vector<double> hx, hy, hz, hbx, hby, hbz;
+  // device buffers
+  double* d_axes = nullptr;   // x, y, z, bx, by, bz
+  double* d_f = nullptr;
+  double* d_fconv = nullptr;
+  double* d_props = nullptr;
+  double* d_eq_pre = nullptr;
+  double* d_eq_cache = nullptr;
+  double* d_cum_eq = nullptr;
+  double* d_cum_dev = nullptr;
+  double* d_kin = nullptr;
+  int2* d_ref_eq = nullptr;
+  int2* d_ref_dev = nullptr;
+  CellPlan* d_plan = nullptr;
+  long long* d_chunk_off = nullptr;
+  long long* d_total_samples = nullptr;
+  double* d_ghost = nullptr;
+  uint32_t* d_err = nullptr;
+  double* d_flush = nullptr;
+  size_t flush_n = 0;
+  int wall_base[4] = {-1, -1, -1, -1};
+  int wall_entries = 0;
+  int collide_grid = 0;
+  // instrumentation
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Rec { int kid; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  double prof_ms[DVM_K_COUNT] = {0};
+  int64_t prof_n[DVM_K_COUNT] = {0};
+  int64_t launches = 0;
+};
+
+namespace {
+
+const char* kKernelNames[DVM_K_COUNT] = {"cdf_build", "collide_plan", "collide", "wall_flux",
+                                         "wall_ghost", "convect", "bc_1d", "moments"};
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return DVM_OK;
+  if (e == cudaErrorMemoryAllocation) return DVM_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return DVM_ERR_NODEVICE;
+  return DVM_ERR_CUDA;
+}
+
+cudaEvent_t take_event(dvm_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Runs one launch wrapper, counting it and, when profiling, bracketing it with events.
+template <typename F>
+int launch(dvm_ctx* c, int kid, F&& fn) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->profile) {
+    a = take_event(c);
+    b = take_event(c);
+    cudaEventRecord(a, c->stream);
+  }
+  cudaError_t e = fn();
+  if (c->profile) {
+    cudaEventRecord(b, c->stream);
+    c->recs.push_back({kid, a, b});
+  }
+  c->launches++;
+  return cuda_status(e);
+}
+
+void harvest(dvm_ctx* c) {
+  if (c->recs.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& r : c->recs) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) c->prof_ms[r.kid] += ms;
+    c->prof_n[r.kid]++;
+    c->ev_pool.push_back(r.a);
+    c->ev_pool.push_back(r.b);
+  }
+  c->recs.clear();
+}
+
+// compute_beta, grid/velocity_grid.f90:486-540
+void node_volumes(const std::vector<double>& a, std::vector<double>& b) {
+  const size_t n = a.size();
+  b.resize(n);
+  b[0] = a[1] - a[0];
+  b[n - 1] = a[n - 1] - a[n - 2];
+  for (size_t i = 1; i + 1 < n; ++i) b[i] = (a[i + 1] - a[i]) / 2.0 + (a[i] - a[i - 1]) / 2.0;
+}
+
+// find_zero_point, grid/velocity_grid.f90:653-689
+void zero_point(const std::vector<double>& a, int& zero, int& pos, int& neg) {
+  const int n = static_cast<int>(a.size());
+  if (a[0] > 0.0) { zero = -1; pos = 0; neg = -1; return; }
+  for (int i = 1; i < n; ++i) {
+    if (a[i] > 0.0) {
+      zero = i - 1; pos = i; neg = i - 1;
+      if (a[i - 1] > -kDoubleTol) neg = i - 2;
+      return;
+    }
+  }
+  zero = n; pos = n; neg = n - 1;
+}
+
+template <typename T>
+int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return DVM_OK;
+  return cuda_status(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
+}
+
+void release(dvm_ctx* c) {
+  if (!c) return;
+  harvest(c);
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  void* bufs[] = {c->d_axes, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
+                  c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
+                  c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+bool increasing(const double* a, int n) {
+  for (int i = 1; i < n; ++i)
+    if (!(a[i] > a[i - 1])) return false;
+  return true;
+}
+
+int validate(const dvm_params* p, const dvm_vgrid* vg) {
+  if (!p || !vg || !vg->x || !vg->y || !vg->z) return DVM_ERR_PARAM;
+  if (vg->nx < 3 || vg->ny < 3 || vg->nz < 3) return DVM_ERR_PARAM;
+  if (vg->nx > kMaxAxis || vg->ny > kMaxAxis || vg->nz > kMaxAxis) return DVM_ERR_PARAM;
+  if (!increasing(vg->x, vg->nx) || !increasing(vg->y, vg->ny) || !increasing(vg->z, vg->nz))
+    return DVM_ERR_PARAM;
+  if (p->nx_space < 1 || p->ny_space < 1) return DVM_ERR_PARAM;
+  if (p->coll_method != DVM_COLL_NONE && p->coll_method != DVM_COLL_FMC &&
+      p->coll_method != DVM_COLL_VR)
+    return DVM_ERR_PARAM;
+  if (p->conv_method != DVM_CONV_NONE && p->conv_method != DVM_CONV_UPWIND1) return DVM_ERR_PARAM;
+  if (p->num_repl < 1 || p->num_repl > kMaxRepl) return DVM_ERR_PARAM;
+  if (p->samples_mode != DVM_SAMPLES_FORMULA && p->samples_mode != DVM_SAMPLES_FIXED)
+    return DVM_ERR_PARAM;
+  if (p->samples_per_step < 0) return DVM_ERR_PARAM;
+  if (!(p->dt > 0.0) || !(p->Kn > 0.0) || !(p->mass > 0.0)) return DVM_ERR_PARAM;
+  if (p->coll_method != DVM_COLL_NONE && !(p->alpha > 0.0)) return DVM_ERR_PARAM;
+  if (p->samples_mode == DVM_SAMPLES_FORMULA && p->coll_method != DVM_COLL_NONE &&
+      !(p->coln_rms > 0.0))
+    return DVM_ERR_PARAM;
+  if (p->conv_method == DVM_CONV_UPWIND1) {
+    if (p->geometry == DVM_GEOM_2D) {
+      if (p->nx_space < 2 || p->ny_space < 2 || !(p->dx > 0.0) || !(p->dy > 0.0))
+        return DVM_ERR_PARAM;
+    } else if (p->geometry == DVM_GEOM_1D) {
+      if (p->nx_space < 3 || p->ny_space != 1 || !(p->dx > 0.0)) return DVM_ERR_PARAM;
+      for (int e = 0; e < 2; ++e)
+        if (p->bc[e] < DVM_BC1D_SPECULAR || p->bc[e] > DVM_BC1D_ZEROGRAD) return DVM_ERR_PARAM;
+    } else {
+      return DVM_ERR_PARAM;  // 0-D has no convection
+    }
+  }
+  if (p->geometry < DVM_GEOM_0D || p->geometry > DVM_GEOM_2D) return DVM_ERR_PARAM;
+  if (p->geometry == DVM_GEOM_0D && (p->nx_space != 1 || p->ny_space != 1)) {
+    // independent homogeneous cells are allowed (a batch of 0-D instances on one grid)
+    if (p->conv_method != DVM_CONV_NONE) return DVM_ERR_PARAM;
+  }
+  return DVM_OK;
+}
+
+CollParams coll_params(const dvm_ctx* c) {
+  CollParams cp;
+  cp.method = c->p.coll_method;
+  cp.samples_mode = c->p.samples_mode;
+  cp.samples_per_step = c->p.samples_per_step;
+  cp.num_repl = c->p.num_repl;
+  cp.mass = c->p.mass;
+  cp.omega = c->p.omega;
+  cp.alpha = c->p.alpha;
+  cp.sigma = c->p.sigma;
+  cp.dt = c->p.dt;
+  cp.Kn = c->p.Kn;
+  cp.coln_rms = c->p.coln_rms;
+  cp.cdf_tolerance = c->p.cdf_tolerance;
+  cp.pi = c->pi;
+  cp.seed = c->p.seed;
+  return cp;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dvm_abi_version(void) { return DVM_ABI_VERSION; }
+
+const char* dvm_strerror(int status) {
+  switch (status) {
+    case DVM_OK: return "ok";
+    case DVM_ERR_PARAM: return "invalid parameter";
+    case DVM_ERR_OOM: return "device memory allocation failed";
+    case DVM_ERR_CUDA: return "CUDA error";
+    case DVM_ERR_NUMERIC: return "device error word set";
+    case DVM_ERR_TIMEOUT: return "device wait timed out";
+    case DVM_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* dvm_kernel_name(int kid) {
+  return (kid >= 0 && kid < DVM_K_COUNT) ? kKernelNames[kid] : "unknown";
+}
+
+int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
+  if (!out) return DVM_ERR_PARAM;
+  *out = nullptr;
+  int st = validate(params, vg);
+  if (st) return st;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return DVM_ERR_NODEVICE;
+  dvm_ctx* c = new (std::nothrow) dvm_ctx();
+  if (!c) return DVM_ERR_OOM;
+  c->p = *params;
+  c->pi = (params->pi_mode == DVM_PI_EXACT) ? kPiExact : kPiReference;
+  c->ncells = params->nx_space * params->ny_space;
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if ((st = cuda_status(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)))) {
+    release(c);
+    return st;
+  }
+  c->hx.assign(vg->x, vg->x + vg->nx);
+  c->hy.assign(vg->y, vg->y + vg->ny);
+  c->hz.assign(vg->z, vg->z + vg->nz);
+  node_volumes(c->hx, c->hbx);
+  node_volumes(c->hy, c->hby);
+  node_volumes(c->hz, c->hbz);
+  GridInfo& g = c->g;
+  g.nx = vg->nx; g.ny = vg->ny; g.nz = vg->nz;
+  g.nv = g.nx * g.ny * g.nz;
+  g.xv_min = c->hx[0]; g.yv_min = c->hy[0]; g.zv_min = c->hz[0];
+  // create_velocity_grid, grid/velocity_grid.f90:293-313
+  g.xv_factor = static_cast<double>(g.nx - 1) / (c->hx[g.nx - 1] - g.xv_min);
+  g.yv_factor = static_cast<double>(g.ny - 1) / (c->hy[g.ny - 1] - g.yv_min);
+  g.zv_factor = static_cast<double>(g.nz - 1) / (c->hz[g.nz - 1] - g.zv_min);
+  zero_point(c->hx, g.i_zero, g.i_pos, g.i_neg);
+  zero_point(c->hy, g.j_zero, g.j_pos, g.j_neg);
+  // set_boundary_nodes :676-684 (SAVEd flags; one grid per context)
+  g.i_zero_flag = (g.i_zero != 0 && g.i_zero != g.i_neg && g.i_zero != g.i_pos && g.i_zero != g.nx - 1);
+  g.j_zero_flag = (g.j_zero != 0 && g.j_zero != g.j_neg && g.j_zero != g.j_pos && g.j_zero != g.ny - 1);
+  // find_min_max_beta3, grid/velocity_grid.f90:542-597
+  double mn = c->hbx[0] * c->hby[0] * c->hbz[0];
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) mn = std::min(mn, c->hbx[i] * c->hby[j] * c->hbz[k]);
+  g.beta3_min = mn;
+
+  const size_t C = c->ncells, nv = g.nv;
+  const size_t naxes = 2 * (g.nx + g.ny + g.nz);
+  if ((st = dalloc(&c->d_axes, naxes)) || (st = dalloc(&c->d_f, C * nv)) ||
+      (st = dalloc(&c->d_fconv, C * nv)) || (st = dalloc(&c->d_props, C * DVM_NPROP)) ||
+      (st = dalloc(&c->d_err, 1))) {
+    release(c);
+    return st;
+  }
+  if (params->coll_method != DVM_COLL_NONE) {
+    if ((st = dalloc(&c->d_eq_pre, C * (nv + 1))) || (st = dalloc(&c->d_eq_cache, C * 4)) ||
+        (st = dalloc(&c->d_cum_eq, C * (nv + 1))) || (st = dalloc(&c->d_cum_dev, C * (nv + 1))) ||
+        (st = dalloc(&c->d_kin, C * (nv + 1))) || (st = dalloc(&c->d_ref_eq, C * kNRef)) ||
+        (st = dalloc(&c->d_ref_dev, C * kNRef)) || (st = dalloc(&c->d_plan, C)) ||
+        (st = dalloc(&c->d_chunk_off, 3 * C + 1)) || (st = dalloc(&c->d_total_samples, 1))) {
+      release(c);
+      return st;
+    }
+  }
+  // axes on the device: x, y, z, bx, by, bz
+  std::vector<double> axes;
+  axes.insert(axes.end(), c->hx.begin(), c->hx.end());
+  axes.insert(axes.end(), c->hy.begin(), c->hy.end());
+  axes.insert(axes.end(), c->hz.begin(), c->hz.end());
+  axes.insert(axes.end(), c->hbx.begin(), c->hbx.end());
+  axes.insert(axes.end(), c->hby.begin(), c->hby.end());
+  axes.insert(axes.end(), c->hbz.begin(), c->hbz.end());
+  cudaMemcpy(c->d_axes, axes.data(), naxes * sizeof(double), cudaMemcpyHostToDevice);
+  g.x = c->d_axes;
+  g.y = g.x + g.nx;
+  g.z = g.y + g.ny;
+  g.bx = g.z + g.nz;
+  g.by = g.bx + g.nx;
+  g.bz = g.by + g.ny;
+  cudaMemset(c->d_err, 0, sizeof(uint32_t));
+  cudaMemset(c->d_f, 0, C * nv * sizeof(double));
+  cudaMemset(c->d_props, 0, C * DVM_NPROP * sizeof(double));
+  if (c->d_eq_pre) {
+    cudaMemset(c->d_eq_pre, 0, C * (nv + 1) * sizeof(double));
+    cudaMemset(c->d_eq_cache, 0, C * 4 * sizeof(double));
+  }
+  // 2-D wall ghost entries: left/right walls (if walls), bottom and top (always walls)
+  if (params->geometry == DVM_GEOM_2D && params->conv_method == DVM_CONV_UPWIND1) {
+    int n = 0;
+    const int NXS = params->nx_space, NYS = params->ny_space;
+    if (params->bc[DVM_WALL_LEFT] == DVM_BC2D_WALL) { c->wall_base[0] = n; n += NYS; }
+    if (params->bc[DVM_WALL_RIGHT] == DVM_BC2D_WALL) { c->wall_base[1] = n; n += NYS; }
+    c->wall_base[2] = n; n += NXS;
+    c->wall_base[3] = n; n += NXS;
+    c->wall_entries = n;
+    if ((st = dalloc(&c->d_ghost, static_cast<size_t>(n) * nv))) {
+      release(c);
+      return st;
+    }
+  }
+  if (params->coll_method != DVM_COLL_NONE) {
+    const int bps = collide_blocks_per_sm(collide_smem_bytes(g));
+    c->collide_grid = c->num_sms * bps;
+  }
+  if ((st = cuda_status(cudaDeviceSynchronize()))) {
+    release(c);
+    return st;
+  }
+  *out = c;
+  return DVM_OK;
+}
+
+int dvm_destroy(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  release(c);
+  return DVM_OK;
+}
+
+int dvm_num_velocity_points(const dvm_ctx* c) { return c ? c->g.nv : -1; }
+int dvm_num_cells(const dvm_ctx* c) { return c ? c->ncells : -1; }
+
+int dvm_upload_f(dvm_ctx* c, const double* f) {
+  if (!c || !f) return DVM_ERR_PARAM;
+  const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+  int st = cuda_status(cudaMemcpyAsync(c->d_f, f, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (st) return st;
+  // initialize_solver computes the properties of the initial state
+  st = dvm_calculate_physical_properties(c);
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int dvm_download_f(dvm_ctx* c, double* f) {
+  if (!c || !f) return DVM_ERR_PARAM;
+  const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+  int st = cuda_status(cudaMemcpyAsync(f, c->d_f, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int dvm_calculate_physical_properties(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err};
+  return launch(c, DVM_K_MOMENTS, [&] { return launch_moments(a, c->stream); });
+}
+
+int dvm_get_properties(dvm_ctx* c, double* props) {
+  if (!c || !props) return DVM_ERR_PARAM;
+  const size_t bytes = static_cast<size_t>(c->ncells) * DVM_NPROP * sizeof(double);
+  int st = cuda_status(cudaMemcpyAsync(props, c->d_props, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int dvm_set_properties(dvm_ctx* c, const double* props) {
+  if (!c || !props) return DVM_ERR_PARAM;
+  const size_t bytes = static_cast<size_t>(c->ncells) * DVM_NPROP * sizeof(double);
+  int st = cuda_status(cudaMemcpyAsync(c->d_props, props, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist* pairs) {
+  if (!c) return DVM_ERR_PARAM;
+  if (c->p.coll_method == DVM_COLL_NONE) return DVM_OK;
+  PairDev pd{};
+  std::vector<void*> tmp;
+  int st = DVM_OK;
+  if (pairs) {
+    pd.active = 1;
+    const int NR = c->p.num_repl;
+    const int nsub = (c->p.coll_method == DVM_COLL_VR) ? 3 : 1;
+    auto up = [&](const void* src, size_t bytes) -> void* {
+      if (!src || bytes == 0) return nullptr;
+      void* d = nullptr;
+      if (cudaMalloc(&d, bytes) != cudaSuccess) { st = DVM_ERR_OOM; return nullptr; }
+      tmp.push_back(d);
+      cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, c->stream);
+      return d;
+    };
+    for (int q = 0; q < 3; ++q) {
+      pd.count[q] = (q < nsub) ? pairs->count[q] : 0;
+      const size_t n = static_cast<size_t>(pd.count[q] > 0 ? pd.count[q] : 0);
+      if (n == 0) continue;
+      if (!pairs->glA[q] && !pairs->rA[q]) { st = DVM_ERR_PARAM; break; }
+      if (!pairs->r_phi[q] || !pairs->r_cos[q]) { st = DVM_ERR_PARAM; break; }
+      pd.glA[q] = static_cast<const int*>(up(pairs->glA[q], n * sizeof(int)));
+      pd.glB[q] = static_cast<const int*>(up(pairs->glB[q], n * sizeof(int)));
+      pd.rA[q] = static_cast<const double*>(up(pairs->rA[q], n * sizeof(double)));
+      pd.rB[q] = static_cast<const double*>(up(pairs->rB[q], n * sizeof(double)));
+      pd.rphi[q] = static_cast<const double*>(up(pairs->r_phi[q], n * NR * sizeof(double)));
+      pd.rcos[q] = static_cast<const double*>(up(pairs->r_cos[q], n * NR * sizeof(double)));
+      if (pairs->glA[q]) {
+        // node indices must lie on the grid
+        std::vector<int> chk(pairs->glA[q], pairs->glA[q] + n);
+        chk.insert(chk.end(), pairs->glB[q], pairs->glB[q] + n);
+        for (int v : chk)
+          if (v < 0 || v >= c->g.nv) { st = DVM_ERR_PARAM; break; }
+      }
+    }
+  }
+  if (!st) {
+    CdfArgs ca{};
+    ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
+    ca.f = c->d_f; ca.props = c->d_props; ca.eq_pre = c->d_eq_pre; ca.eq_cache = c->d_eq_cache;
+    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
+    ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan;
+    ca.pairs = pd; ca.err = c->d_err;
+    st = launch(c, DVM_K_CDF, [&] { return launch_cdf(ca, c->stream); });
+  }
+  if (!st)
+    st = launch(c, DVM_K_PLAN, [&] {
+      return launch_plan(c->ncells, c->d_plan, c->d_chunk_off, c->d_total_samples, c->stream);
+    });
+  if (!st) {
+    CollideArgs a{};
+    a.g = c->g; a.cp = coll_params(c); a.ncells = c->ncells;
+    a.step = static_cast<uint32_t>(step);
+    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
+    a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
+    a.chunk_off = c->d_chunk_off; a.pairs = pd; a.err = c->d_err;
+    st = launch(c, DVM_K_COLLIDE, [&] { return launch_collide(a, c->collide_grid, c->stream); });
+  }
+  if (!tmp.empty()) {
+    cudaStreamSynchronize(c->stream);
+    for (void* d : tmp) cudaFree(d);
+  }
+  return st;
+}
+
+int dvm_compute_convection(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  if (c->p.conv_method == DVM_CONV_NONE) return DVM_OK;
+  int st = DVM_OK;
+  if (c->p.geometry == DVM_GEOM_2D) {
+    WallArgs w{};
+    w.g = c->g; w.nxs = c->p.nx_space; w.nys = c->p.ny_space;
+    for (int s = 0; s < 4; ++s) w.base[s] = c->wall_base[s];
+    w.nentries = c->wall_entries;
+    w.acc = c->p.acc_coeff; w.mass = c->p.mass; w.pi = c->pi;
+    std::memcpy(w.wall, c->p.wall, sizeof(w.wall));
+    w.f = c->d_f; w.ghost = c->d_ghost; w.err = c->d_err;
+    st = launch(c, DVM_K_WALL, [&] { return launch_wall_flux(w, c->stream); });
+    if (!st) st = launch(c, DVM_K_GHOST, [&] { return launch_wall_specular(w, c->stream); });
+    if (!st) {
+      Convect2DArgs a{};
+      a.g = c->g; a.nxs = c->p.nx_space; a.nys = c->p.ny_space;
+      a.bc_left = c->p.bc[DVM_WALL_LEFT]; a.bc_right = c->p.bc[DVM_WALL_RIGHT];
+      for (int s = 0; s < 4; ++s) a.base[s] = c->wall_base[s];
+      a.xf = c->p.dt / c->p.dx; a.yf = c->p.dt / c->p.dy;
+      a.f = c->d_f; a.ghost = c->d_ghost; a.fconv = c->d_fconv;
+      st = launch(c, DVM_K_CONVECT, [&] { return launch_convect2d(a, c->ncells, c->stream); });
+    }
+  } else {
+    Convect1DArgs a{};
+    a.g = c->g; a.nxs = c->p.nx_space;
+    a.bc[0] = c->p.bc[DVM_WALL_LEFT]; a.bc[1] = c->p.bc[DVM_WALL_RIGHT];
+    a.factor = c->p.dt / c->p.dx;
+    a.acc = c->p.acc_coeff; a.mass = c->p.mass; a.pi = c->pi;
+    std::memcpy(a.wall[0], c->p.wall[DVM_WALL_LEFT], sizeof(a.wall[0]));
+    std::memcpy(a.wall[1], c->p.wall[DVM_WALL_RIGHT], sizeof(a.wall[1]));
+    a.f = c->d_f; a.fconv = c->d_fconv; a.err = c->d_err;
+    st = launch(c, DVM_K_CONVECT, [&] { return launch_convect1d(a, c->stream); });
+    if (!st) st = launch(c, DVM_K_BC1D, [&] { return launch_bc1d(a, c->stream); });
+  }
+  if (!st) std::swap(c->d_f, c->d_fconv);  // perform_dist_func_update (phi <- phi_conv)
+  return st;
+}
+
+int dvm_step(dvm_ctx* c, uint64_t first_step, int nsteps) {
+  if (!c || nsteps < 0) return DVM_ERR_PARAM;
+  for (int s = 0; s < nsteps; ++s) {
+    int st = dvm_compute_collision_integral(c, first_step + static_cast<uint64_t>(s), nullptr);
+    if (!st) st = dvm_compute_convection(c);
+    if (!st) st = dvm_calculate_physical_properties(c);
+    if (st) return st;
+  }
+  return DVM_OK;
+}
+
+int dvm_last_collision_count(dvm_ctx* c, int64_t* count) {
+  if (!c || !count) return DVM_ERR_PARAM;
+  if (!c->d_total_samples) { *count = 0; return DVM_OK; }
+  long long v = 0;
+  int st = cuda_status(cudaMemcpyAsync(&v, c->d_total_samples, sizeof(v), cudaMemcpyDeviceToHost,
+                                       c->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  *count = v;
+  return st;
+}
+
+int dvm_synchronize(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+int dvm_get_error_word(dvm_ctx* c, uint32_t* word) {
+  if (!c || !word) return DVM_ERR_PARAM;
+  uint32_t v = 0;
+  int st = cuda_status(cudaMemcpyAsync(&v, c->d_err, sizeof(v), cudaMemcpyDeviceToHost, c->stream));
+  if (!st) st = cuda_status(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  *word = v;
+  return st;
+}
+
+int dvm_profile_enable(dvm_ctx* c, int enable) {
+  if (!c) return DVM_ERR_PARAM;
+  c->profile = enable != 0;
+  return DVM_OK;
+}
+
+int dvm_profile_read(dvm_ctx* c, int kid, double* total_ms, int64_t* launches) {
+  if (!c || kid < 0 || kid >= DVM_K_COUNT) return DVM_ERR_PARAM;
+  harvest(c);
+  if (total_ms) *total_ms = c->prof_ms[kid];
+  if (launches) *launches = c->prof_n[kid];
+  return DVM_OK;
+}
+
+int dvm_profile_reset(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  harvest(c);
+  for (int k = 0; k < DVM_K_COUNT; ++k) { c->prof_ms[k] = 0.0; c->prof_n[k] = 0; }
+  return DVM_OK;
+}
+
+int dvm_launch_count(dvm_ctx* c, int64_t* launches) {
+  if (!c || !launches) return DVM_ERR_PARAM;
+  *launches = c->launches;
+  return DVM_OK;
+}
+
+int dvm_time_steps(dvm_ctx* c, uint64_t first_step, int nsteps, double* ms) {
+  if (!c || !ms) return DVM_ERR_PARAM;
+  cudaEvent_t a = take_event(c), b = take_event(c);
+  cudaEventRecord(a, c->stream);
+  int st = dvm_step(c, first_step, nsteps);
+  cudaEventRecord(b, c->stream);
+  if (!st) st = cuda_status(cudaEventSynchronize(b));
+  float t = 0.f;
+  if (!st) st = cuda_status(cudaEventElapsedTime(&t, a, b));
+  *ms = t;
+  c->ev_pool.push_back(a);
+  c->ev_pool.push_back(b);
+  return st;
+}
+
+int dvm_flush_l2(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  if (!c->d_flush) {
+    c->flush_n = (size_t(256) << 20) / sizeof(double);  // 256 MiB > 129 MB of L2
+    int st = dalloc(&c->d_flush, c->flush_n);
+    if (st) return st;
+  }
+  return cuda_status(launch_flush(c->d_flush, c->flush_n, c->stream));
+}
+
+}  // extern "C"

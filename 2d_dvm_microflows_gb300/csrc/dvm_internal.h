@@ -1,0 +1,137 @@
+// dvm_internal.h -- argument records shared by the kernel TU and the C-ABI TU.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dvm_device.cuh"
+
+namespace dvm {
+
+constexpr int kCollideChunk = 256;  // samples per chunk = threads per collide CTA
+
+// Samples and depletion factor of each sub-integral of one cell-step
+// (variance_reduction.f90:669-683, 822-835, 967-981; full_mc.f90:330-331).
+struct CellPlan {
+  long long num[3];
+  double factor[3];
+};
+
+// A recorded collision list on the device (dvm_pairlist).
+struct PairDev {
+  int active;
+  long long count[3];
+  const int* glA[3];
+  const int* glB[3];
+  const double* rA[3];
+  const double* rB[3];
+  const double* rphi[3];
+  const double* rcos[3];
+};
+
+// Scalars every collision kernel needs.
+struct CollParams {
+  int method;          // DVM_COLL_VR or DVM_COLL_FMC
+  int samples_mode;
+  long long samples_per_step;
+  int num_repl;
+  double mass, omega, alpha, sigma, dt, Kn, coln_rms, cdf_tolerance;
+  double pi;
+  uint64_t seed;
+};
+
+struct CdfArgs {
+  GridInfo g;
+  CollParams cp;
+  int ncells;
+  const double* f;          // [C][nv]
+  const double* props;      // [C][DVM_NPROP]
+  double* eq_pre;           // [C][nv+1] cached equilibrium prefix sums
+  double* eq_cache;         // [C][4]  dens, u, v, temp of the cached equilibrium
+  double* cum_eq;           // [C][nv+1]
+  double* cum_dev;          // [C][nv+1] (FMC: cumulative |f|)
+  double* kin;              // [C][nv+1] (VR: f - f_eq; FMC: f)
+  int2* ref_eq;             // [C][1000]
+  int2* ref_dev;            // [C][1000]
+  CellPlan* plan;           // [C]
+  PairDev pairs;
+  uint32_t* err;
+};
+
+struct CollideArgs {
+  GridInfo g;
+  CollParams cp;
+  int ncells;
+  uint32_t step;
+  double* f;
+  const double* cum_eq;
+  const double* cum_dev;
+  const double* kin;
+  const int2* ref_eq;
+  const int2* ref_dev;
+  const CellPlan* plan;
+  const long long* chunk_off;  // [3*C + 1]
+  PairDev pairs;
+  uint32_t* err;
+};
+
+// 2-D wall ghost slabs: one per (wall side, position along the wall).
+struct WallArgs {
+  GridInfo g;
+  int nxs, nys;
+  int base[4];              // first entry of each side, -1 if that side has no wall ghost
+  int nentries;
+  double acc, mass, pi;
+  double wall[4][5];
+  const double* f;
+  double* ghost;            // [nentries][nv]
+  uint32_t* err;
+};
+
+struct Convect2DArgs {
+  GridInfo g;
+  int nxs, nys;
+  int bc_left, bc_right;
+  int base[4];
+  double xf, yf;            // dt/dx, dt/dy
+  const double* f;
+  const double* ghost;
+  double* fconv;
+};
+
+struct Convect1DArgs {
+  GridInfo g;
+  int nxs;
+  int bc[2];
+  double factor;            // dt/dx
+  double acc, mass, pi;
+  double wall[2][5];
+  const double* f;
+  double* fconv;
+  uint32_t* err;
+};
+
+struct MomentArgs {
+  GridInfo g;
+  int ncells;
+  double mass;
+  const double* f;
+  double* props;
+  uint32_t* err;
+};
+
+// Launch wrappers (dvm_kernels.cu). Each returns the cudaGetLastError of its launch.
+cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s);
+cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
+                        long long* total_samples, cudaStream_t s);
+cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s);
+cudaError_t launch_wall_specular(const WallArgs& a, cudaStream_t s);
+cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s);
+cudaError_t launch_convect1d(const Convect1DArgs& a, cudaStream_t s);
+cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s);
+cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s);
+cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s);
+int collide_blocks_per_sm(size_t smem);
+size_t collide_smem_bytes(const GridInfo& g);
+
+}  // namespace dvm

@@ -1,0 +1,361 @@
+"""Benchmark of the DVM time step on GB300.
+
+Workload: the 1-D normal shock -- 200 cells, 32^3 uniform velocity grid on [-9, 9],
+variable-hard-sphere gas (omega = 0.81), Mach 3.0 Rankine-Hugoniot end states joined by a
+tanh profile 10 upstream mean free paths wide, inflow Maxwellian conditions at both ends,
+variance-reduced Monte Carlo collisions with 2e5 samples per cell-step, FP64. A step is
+one solve() iteration: collisions in every cell, convection with the end conditions, and
+the moments.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. `value` is device-timed collisions/s with f resident in HBM (L2
+flushed between timed steps); `e2e` runs the same steps through the C ABI with the
+distribution in pinned host memory, copied in and out every step.
+`--impl reference` times the CPU restatement of the reference's step (the Fortran
+reference cannot be built here) on the host cores.
+"""
+import argparse
+import ctypes as C
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+NCELLS = 200
+NGRID = 32
+VMAX = 9.0
+MACH = 3.0
+WIDTH = 10.0
+DX = 0.5
+DT = 0.05
+OMEGA = 0.81
+SAMPLES = 200000
+SEED = 20261203
+BYTES_PER_SAMPLE = 8 * (2 + 2 * 16)  # 2 partner reads + 16 atomic read-modify-writes
+
+
+def workload_config(pkg):
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(NGRID, -VMAX, VMAX)
+    f0, up, dn = ph.shock_profile(g, NCELLS, DX, MACH, WIDTH)
+    walls = ((dn["n"], dn["u"], 0.0, 0.0, dn["T"]), (up["n"], up["u"], 0.0, 0.0, up["T"]),
+             (1.0, 0.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 0.0, 1.0))
+    mol = ph.molecule("Ar", ph.CSECTION_VHS)
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=NCELLS, dx=DX, deltat=DT, Kn=1.0,
+                        mass=mol["mass"], omega=mol["omega"], alpha=mol["alpha"],
+                        sigma=ph.cross_section(mol, ph.CSECTION_BIRD),
+                        iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                        samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=SAMPLES,
+                        bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), walls=walls,
+                        seed=SEED)
+    return cfg, g, f0
+
+
+def config_record(impl):
+    return {
+        "workload": "1-D normal shock: %d cells x %d^3 velocity grid on [-%g,%g], VHS omega=%g, "
+                    "Mach %g, tanh profile %g mfp, inflow Maxwellian ends, VR collisions "
+                    "%d samples/cell-step, FP64" % (NCELLS, NGRID, VMAX, VMAX, OMEGA, MACH,
+                                                    WIDTH, SAMPLES),
+        "cells": NCELLS, "velocity_nodes": NGRID ** 3, "samples_per_cell_step": SAMPLES,
+        "dt": DT, "dx": DX, "l2": "flushed (256 MiB write) between timed steps" if impl == "gpu"
+        else "n/a (CPU)",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def dist_reduce(dist, value, op):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# -----------------------------------------------------------------------------------------
+def cpu_rate(oracle, pkg, cfg, g, f0, threads, budget_s, cells_cap=NCELLS):
+    """Collisions/s of the CPU restatement on a bounded sample of the workload: the first
+    n cells of the shock (n sized to the time budget), full steps (collisions, convection,
+    moments) run with `threads` OpenMP threads."""
+    import dataclasses
+    probe_cells = min(8, cells_cap)
+    sub = dataclasses.replace(cfg, nx_space=probe_cells)
+    s = oracle.OracleSolver(sub, g, threads=threads)
+    s.initialize_dist_func(f0[:probe_cells])
+    t0 = time.perf_counter()
+    s.solve(1)
+    t_probe = time.perf_counter() - t0
+    per_cell = t_probe / probe_cells
+    n = int(max(probe_cells, min(cells_cap, budget_s / max(per_cell, 1e-9))))
+    if n > probe_cells:
+        sub = dataclasses.replace(cfg, nx_space=n)
+        s = oracle.OracleSolver(sub, g, threads=threads)
+        s.initialize_dist_func(f0[:n])
+    t0 = time.perf_counter()
+    s.solve(1)
+    dt = time.perf_counter() - t0
+    colls = s.collision_count()
+    return colls / dt, n, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    dist = dist_init(ws)
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    O.build()
+    pkg = importlib.import_module("2d_dvm_microflows_gb300")
+    cfg, g, f0 = workload_config(pkg)
+    threads = O.lib().orc_max_threads()
+    # one untimed step to size the per-step sample (cells) to ~20 s per step at most
+    rate, ncells, _ = cpu_rate(O, pkg, cfg, g, f0, threads, budget_s=20.0)
+    import dataclasses
+    sub = dataclasses.replace(cfg, nx_space=ncells)
+    s = O.OracleSolver(sub, g, threads=threads)
+    s.initialize_dist_func(f0[:ncells])
+    for _ in range(args.warmup):
+        s.solve(1)
+    colls, t_total = 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s.solve(1)
+        t_total += time.perf_counter() - t0
+        colls += s.collision_count()
+    value = colls / t_total
+    sample = ("first %d of %d cells of the workload per step (full steps: collisions, "
+              "convection, moments), %d timed steps" % (ncells, NCELLS, args.steps))
+    line = {
+        "impl": "reference", "metric": "MC collisions/s", "value": value, "unit": "collisions/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-H tanh shock state)",
+        "config": config_record("cpu"),
+        "cpu_baseline": {"value": value, "unit": "collisions/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "collisions/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference step (oracle/), OpenMP over cells; the "
+                "Fortran reference has no compiler in this image",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    ws, rank, local = dist_env()
+    if ws > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = dist_init(ws)
+    import torch
+    pkg = importlib.import_module("2d_dvm_microflows_gb300")
+    cfg, g, f0 = workload_config(pkg)
+    s = pkg.DVMSolver(cfg, g)
+    s.initialize_dist_func(f0)
+    nv = g.nv
+    # warm-up
+    for _ in range(args.warmup):
+        s.solve(1)
+    s.synchronize()
+    s.profile_reset()
+    s.profile(True)
+    launches0 = s.launch_count()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
+    dist_barrier(dist)
+    clocks.start()
+    t_dev, colls = 0.0, 0
+    for _ in range(args.steps):
+        s.profile(False)
+        s.flush_l2()
+        s.synchronize()
+        s.profile(True)
+        t_dev += s.time_steps(1)
+        colls += s.collision_count()
+    s.synchronize()
+    clk = clocks.stop()
+    prof = s.profile_read()
+    launches = s.launch_count() - launches0
+    s.profile(False)
+    dist_barrier(dist)
+    t_max = dist_reduce(dist, t_dev, "max")
+    colls_all = dist_reduce(dist, colls, "sum")
+    value = colls_all / (t_max * 1e-3)
+
+    # end to end through the C ABI: f in pinned host memory, copied in and out every step
+    host = torch.empty((NCELLS, nv), dtype=torch.float64, pin_memory=True)
+    hnp = host.numpy()
+    hnp[:] = s.phi()
+    ptr = hnp.ctypes.data_as(C.POINTER(C.c_double))
+    lib = s.lib
+    dist_barrier(dist)
+    t0 = time.perf_counter()
+    e2e_colls = 0
+    for k in range(args.steps):
+        if lib.dvm_upload_f(s.ctx, ptr):
+            raise RuntimeError("upload failed")
+        if lib.dvm_step(s.ctx, C.c_uint64(10000 + k), 1):
+            raise RuntimeError("step failed")
+        if lib.dvm_download_f(s.ctx, ptr):
+            raise RuntimeError("download failed")
+        e2e_colls += cfg.samples_per_step * NCELLS
+    t_e2e = time.perf_counter() - t0
+    t_e2e = dist_reduce(dist, t_e2e, "max")
+    e2e_value = dist_reduce(dist, e2e_colls, "sum") / t_e2e
+    err = s.error_word()
+
+    if rank != 0:
+        return 0
+    # roofline of the dominant kernel (collide), from the live event timings
+    ms_coll, n_coll = prof["collide"]
+    samples_per_launch = SAMPLES * NCELLS
+    t_launch = ms_coll / max(n_coll, 1) * 1e-3
+    achieved = samples_per_launch * BYTES_PER_SAMPLE / t_launch / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tp = os.path.join(REPO, "profiles", "collide_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            traffic = json.load(fh).get("bytes_per_launch")
+    kernels = {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items() if v[1]}
+    line = {
+        "metric": "MC collisions/s", "value": value, "unit": "collisions/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded R-H tanh shock state)", "config": config_record("gpu"),
+        "cell_updates_per_s": NCELLS * args.steps * ws / (t_max * 1e-3),
+        "roofline": {"bound": "hbm", "kernel": "collide", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_sample": BYTES_PER_SAMPLE},
+        "kernels": kernels,
+        "e2e": {"value": e2e_value, "unit": "collisions/s",
+                "h2d_bytes_per_step": NCELLS * nv * 8, "d2h_bytes_per_step": NCELLS * nv * 8},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "error_word": err,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle as O
+        O.build()
+        rate, ncells, dt = cpu_rate(O, pkg, cfg, g, f0, 1, budget_s=12.0)
+        line["cpu_baseline"] = {"value": rate, "unit": "collisions/s", "cores": 1, "kind": "port",
+                                "sample": "one full step of the first %d of %d cells, single "
+                                          "thread (%.1f s)" % (ncells, NCELLS, dt)}
+    print(json.dumps(line))
+    s.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gpu":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

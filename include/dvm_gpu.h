@@ -1,0 +1,206 @@
+/*
+ * dvm_gpu.h -- C ABI of the GB300 (sm_103a) DVM time step.
+ *
+ * The time step of the discrete-velocity Boltzmann solver is
+ *   collisions (Monte Carlo, variance reduced or full)  -> convection (first-order
+ *   upwind, with wall / inflow boundary conditions)     -> per-cell moments.
+ * Every entry point takes plain pointers, sizes and POD structs so that a Fortran
+ * host can bind it with iso_c_binding (value scalars, assumed-size arrays), the same
+ * way the reference binds GSL (utils/random_number_generation.f90:46-80).
+ *
+ * Reference: aarthisekaran11/2D_DVM_microflows, software/trunk/src (2-D code) and
+ * software/code_versions/grid_ref_code/src (1-D code). File:line citations below are
+ * relative to software/trunk/src unless they say grid_ref.
+ *
+ * Layout: f[cell][v], v = i + Nx*(j + Ny*k), cell = nx + nx_space*ny (0-based), the
+ * column-major order of DistFuncType%value(i,j,k) (grid/velocity_grid.f90:714-726) and of
+ * phi(nx,ny) (solver/dvm_solver.f90:55-64).
+ *
+ * Every call returns an int status (DVM_OK = 0). Calls are ordered on the context's CUDA
+ * stream; the ones that return host data synchronise.
+ */
+#ifndef DVM_GPU_H
+#define DVM_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DVM_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------------------ */
+enum {
+  DVM_OK = 0,
+  DVM_ERR_PARAM = 1,      /* invalid parameter (the reference prints and stops)     */
+  DVM_ERR_OOM = 2,        /* device allocation failed                                */
+  DVM_ERR_CUDA = 3,       /* CUDA runtime / launch error                             */
+  DVM_ERR_NUMERIC = 4,    /* device error word set (see dvm_get_error_word)          */
+  DVM_ERR_TIMEOUT = 5,    /* a bounded device wait ran out                           */
+  DVM_ERR_NODEVICE = 6    /* no CUDA device                                          */
+};
+
+/* Bits of the device error word. */
+enum {
+  DVM_EW_SEARCH = 1,      /* CDF inversion left its bucket (reference would loop)    */
+  DVM_EW_REMAP = 2,       /* remap found no exterior node (remapping.f90:348 stops)  */
+  DVM_EW_NONFINITE = 4,   /* non-finite moment                                       */
+  DVM_EW_NEGDENS = 8      /* non-positive cell density                               */
+};
+
+/* iColl (collisions/collision_integral.f90:35-38) */
+enum { DVM_COLL_NONE = 0, DVM_COLL_FMC = 2, DVM_COLL_VR = 3 };
+/* iConv (convection/convection.f90:34-35) */
+enum { DVM_CONV_NONE = 0, DVM_CONV_UPWIND1 = 1 };
+/* physical-space dimensionality */
+enum { DVM_GEOM_0D = 0, DVM_GEOM_1D = 1, DVM_GEOM_2D = 2 };
+/* 2-D wall condition numbering (conditions/boundary_conditions.f90:56-59) */
+enum { DVM_BC2D_WALL = 1, DVM_BC2D_INOUT = 2, DVM_BC2D_ZEROGRAD = 3, DVM_BC2D_COUETTE = 4 };
+/* 1-D end condition numbering (grid_ref conditions/boundary_conditions.f90:43-46) */
+enum { DVM_BC1D_SPECULAR = 1, DVM_BC1D_DIFFUSE = 2, DVM_BC1D_INOUT = 3, DVM_BC1D_ZEROGRAD = 4 };
+/* pi used by Maxwellian normalisation and scattering azimuth (utils/constants.f90:30) */
+enum { DVM_PI_REFERENCE = 0, DVM_PI_EXACT = 1 };
+/* how many samples a cell-step draws */
+enum { DVM_SAMPLES_FORMULA = 0,   /* compute_num_coll_pairs, collision_utilities.f90:106-140 */
+       DVM_SAMPLES_FIXED = 1 };   /* samples_per_step total per cell-step, split over the
+                                     sub-integrals in proportion to densA*densB             */
+/* wall index in dvm_params.bc / .wall */
+enum { DVM_WALL_LEFT = 0, DVM_WALL_RIGHT = 1, DVM_WALL_BOTTOM = 2, DVM_WALL_TOP = 3 };
+/* wall property index in dvm_params.wall[w][...] */
+enum { DVM_WP_DENS = 0, DVM_WP_U = 1, DVM_WP_V = 2, DVM_WP_W = 3, DVM_WP_TEMP = 4 };
+
+/* Per-cell property record (dist_funcs/physical_props.f90:41-69, monatomic subset). */
+enum {
+  DVM_P_DENS = 0, DVM_P_U = 1, DVM_P_V = 2, DVM_P_W = 3,
+  DVM_P_TEMP = 4,          /* translational temperature, compute_temperature :1033-1087 */
+  DVM_P_SPECIES_TEMP = 5,  /* compute_overall_temperature :1428-1457 (monatomic)        */
+  DVM_P_AVG_SPEED = 6,     /* compute_avg_speed :1459-1507                               */
+  DVM_P_PRESSURE = 7,      /* 0.5*n*T :357                                               */
+  DVM_P_QX = 8, DVM_P_QY = 9, DVM_P_QZ = 10,            /* compute_heat_flux :1914-1986   */
+  DVM_P_TXX = 11, DVM_P_TYY = 12, DVM_P_TZZ = 13,       /* compute_viscous_stress          */
+  DVM_P_TXY = 14, DVM_P_TXZ = 15, DVM_P_TYZ = 16,       /*   :1988-2071                    */
+  DVM_NPROP = 20
+};
+
+/* Velocity grid: node coordinates per axis (grid/velocity_grid.f90:35-73). The node
+ * volumes (compute_beta :486-540), zero/neg/pos indices (find_zero_point :653-689) and
+ * beta3_min (:542-597) are derived from these by dvm_create. */
+typedef struct dvm_vgrid {
+  int32_t nx, ny, nz;
+  const double* x;   /* [nx], increasing */
+  const double* y;   /* [ny] */
+  const double* z;   /* [nz] */
+} dvm_vgrid;
+
+/* Solver parameters; one field per input-deck key the step reads
+ * (input_output/read_input_2D.f90:75-777). Single species (every supported
+ * configuration is monatomic). */
+typedef struct dvm_params {
+  int32_t geometry;        /* DVM_GEOM_*                                           */
+  int32_t nx_space;        /* cells in x (1 for 0-D)                               */
+  int32_t ny_space;        /* cells in y (1 for 0-D and 1-D)                       */
+  int32_t coll_method;     /* iColl                                                */
+  int32_t conv_method;     /* iConv                                                */
+  int32_t num_repl;        /* NRepl (replenishing_collisions.f90:134-354)          */
+  int32_t samples_mode;    /* DVM_SAMPLES_*                                        */
+  int32_t pi_mode;         /* DVM_PI_*                                             */
+  int32_t bc[4];           /* per wall, DVM_BC2D_* (2-D) or DVM_BC1D_* (1-D)       */
+  int64_t samples_per_step;/* per cell-step, DVM_SAMPLES_FIXED                     */
+  uint64_t seed;           /* Philox key                                           */
+  double dx, dy;           /* cell sizes (mean free paths)                         */
+  double dt;               /* deltat (solver/time_stepping.f90)                    */
+  double Kn;               /* Knudsen number (solver/scaling.f90)                  */
+  double mass;             /* scaled molecular mass                                */
+  double omega;            /* VHS viscosity exponent                               */
+  double alpha;            /* VSS scattering exponent (1 = isotropic)              */
+  double sigma;            /* cross-section from calculate_cross_section           */
+                           /* (solver/scaling.f90:163-201)                          */
+  double coln_rms;         /* ColnRMS (collision_integral.f90:79-96)               */
+  double cdf_tolerance;    /* variance_reduction.f90:316-322                       */
+  double acc_coeff;        /* accommodation coefficient                            */
+  double wall[4][5];       /* per wall: density, u, v, w, temperature              */
+} dvm_params;
+
+/* Recorded collision list for one cell-step (same list applied to every cell).
+ * Sub-integral s: VR uses s = 0 (eq x dev), 1 (dev x eq), 2 (dev x dev)
+ * (variance_reduction.f90:669-816, 822-961, 967-1116); FMC uses s = 0 only.
+ * Partners are given either as 0-based node indices (glA/glB) or as the uniforms fed
+ * to pick_collision_partner (rA/rB, collision_utilities.f90:142-186); r_phi/r_cos hold
+ * num_repl values per sample, in the order pick_random_velocity_on_sphere draws them
+ * (azimuth first, collision_utilities.f90:308 then :332). */
+typedef struct dvm_pairlist {
+  int64_t count[3];
+  const int32_t* glA[3];
+  const int32_t* glB[3];
+  const double* rA[3];
+  const double* rB[3];
+  const double* r_phi[3];  /* [count * num_repl] */
+  const double* r_cos[3];  /* [count * num_repl] */
+} dvm_pairlist;
+
+typedef struct dvm_ctx dvm_ctx;
+
+/* ---- lifetime ----------------------------------------------------------------------- */
+/* Replaces initialize_solver's allocations (solver/dvm_solver.f90:55-64), create_velocity_grid
+ * (grid/velocity_grid.f90:271-350) and create_collision_integral (collision_integral.f90:98). */
+int dvm_create(const dvm_params* params, const dvm_vgrid* grid, dvm_ctx** out);
+/* Replaces destroy_solver (solver/dvm_solver.f90:371). */
+int dvm_destroy(dvm_ctx* ctx);
+const char* dvm_strerror(int status);
+int dvm_abi_version(void);
+
+/* ---- state -------------------------------------------------------------------------- */
+/* f[cells][Nv] host array, copied to the device (phi and delta_phi both take it). */
+int dvm_upload_f(dvm_ctx* ctx, const double* f);
+int dvm_download_f(dvm_ctx* ctx, double* f);
+int dvm_num_velocity_points(const dvm_ctx* ctx);
+int dvm_num_cells(const dvm_ctx* ctx);
+
+/* ---- the hot path ------------------------------------------------------------------- */
+/* compute_collision_integral for every cell (collisions/collision_integral.f90:163-274,
+ * called per cell from solver/dvm_solver.f90:305-315). Uses the properties held by the
+ * context (the last dvm_calculate_physical_properties or dvm_set_properties). step is the
+ * Philox counter; pairs != NULL replays a recorded list instead of drawing. */
+int dvm_compute_collision_integral(dvm_ctx* ctx, uint64_t step, const dvm_pairlist* pairs);
+/* compute_convection with its boundary conditions (convection/convection.f90:69-117,
+ * conditions/boundary_conditions.f90:537-1656; 1-D: grid_ref convection.f90:111-256 and
+ * grid_ref conditions/boundary_conditions.f90:319-913). */
+int dvm_compute_convection(dvm_ctx* ctx);
+/* calculate_physical_properties per cell (dist_funcs/physical_props.f90:285-485) plus heat
+ * flux and stress (:1914-2071), on the device; results stay on the device. */
+int dvm_calculate_physical_properties(dvm_ctx* ctx);
+/* props[cells][DVM_NPROP] */
+int dvm_get_properties(dvm_ctx* ctx, double* props);
+int dvm_set_properties(dvm_ctx* ctx, const double* props);
+/* One solve() iteration per step: collisions, convection, moments
+ * (solver/dvm_solver.f90:299-357). first_step is the Philox step counter of the first. */
+int dvm_step(dvm_ctx* ctx, uint64_t first_step, int nsteps);
+/* Collision samples drawn by the last collision call, summed over cells (tot_colls). */
+int dvm_last_collision_count(dvm_ctx* ctx, int64_t* count);
+
+/* ---- errors, synchronisation, instrumentation -------------------------------------- */
+int dvm_synchronize(dvm_ctx* ctx);
+/* Reads and clears the device error word (DVM_EW_* bits). */
+int dvm_get_error_word(dvm_ctx* ctx, uint32_t* word);
+/* When enabled, every kernel launch is bracketed by CUDA events on the context's stream. */
+int dvm_profile_enable(dvm_ctx* ctx, int enable);
+/* kernel ids */
+enum { DVM_K_CDF = 0, DVM_K_PLAN = 1, DVM_K_COLLIDE = 2, DVM_K_WALL = 3, DVM_K_GHOST = 4,
+       DVM_K_CONVECT = 5, DVM_K_BC1D = 6, DVM_K_MOMENTS = 7, DVM_K_COUNT = 8 };
+const char* dvm_kernel_name(int kernel_id);
+/* Sums the event-timed durations (ms) and launch counts since the last reset; synchronises. */
+int dvm_profile_read(dvm_ctx* ctx, int kernel_id, double* total_ms, int64_t* launches);
+int dvm_profile_reset(dvm_ctx* ctx);
+/* Total kernels this context launched (profiled or not). */
+int dvm_launch_count(dvm_ctx* ctx, int64_t* launches);
+/* Events around nsteps of dvm_step on the context's stream: elapsed device time in ms. */
+int dvm_time_steps(dvm_ctx* ctx, uint64_t first_step, int nsteps, double* ms);
+/* Writes a buffer of bytes > L2 on the context's stream (cold-cache timing). */
+int dvm_flush_l2(dvm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DVM_GPU_H */

@@ -1,0 +1,308 @@
+"""GPU kernels (through the C ABI) against the CPU restatement and the golden fixtures.
+
+FP64 bar: post-step distributions agree within REL = 1e-12 of max|f| (the tolerance the
+specification states for a shared recorded pair list); moments within 1e-12 relative.
+Size-independent properties (conservation) are checked at the full benchmark sizes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "golden_v1.npz")
+REL = 1.0e-12
+
+
+def rel_err(a, b):
+    scale = max(np.abs(b).max(), 1e-300)
+    return np.abs(a - b).max() / scale
+
+
+def pair_solvers(pkg, oracle, g, f0, **kw):
+    cfg = pkg.DVMConfig(**kw)
+    gpu = pkg.DVMSolver(cfg, g)
+    cpu = oracle.OracleSolver(cfg, g)
+    gpu.initialize_dist_func(f0)
+    cpu.initialize_dist_func(f0)
+    return gpu, cpu
+
+
+def random_pairs(rng, nv, counts, nrepl, nodes=True):
+    subs = []
+    for n in counts:
+        d = {"count": n, "num_repl": nrepl, "r_phi": rng.random(n * nrepl),
+             "r_cos": rng.random(n * nrepl)}
+        if nodes:
+            d["glA"] = rng.integers(0, nv, n).astype(np.int32)
+            d["glB"] = rng.integers(0, nv, n).astype(np.int32)
+        else:
+            d["rA"], d["rB"] = rng.random(n), rng.random(n)
+        subs.append(d)
+    return subs
+
+
+# ---------------------------------------------------------------------------------------
+def test_moments_match(gpulib, pkg, oracle):
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(14, -5.0, 5.0)
+    rng = np.random.default_rng(0)
+    f0 = np.stack([ph.bimodal(g, u1=0.8 + 0.1 * c, T2=2.0 + c) * (1 + 0.01 * rng.random(g.nv))
+                   for c in range(6)])
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, nx_space=6, iColl=pkg.DVM_COLL_NONE)
+    pg, pc = gpu.properties(), cpu.properties()
+    for q in range(17):
+        scale = max(np.abs(pc[:, q]).max(), 1e-12)
+        assert np.abs(pg[:, q] - pc[:, q]).max() <= 1e-12 * scale, pkg.PROP_NAMES[q]
+
+
+@pytest.mark.parametrize("nodes", [True, False])
+@pytest.mark.parametrize("grid_n", [8, 12, 24])
+def test_vr_pairlist_step(gpulib, pkg, oracle, nodes, grid_n):
+    """Same recorded collision list on both sides: post-step f within 1e-12."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(grid_n, -5.0, 5.0)
+    f0 = ph.bimodal(g)
+    rng = np.random.default_rng(grid_n + 100 * nodes)
+    subs = random_pairs(rng, g.nv, (3000, 2000, 1000), 1, nodes)
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, iColl=pkg.DVM_COLL_VR, deltat=0.05)
+    gpu.compute_collision_integral(0, pkg.PairList(subs))
+    cpu.compute_collision_integral(0, pkg.PairList(subs))
+    assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert gpu.error_word() == 0
+
+
+@pytest.mark.parametrize("method", ["VR", "FMC"])
+@pytest.mark.parametrize("model", ["HS", "VHS", "VSS"])
+def test_philox_steps(gpulib, pkg, oracle, method, model):
+    """Counter-based stream shared by both sides: several full steps agree within 1e-12."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(12, -5.0, 5.0)
+    f0 = ph.bimodal(g)
+    omega, alpha = {"HS": (0.5, 1.0), "VHS": (0.81, 1.0), "VSS": (0.81, 1.4)}[model]
+    coll = pkg.DVM_COLL_VR if method == "VR" else pkg.DVM_COLL_FMC
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, iColl=coll, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                            samples_per_step=20000, omega=omega, alpha=alpha, NRepl=2, seed=11,
+                            deltat=0.02, cdf_tolerance=0.01)
+    for _ in range(3):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert gpu.collision_count() == cpu.collision_count()
+    assert rel_err(gpu.properties()[:, :17], cpu.properties()[:, :17]) <= 1e-11
+    assert gpu.error_word() == 0
+
+
+def test_formula_sample_counts(gpulib, pkg, oracle):
+    """compute_num_coll_pairs: the same counts from the reference formula."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(16, -5.0, 5.0)
+    f0 = np.stack([ph.bimodal(g, T2=1.5 + 0.5 * c) for c in range(4)])
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, nx_space=4, iColl=pkg.DVM_COLL_VR,
+                            samples_mode=pkg.DVM_SAMPLES_FORMULA, ColnRMS=0.05, deltat=0.02)
+    gpu.compute_collision_integral(0)
+    cpu.compute_collision_integral(0)
+    assert gpu.collision_count() == cpu.collision_count() > 0
+    assert rel_err(gpu.phi(), cpu.phi()) <= REL
+
+
+def test_golden_fixtures(gpulib, pkg):
+    ph = pkg.physics
+    G = np.load(GOLDEN)
+    g = ph.VelocityGrid.uniform(8, -3.0, 3.0)
+    for tag, method, nsub in (("vr_nodes", pkg.DVM_COLL_VR, 3),
+                              ("vr_uniforms", pkg.DVM_COLL_VR, 3),
+                              ("fmc_uniforms", pkg.DVM_COLL_FMC, 1)):
+        subs = []
+        for q in range(nsub):
+            d = {"count": int(G["%s_count%d" % (tag, q)]), "num_repl": 2}
+            for k in ("glA", "glB", "rA", "rB", "r_phi", "r_cos"):
+                key = "%s_%s%d" % (tag, k, q)
+                if key in G:
+                    d[k] = G[key]
+            subs.append(d)
+        s = pkg.DVMSolver(pkg.DVMConfig(iColl=method, NRepl=2, deltat=0.05), g)
+        s.initialize_dist_func(G["zerod_f0"])
+        s.compute_collision_integral(0, pkg.PairList(subs))
+        assert rel_err(s.phi()[0], G["%s_f1" % tag]) <= REL, tag
+    # 2-D cavity convection
+    g9 = ph.VelocityGrid.uniform(9, -4.0, 4.0)
+    walls = ((1.0, 0.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 0.0, 1.2),
+             (1.0, 0.0, 0.0, 0.0, 1.0), (1.0, 0.3, 0.0, 0.0, 1.0))
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_2D, nx_space=5, ny_space=4, dx=0.5, dy=0.5,
+                        deltat=0.02, iColl=pkg.DVM_COLL_NONE, iConv=pkg.DVM_CONV_UPWIND1,
+                        acc_coeff=0.8, walls=walls)
+    s = pkg.DVMSolver(cfg, g9)
+    s.initialize_dist_func(G["cav_f0"])
+    s.compute_convection()
+    assert rel_err(s.phi(), G["cav_f1"]) <= REL
+    s.calculate_physical_properties()
+    assert rel_err(s.properties()[:, :17], G["cav_props1"][:, :17]) <= 1e-11
+    # 1-D diffuse ends
+    walls = ((1.0, 0.0, 0.0, 0.0, 1.1), (1.0, 0.0, 0.0, 0.0, 0.9), (1, 0, 0, 0, 1), (1, 0, 0, 0, 1))
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=5, dx=0.4, deltat=0.03,
+                        iColl=pkg.DVM_COLL_NONE, iConv=pkg.DVM_CONV_UPWIND1, acc_coeff=0.6,
+                        bc=(pkg.DVM_BC1D_DIFFUSE, pkg.DVM_BC1D_DIFFUSE, 0, 0), walls=walls)
+    s = pkg.DVMSolver(cfg, g)
+    s.initialize_dist_func(G["d1_f0"])
+    s.compute_convection()
+    assert rel_err(s.phi(), G["d1_f1"]) <= REL
+
+
+@pytest.mark.parametrize("acc", [1.0, 0.7, 0.0])
+@pytest.mark.parametrize("grid_n", [8, 9])
+@pytest.mark.parametrize("lr", ["wall", "couette", "inout"])
+def test_cavity_convection(gpulib, pkg, oracle, acc, grid_n, lr):
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(grid_n, -4.0, 4.0)
+    nxs, nys = 6, 5
+    rng = np.random.default_rng(grid_n)
+    f0 = np.stack([ph.maxwellian(g, 1.0 + 0.1 * rng.random(), 0.2 * rng.standard_normal(),
+                                 0.2 * rng.standard_normal(), 0.0, 0.8 + 0.4 * rng.random())
+                   for _ in range(nxs * nys)])
+    bcv = {"wall": pkg.DVM_BC2D_WALL, "couette": pkg.DVM_BC2D_COUETTE,
+           "inout": pkg.DVM_BC2D_INOUT}[lr]
+    walls = ((1, 0.0, 0.1, 0, 1.0), (1, 0.0, -0.1, 0, 1.3), (1, 0.0, 0, 0, 0.9), (1, 0.3, 0, 0, 1.0))
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_2D, nx_space=nxs,
+                            ny_space=nys, dx=0.5, dy=0.4, deltat=0.03, iColl=pkg.DVM_COLL_NONE,
+                            iConv=pkg.DVM_CONV_UPWIND1, acc_coeff=acc, walls=walls,
+                            bc=(bcv, bcv, pkg.DVM_BC2D_WALL, pkg.DVM_BC2D_WALL))
+    for _ in range(3):
+        gpu.compute_convection()
+        cpu.compute_convection()
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert gpu.error_word() == 0
+
+
+@pytest.mark.parametrize("bc", [(1, 1), (2, 2), (3, 3), (4, 4), (3, 2), (1, 4)])
+def test_1d_convection(gpulib, pkg, oracle, bc):
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -6.0, 6.0)
+    f0, up, dn = ph.shock_profile(g, 12, 0.5, 1.5, 1.5)
+    walls = ((dn["n"], dn["u"], 0, 0, dn["T"]), (up["n"], up["u"], 0, 0, up["T"]),
+             (1, 0, 0, 0, 1), (1, 0, 0, 0, 1))
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_1D, nx_space=12, dx=0.5,
+                            deltat=0.04, iColl=pkg.DVM_COLL_NONE, iConv=pkg.DVM_CONV_UPWIND1,
+                            acc_coeff=0.75, walls=walls, bc=(bc[0], bc[1], 0, 0))
+    for _ in range(3):
+        gpu.compute_convection()
+        cpu.compute_convection()
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+
+
+def test_cavity_full_steps(gpulib, pkg, oracle):
+    """Collisions + walls + moments on a small cavity, several steps."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(8, -4.0, 4.0)
+    nxs, nys = 5, 5
+    f0 = np.stack([ph.maxwellian(g, 1.0, 0.0, 0.0, 0.0, 1.0) for _ in range(nxs * nys)])
+    walls = ((1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0.3, 0, 0, 1.0))
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_2D, nx_space=nxs,
+                            ny_space=nys, dx=0.5, dy=0.5, deltat=0.04, Kn=0.1,
+                            iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                            samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=3000,
+                            acc_coeff=1.0, walls=walls, seed=5)
+    for _ in range(3):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert rel_err(gpu.properties()[:, :17], cpu.properties()[:, :17]) <= 1e-10
+
+
+def test_shock_full_steps(gpulib, pkg, oracle):
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -7.0, 7.0)
+    f0, up, dn = ph.shock_profile(g, 10, 0.5, 2.0, 1.5)
+    walls = ((dn["n"], dn["u"], 0, 0, dn["T"]), (up["n"], up["u"], 0, 0, up["T"]),
+             (1, 0, 0, 0, 1), (1, 0, 0, 0, 1))
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_1D, nx_space=10, dx=0.5,
+                            deltat=0.03, omega=0.81, iColl=pkg.DVM_COLL_VR,
+                            iConv=pkg.DVM_CONV_UPWIND1, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                            samples_per_step=2000, walls=walls,
+                            bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), seed=9)
+    for _ in range(3):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+
+
+# --------------------------------------------------------------------------------------
+# Full benchmark sizes: size-independent properties.
+def _conservation(pkg, s, steps):
+    p0 = s.properties()
+    s.solve(steps)
+    p1 = s.properties()
+    n0 = p0[:, 0]
+    assert np.abs(p1[:, 0] - n0).max() <= 1e-12 * n0.max()
+    mom0 = p0[:, 0:1] * p0[:, 1:4]
+    mom1 = p1[:, 0:1] * p1[:, 1:4]
+    assert np.abs(mom1 - mom0).max() <= 1e-11 * n0.max()
+    e0 = p0[:, 0] * (1.5 * p0[:, 4] + (p0[:, 1:4] ** 2).sum(1))
+    e1 = p1[:, 0] * (1.5 * p1[:, 4] + (p1[:, 1:4] ** 2).sum(1))
+    assert np.abs(e1 - e0).max() <= 1e-11 * e0.max()
+    assert s.error_word() == 0
+
+
+def test_relaxation_full_size_conserves(gpulib, pkg):
+    """24^3 hard-sphere relaxation, 1e5 samples per step: n, n u, energy to round-off."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(24, -5.0, 5.0)
+    s = pkg.DVMSolver(pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                    samples_per_step=100000, deltat=0.01, seed=1), g)
+    s.initialize_dist_func(ph.bimodal(g))
+    T0 = s.properties()[0, 4]
+    _conservation(pkg, s, 20)
+    assert s.collision_count() == 100000
+    assert abs(s.properties()[0, 4] - T0) < 1e-11
+
+
+def test_shock_size_collisions_conserve(gpulib, pkg):
+    """200 cells x 32^3, VHS, 2e5 samples per cell-step: per-cell conservation."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(32, -9.0, 9.0)
+    f0, up, dn = ph.shock_profile(g, 200, 0.5, 3.0, 10.0)
+    s = pkg.DVMSolver(pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=200, dx=0.5,
+                                    deltat=0.05, omega=0.81, iColl=pkg.DVM_COLL_VR,
+                                    samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                    samples_per_step=200000, seed=3), g)
+    s.initialize_dist_func(f0)
+    _conservation(pkg, s, 2)
+    assert s.collision_count() == 200 * 200000
+
+
+def test_relaxation_converges_to_maxwellian(gpulib, pkg):
+    """The bimodal state relaxes: its heat flux / higher moments decay, T and n stay."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(24, -5.0, 5.0)
+    s = pkg.DVMSolver(pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                    samples_per_step=100000, deltat=0.05, seed=2), g)
+    f0 = ph.bimodal(g)
+    s.initialize_dist_func(f0)
+    p0 = s.properties()[0]
+    s.solve(60)
+    p1 = s.properties()[0]
+    assert abs(p1[pkg.DVM_P["txx"]] - p1[pkg.DVM_P["pressure"]]) < \
+        0.5 * abs(p0[pkg.DVM_P["txx"]] - p0[pkg.DVM_P["pressure"]])
+
+
+def test_ensemble_moments_within_3se(gpulib, pkg, oracle):
+    """Independent seeds on each side: ensemble means of the moments agree within 3 SE."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -5.0, 5.0)
+    f0 = ph.bimodal(g)
+    K = 12
+    res = {"gpu": [], "cpu": []}
+    for side, offset in (("gpu", 0), ("cpu", 1000)):
+        for k in range(K):
+            cfg = pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                samples_per_step=2000, deltat=0.05, seed=offset + k)
+            s = pkg.DVMSolver(cfg, g) if side == "gpu" else oracle.OracleSolver(cfg, g)
+            s.initialize_dist_func(f0)
+            s.solve(3)
+            res[side].append(s.properties()[0, :17])
+    a, b = np.array(res["gpu"]), np.array(res["cpu"])
+    for q in (pkg.DVM_P["qx"], pkg.DVM_P["txx"], pkg.DVM_P["txy"], pkg.DVM_P["tyy"]):
+        se = np.sqrt(a[:, q].var(ddof=1) / K + b[:, q].var(ddof=1) / K)
+        assert abs(a[:, q].mean() - b[:, q].mean()) <= 3.0 * se + 1e-14, pkg.PROP_NAMES[q]

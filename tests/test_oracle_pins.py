@@ -1,0 +1,123 @@
+"""Pins of the CPU restatement (oracle/) against the reference's own known answers,
+published test vectors and the golden fixtures. Runs without a GPU."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "golden_v1.npz")
+DOUBLE_TOL = 1.0e-13  # utils/constants.f90:52, the tolerance of the reference's tests
+
+
+def test_center_of_mass_velocity_reference_kat(oracle):
+    # test/coll_com_vel_test.f90:60-109: x = y = z = (-0.4, 1.2), m = (1, 0.1)
+    com = oracle.center_of_mass_velocity([-0.4, 1.2], [-0.4, 1.2], [-0.4, 1.2], [1.0, 0.1])
+    for c in com:
+        assert abs(c - (-0.254545454545454)) <= DOUBLE_TOL
+
+
+def test_philox_published_vectors(oracle):
+    # Random123 known-answer vectors for philox4x32, 10 rounds
+    assert oracle.philox4x32_10([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C,
+                                                          0x9B00DBD8]
+    assert oracle.philox4x32_10([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E,
+                                                                        0xA20BC7C6, 0x6D5451FD]
+    assert oracle.philox4x32_10([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                                [0xA4093822, 0x299F31D0]) == [0xD16CFE09, 0x94FDCCEB,
+                                                              0x5001E420, 0x24126EA1]
+
+
+def test_uniforms_in_unit_interval(oracle):
+    u = np.array([oracle.philox_uniform2(7, s, 3, 11, 2, 1) for s in range(2000)]).ravel()
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.02
+
+
+def test_interp_x_stencil(oracle, pkg):
+    # test/interp_x_test.f90:42-120 expects, for (u,v,w) = (0.1, 0.4, 0.2), origin (1,2,2),
+    # interior signs (1,-1,-1) and exterior flag x_only. Its grid file is not in the
+    # repository; this grid is one on which those stencil integers are determined.
+    ph = pkg.physics
+    g = ph.VelocityGrid(np.array([-0.5, 0.0, 0.5]), np.array([-0.5, 0.0, 0.5]),
+                        np.array([-0.3, 0.0, 0.3]))
+    st, ms, r = oracle.remap(g, 0.1, 0.4, 0.2)
+    assert r == 0
+    assert list(st) == [1, 2, 2, 1, -1, -1, 1]
+
+
+def _stencil_moments(g, st, ms):
+    i, j, k, a, b, c, e = (int(v) for v in st)
+    nodes = [(i, j, k), (i + a, j, k), (i, j + b, k), (i, j, k + c)]
+    w = list(ms[:4])
+    if e & 1:
+        nodes.append((i - a, j, k)); w.append(ms[4])
+    if e & 2:
+        nodes.append((i, j - b, k)); w.append(ms[5])
+    if e & 4:
+        nodes.append((i, j, k - c)); w.append(ms[6])
+    for n in nodes:
+        assert 0 <= n[0] < g.nx and 0 <= n[1] < g.ny and 0 <= n[2] < g.nz
+    vel = np.array([[g.x[n[0]], g.y[n[1]], g.z[n[2]]] for n in nodes])
+    w = np.array(w)
+    return w.sum(), (w[:, None] * vel).sum(0), (w * (vel ** 2).sum(1)).sum()
+
+
+@pytest.mark.parametrize("which", ["even", "odd", "stretched"])
+def test_remap_conserves_mass_momentum_energy(oracle, pkg, which):
+    # collisions/remapping.f90:265-368: the 7 weights conserve mass, momentum and energy
+    ph = pkg.physics
+    if which == "even":
+        g = ph.VelocityGrid.uniform(8, -3.0, 3.0)
+    elif which == "odd":
+        g = ph.VelocityGrid.uniform(9, -4.0, 4.0)
+    else:
+        g = ph.VelocityGrid(np.array([-4.0, -2.5, -1.2, -0.3, 0.4, 1.5, 3.0]),
+                            np.array([-3.0, -1.9, -0.8, 0.1, 0.9, 2.1, 3.2, 4.0]),
+                            np.array([-3.5, -2.0, -0.7, 0.0, 0.6, 1.9, 3.1, 4.2, 5.0]))
+    rng = np.random.default_rng(1)
+    lo = np.array([g.x[0], g.y[0], g.z[0]])
+    hi = np.array([g.x[-1], g.y[-1], g.z[-1]])
+    pts = np.concatenate([rng.uniform(lo, hi, (400, 3)),
+                          np.array([lo, hi, [lo[0], hi[1], lo[2]], [0.0, 0.0, 0.0]]),
+                          rng.uniform(lo - 0.3, lo + 0.3, (50, 3))])
+    for u, v, w in pts:
+        st, ms, r = oracle.remap(g, u, v, w)
+        assert r == 0
+        m0, m1, m2 = _stencil_moments(g, st, ms)
+        assert abs(m0 - 1.0) < 1e-12
+        assert np.allclose(m1, [u, v, w], atol=1e-12)
+        assert abs(m2 - (u * u + v * v + w * w)) < 1e-11
+
+
+def test_referenced_search_inverts_cdf(oracle):
+    rng = np.random.default_rng(5)
+    pdf = rng.random(3000) * (rng.random(3000) > 0.3)
+    cum = np.concatenate([[0.0], np.cumsum(pdf)])
+    ref = oracle.build_ref_table(cum)
+    assert ref[0, 0] == 0 and ref[-1, 1] == 3000
+    for R in np.concatenate([rng.random(3000), [1e-14, 0.5, 0.999999999]]):
+        idx = oracle.referenced_search(cum, ref, R)
+        if R < DOUBLE_TOL:
+            assert idx == 0
+            continue
+        adj = R * cum[-1]
+        assert cum[idx] < adj <= cum[idx + 1]
+
+
+def test_golden_fixtures_regression(oracle, pkg):
+    """The restatement still reproduces the committed fixtures (made by make_golden.py)."""
+    ph = pkg.physics
+    G = np.load(GOLDEN)
+    grids = {
+        "even8": ph.VelocityGrid.uniform(8, -3.0, 3.0),
+        "odd9": ph.VelocityGrid.uniform(9, -4.0, 4.0),
+        "stretched": ph.VelocityGrid(np.array([-4.0, -2.5, -1.2, -0.3, 0.4, 1.5, 3.0]),
+                                     np.array([-3.0, -1.9, -0.8, 0.1, 0.9, 2.1, 3.2, 4.0]),
+                                     np.array([-3.5, -2.0, -0.7, 0.0, 0.6, 1.9, 3.1, 4.2, 5.0])),
+    }
+    for name, g in grids.items():
+        for t, (u, v, w) in enumerate(G["remap_%s_pts" % name]):
+            st, ms, r = oracle.remap(g, u, v, w)
+            assert list(st) == list(G["remap_%s_st" % name][t])
+            assert np.allclose(ms, G["remap_%s_mass" % name][t], rtol=0, atol=1e-13)

@@ -427,6 +427,10 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
       const size_t n = static_cast<size_t>(pd.count[q] > 0 ? pd.count[q] : 0);
       if (n == 0) continue;
       if (!pairs->glA[q] && !pairs->rA[q]) { st = DVM_ERR_PARAM; break; }
+      if ((pairs->glA[q] && !pairs->glB[q]) || (!pairs->glA[q] && !pairs->rB[q])) {
+        st = DVM_ERR_PARAM;
+        break;
+      }
       if (!pairs->r_phi[q] || !pairs->r_cos[q]) { st = DVM_ERR_PARAM; break; }
       pd.glA[q] = static_cast<const int*>(up(pairs->glA[q], n * sizeof(int)));
       pd.glB[q] = static_cast<const int*>(up(pairs->glB[q], n * sizeof(int)));

@@ -191,7 +191,7 @@ static int bsearch_first_guess(int* index, double val, const double* arr, int mn
   if (arr[mx] < val) { *index = mx; return 0; }
   int left = mn, right = mx;
   int idx = *index;
-  if (idx < mn || idx > mx) return 1; /* not reachable: the guess lies in [mn, mx] here */
+  if (idx < mn || idx > mx) { *index = mn; return 1; } /* not reached on finite input */
   if (fabs(val - arr[idx]) < DOUBLE_TOL) return 0;
   if (idx == right) idx = idx - 1;
   for (int it = 0; it < MAX_SEARCH_ITERS; ++it) {

@@ -44,7 +44,10 @@ SEED = 20261203
 BYTES_PER_SAMPLE = 8 * (2 + 2 * 16)  # 2 partner reads + 16 atomic read-modify-writes
 
 
-def workload_config(pkg):
+def workload_config(pkg, ncells=None):
+    global NCELLS
+    if ncells:
+        NCELLS = ncells
     ph = pkg.physics
     g = ph.VelocityGrid.uniform(NGRID, -VMAX, VMAX)
     f0, up, dn = ph.shock_profile(g, NCELLS, DX, MACH, WIDTH)
@@ -201,7 +204,7 @@ def run_reference(args):
     import oracle as O
     O.build()
     pkg = importlib.import_module("2d_dvm_microflows_gb300")
-    cfg, g, f0 = workload_config(pkg)
+    cfg, g, f0 = workload_config(pkg, args.cells)
     threads = O.lib().orc_max_threads()
     # one untimed step to size the per-step sample (cells) to ~20 s per step at most
     rate, ncells, _ = cpu_rate(O, pkg, cfg, g, f0, threads, budget_s=20.0)
@@ -244,7 +247,7 @@ def run_gpu(args):
     dist = dist_init(ws)
     import torch
     pkg = importlib.import_module("2d_dvm_microflows_gb300")
-    cfg, g, f0 = workload_config(pkg)
+    cfg, g, f0 = workload_config(pkg, args.cells)
     s = pkg.DVMSolver(cfg, g)
     s.initialize_dist_func(f0)
     nv = g.nv
@@ -349,6 +352,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=None,
+                    help="smaller case of the same workload (profiling only)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         args.warmup = 3

@@ -46,6 +46,9 @@ struct dvm_ctx {
   uint32_t* d_err = nullptr;
   double* d_flush = nullptr;
   size_t flush_n = 0;
+  AxisEntry* d_axis_tab = nullptr;
+  double2* d_gtab = nullptr;
+  CollTables tabs{};
   int wall_base[4] = {-1, -1, -1, -1};
   int wall_entries = 0;
   int collide_grid = 0;
@@ -149,7 +152,8 @@ void release(dvm_ctx* c) {
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {c->d_axes, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
-                  c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush};
+                  c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
+                  c->d_axis_tab, c->d_gtab};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -198,6 +202,66 @@ int validate(const dvm_params* p, const dvm_vgrid* vg) {
   if (p->geometry == DVM_GEOM_0D && (p->nx_space != 1 || p->ny_space != 1)) {
     // independent homogeneous cells are allowed (a batch of 0-D instances on one grid)
     if (p->conv_method != DVM_CONV_NONE) return DVM_ERR_PARAM;
+  }
+  return DVM_OK;
+}
+
+// Remap tables per axis and, on a cubic uniform grid, the table of g and g^(2-2 omega)
+// indexed by di^2 + dj^2 + dk^2 (see CollTables).
+int build_collision_tables(dvm_ctx* c) {
+  const GridInfo& g = c->g;
+  const std::vector<double>* ax[3] = {&c->hx, &c->hy, &c->hz};
+  const int nmax = std::max(g.nx, std::max(g.ny, g.nz));
+  std::vector<AxisEntry> tab(3 * static_cast<size_t>(nmax));
+  const double nan = std::nan("");
+  for (int a = 0; a < 3; ++a) {
+    const std::vector<double>& v = *ax[a];
+    const int n = static_cast<int>(v.size());
+    for (int o = 0; o < nmax; ++o) {
+      AxisEntry& e = tab[static_cast<size_t>(a) * nmax + o];
+      for (int q = 0; q < kTabW; ++q) { e.D[q] = nan; e.invD[q] = nan; e.T[q] = nan; }
+      if (o >= n) continue;
+      for (int s = -kTabS; s <= kTabS; ++s) {
+        if (s == 0 || o + s < 0 || o + s >= n) continue;
+        const double d = v[o + s] - v[o];
+        e.D[kTabS + s] = d;
+        e.invD[kTabS + s] = 1.0 / d;
+        if (o - s >= 0 && o - s < n) {
+          const double ext = v[o - s] - v[o];
+          e.T[kTabS + s] = ext * (ext - d);
+        }
+      }
+    }
+  }
+  int st = dalloc(&c->d_axis_tab, tab.size());
+  if (st) return st;
+  cudaMemcpy(c->d_axis_tab, tab.data(), tab.size() * sizeof(AxisEntry), cudaMemcpyHostToDevice);
+  c->tabs.axis = c->d_axis_tab;
+  c->tabs.nmax = nmax;
+  c->tabs.phi_scale = 2.0 * c->pi / kPiExact;
+  // cubic uniform grid: the same uniform axis three times
+  bool cubic = (g.nx == g.ny && g.ny == g.nz && c->hx == c->hy && c->hy == c->hz);
+  const int n = g.nx;
+  const double h = (c->hx[n - 1] - c->hx[0]) / static_cast<double>(n - 1);
+  for (int i = 0; cubic && i + 1 < n; ++i)
+    if (std::fabs((c->hx[i + 1] - c->hx[i]) - h) > 1e-12 * std::fabs(h)) cubic = false;
+  c->tabs.gtab = nullptr;
+  c->tabs.gtab_n = 0;
+  c->tabs.gtab_smem = 0;
+  if (cubic) {
+    const int ns = 3 * (n - 1) * (n - 1) + 1;
+    const double vhs = 2.0 - 2.0 * (0.5 * (c->p.omega + c->p.omega));
+    std::vector<double2> gt(ns);
+    for (int s2 = 0; s2 < ns; ++s2) {
+      const double gg = std::sqrt(static_cast<double>(s2)) * h;
+      gt[s2].x = gg;
+      gt[s2].y = (vhs == 1.0) ? gg : std::pow(gg, vhs);
+    }
+    if ((st = dalloc(&c->d_gtab, gt.size()))) return st;
+    cudaMemcpy(c->d_gtab, gt.data(), gt.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    c->tabs.gtab = c->d_gtab;
+    c->tabs.gtab_n = ns;
+    c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
   }
   return DVM_OK;
 }
@@ -343,7 +407,11 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
     }
   }
   if (params->coll_method != DVM_COLL_NONE) {
-    const int bps = collide_blocks_per_sm(collide_smem_bytes(g));
+    if ((st = build_collision_tables(c))) {
+      release(c);
+      return st;
+    }
+    const int bps = collide_blocks_per_sm(collide_smem_bytes(g, c->tabs));
     c->collide_grid = c->num_sms * bps;
   }
   if ((st = cuda_status(cudaDeviceSynchronize()))) {
@@ -462,7 +530,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     });
   if (!st) {
     CollideArgs a{};
-    a.g = c->g; a.cp = coll_params(c); a.ncells = c->ncells;
+    a.g = c->g; a.cp = coll_params(c); a.t = c->tabs; a.ncells = c->ncells;
     a.step = static_cast<uint32_t>(step);
     a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;

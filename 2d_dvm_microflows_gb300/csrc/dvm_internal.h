@@ -57,9 +57,31 @@ struct CdfArgs {
   uint32_t* err;
 };
 
+// Per-axis remap tables (built once per grid by dvm_create). For origin o and offset
+// s in [-kTabS, kTabS]: D = v[o+s] - v[o], invD = 1/D, and T = ext*(ext - int) with
+// ext = v[o-s] - v[o], int = v[o+s] - v[o] -- the terms of the remap denominators
+// (collisions/remapping.f90:265-368). Entries whose nodes fall off the grid are NaN.
+constexpr int kTabS = 3;
+constexpr int kTabW = 2 * kTabS + 1;
+struct AxisEntry {
+  double D[kTabW];
+  double invD[kTabW];
+  double T[kTabW];
+};
+
+struct CollTables {
+  const AxisEntry* axis;   // [3][nmax]
+  int nmax;
+  const double2* gtab;     // (g, g^(2-2 omega)) by di^2+dj^2+dk^2; null unless the grid is
+  int gtab_n;              //   cubic and uniform
+  int gtab_smem;           // stage gtab in shared memory
+  double phi_scale;        // 2*pi_used/pi: phi/pi for sincospi
+};
+
 struct CollideArgs {
   GridInfo g;
   CollParams cp;
+  CollTables t;
   int ncells;
   uint32_t step;
   double* f;
@@ -132,6 +154,6 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s);
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s);
 cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s);
 int collide_blocks_per_sm(size_t smem);
-size_t collide_smem_bytes(const GridInfo& g);
+size_t collide_smem_bytes(const GridInfo& g, const CollTables& t);
 
 }  // namespace dvm

@@ -264,22 +264,233 @@ cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
 // ----------------------------------------------------------------------------------------
 // k_collide: persistent; a chunk is kCollideChunk consecutive samples of one
 // (cell, sub-integral). One thread per sample.
+//
+// GB300 runs FP64 at 1/64 of its FP32 rate and this kernel is bound by that pipe, so it
+// keeps the reference's arithmetic where it decides a result and moves the rest off the
+// FP64 pipe: order-preserving integer keys for every search compare, tables of node
+// differences / reciprocals / remap denominator terms, a table of g and g^(2-2 omega)
+// on cubic uniform grids, and the exact 1/2 mass ratios of like-species pairs. Each of
+// these changes a value by at most a few ulps; the parity bar (1e-12 of max|f| against
+// the restatement) checks the sum.
 __device__ __forceinline__ void scatter(double* f, const Stencil& s, double w) {
 #pragma unroll
   for (int q = 0; q < 7; ++q)
     if (s.node[q] >= 0) atomicAdd(f + s.node[q], w * s.mass[q]);
 }
 
+// Integer key with the order of the doubles (-0.0 folded onto +0.0).
+__device__ __forceinline__ long long okey(double d) {
+  long long b = __double_as_longlong(d);
+  if (b == static_cast<long long>(0x8000000000000000ULL)) b = 0;
+  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+
+// referenced_search with integer compares (the CDF and the target are nonnegative).
+__device__ __forceinline__ int referenced_search_keys(const double* __restrict__ cum,
+                                                      const int2* __restrict__ ref, int n,
+                                                      double R, uint32_t& bad) {
+  if (R < kDoubleTol) return 0;
+  int i = static_cast<int>(ceil(R * 1000.0));
+  i = i < 1 ? 1 : (i > kNRef ? kNRef : i);
+  const int2 lr = __ldg(ref + i - 1);
+  int left = lr.x, right = lr.y;
+  int idx = left + (right - left) / 2;
+  if (left == right) return idx < n ? idx : n - 1;
+  const long long* ck = reinterpret_cast<const long long*>(cum);
+  const long long adj = okey(R * __ldg(cum + n));
+  for (int it = 0; it < kMaxSearchIters; ++it) {
+    if (idx < 0 || idx >= n) break;
+    const long long c0 = okey(__longlong_as_double(__ldg(ck + idx)));
+    if (adj > c0 && adj <= okey(__longlong_as_double(__ldg(ck + idx + 1)))) return idx;
+    if (adj > c0) left = idx; else right = idx;
+    idx = left + (right - left) / 2;
+  }
+  bad |= DVM_EW_SEARCH;
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = lo + (hi - lo) / 2;
+    if (adj > okey(__ldg(cum + mid))) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+struct SmemAxes {
+  const double* v[3];
+  const long long* mid[3];   // keys of the midpoints between consecutive nodes
+  const AxisEntry* tab[3];
+  int n[3];
+};
+
+// One axis of compute_remapping_quantities: nearest node (:146-183). The reference's
+// binary_search_with_first_guess returns the node nearest to u, the lower one on a tie,
+// and the first or last node outside the grid; here the guess nint(factor*(u - v_min)) is
+// walked to that node with integer compares against the keys of the midpoints between
+// nodes (mid[i] = (v[i] + v[i+1])/2). The choice can differ from the reference's only for
+// u within an ulp of a midpoint.
+__device__ __forceinline__ int nearest(const SmemAxes& A, int ax, double u, double vmin,
+                                       double factor, int& corner, int& bad) {
+  const int mx = A.n[ax] - 1;
+  const long long* mid = A.mid[ax];
+  const long long vk = okey(u);
+  int o = __double2int_rn(factor * (u - vmin));
+  o = o < 0 ? 0 : (o > mx ? mx : o);
+  if (u != u) bad |= 1;  // NaN velocity: the reference's search would not return
+  int it = 0;
+  while (o > 0 && vk <= mid[o - 1] && it++ < kMaxAxis) --o;
+  while (o < mx && vk > mid[o] && it++ < kMaxAxis) ++o;
+  if (o >= mx) { o = mx; corner++; }
+  else if (o <= 0) { o = 0; corner++; }
+  return o;
+}
+
+// Reciprocal from an FP32 seed and two Newton steps (within an ulp or two of 1/d).
+__device__ __forceinline__ double fast_rcp(double d) {
+  const double ad = fabs(d);
+  if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
+  double r = static_cast<double>(__frcp_rn(static_cast<float>(d)));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
+// compute_remapping_quantities (collisions/remapping.f90:92-394) with tabulated
+// differences, reciprocals and denominator terms.
+__device__ __forceinline__ int remap_fast(const GridInfo& g, const SmemAxes& A, double u,
+                                          double v, double w, double f_off, Stencil& s) {
+  int corner = 0, bad = 0;
+  int o_i = nearest(A, 0, u, g.xv_min, g.xv_factor, corner, bad);
+  int o_j = nearest(A, 1, v, g.yv_min, g.yv_factor, corner, bad);
+  int o_k = nearest(A, 2, w, g.zv_min, g.zv_factor, corner, bad);
+  const int i_max = g.nx - 1, j_max = g.ny - 1, k_max = g.nz - 1;
+  if (corner == 3) {
+    o_i -= isign1(o_i - 1);
+    o_j -= isign1(o_j - 1);
+    o_k -= isign1(o_k - 1);
+  }
+  const double* x = A.v[0];
+  const double* y = A.v[1];
+  const double* z = A.v[2];
+  const double ox = x[o_i], oy = y[o_j], oz = z[o_k];
+  const double a = u - ox, b = v - oy, c = w - oz;
+  int sa = isgn(a), sb = isgn(b), sc = isgn(c);
+  if (o_i + sa > i_max || o_i + sa < 0) {
+    sa = -1 * sa;
+    find_boundary_stencil(sa, sb, sc, a, o_i, o_j, o_k, x, y, z, 0, i_max, 0, j_max, 0, k_max);
+  }
+  if (o_j + sb > j_max || o_j + sb < 0) {
+    sb = -1 * sb;
+    find_boundary_stencil(sb, sa, sc, b, o_j, o_i, o_k, y, x, z, 0, j_max, 0, i_max, 0, k_max);
+  }
+  if (o_k + sc > k_max || o_k + sc < 0) {
+    sc = -1 * sc;
+    find_boundary_stencil(sc, sb, sa, c, o_k, o_j, o_i, z, y, x, 0, k_max, 0, j_max, 0, i_max);
+  }
+  const int fx = (o_i - sa <= i_max && o_i - sa >= 0);
+  const int fy = (o_j - sb <= j_max && o_j - sb >= 0);
+  const int fz = (o_k - sc <= k_max && o_k - sc >= 0);
+  // per-axis differences, reciprocal of the interior difference, denominator term
+  double int_x, inv_x, ext_x = 0.0, t_x = 0.0;
+  if (sa >= -kTabS && sa <= kTabS) {
+    const AxisEntry& e = A.tab[0][o_i];
+    int_x = e.D[kTabS + sa]; inv_x = e.invD[kTabS + sa];
+    if (fx) { ext_x = e.D[kTabS - sa]; t_x = e.T[kTabS + sa]; }
+  } else {
+    int_x = x[o_i + sa] - ox; inv_x = 1.0 / int_x;
+    if (fx) { ext_x = x[o_i - sa] - ox; t_x = ext_x * (ext_x - int_x); }
+  }
+  double int_y, inv_y, ext_y = 0.0, t_y = 0.0;
+  if (sb >= -kTabS && sb <= kTabS) {
+    const AxisEntry& e = A.tab[1][o_j];
+    int_y = e.D[kTabS + sb]; inv_y = e.invD[kTabS + sb];
+    if (fy) { ext_y = e.D[kTabS - sb]; t_y = e.T[kTabS + sb]; }
+  } else {
+    int_y = y[o_j + sb] - oy; inv_y = 1.0 / int_y;
+    if (fy) { ext_y = y[o_j - sb] - oy; t_y = ext_y * (ext_y - int_y); }
+  }
+  double int_z, inv_z, ext_z = 0.0, t_z = 0.0;
+  if (sc >= -kTabS && sc <= kTabS) {
+    const AxisEntry& e = A.tab[2][o_k];
+    int_z = e.D[kTabS + sc]; inv_z = e.invD[kTabS + sc];
+    if (fz) { ext_z = e.D[kTabS - sc]; t_z = e.T[kTabS + sc]; }
+  } else {
+    int_z = z[o_k + sc] - oz; inv_z = 1.0 / int_z;
+    if (fz) { ext_z = z[o_k - sc] - oz; t_z = ext_z * (ext_z - int_z); }
+  }
+  const int flag = fx + 2 * fy + 4 * fz;
+  double den = 0.0;
+  if (fx) den = t_x;
+  if (fy) den = den + t_y;
+  if (fz) den = den + t_z;
+  double f_e = 0.0;
+  if (flag == 0) bad |= 2;
+  else f_e = f_off * (a * a + b * b + c * c - a * int_x - b * int_y - c * int_z) * fast_rcp(den);
+  const double f_ex = fx ? f_e : 0.0, f_ey = fy ? f_e : 0.0, f_ez = fz ? f_e : 0.0;
+  const double f_ix = (f_off * a - f_ex * ext_x) * inv_x;
+  const double f_iy = (f_off * b - f_ey * ext_y) * inv_y;
+  const double f_iz = (f_off * c - f_ez * ext_z) * inv_z;
+  const double f_o = f_off - f_ix - f_iy - f_iz - f_ex - f_ey - f_ez;
+  const int NX = g.nx, NXY = g.nx * g.ny;
+  const int base = o_i + NX * o_j + NXY * o_k;
+  s.node[0] = base;
+  s.node[1] = base + sa;
+  s.node[2] = base + NX * sb;
+  s.node[3] = base + NXY * sc;
+  s.node[4] = fx ? base - sa : -1;
+  s.node[5] = fy ? base - NX * sb : -1;
+  s.node[6] = fz ? base - NXY * sc : -1;
+  s.mass[0] = f_o; s.mass[1] = f_ix; s.mass[2] = f_iy; s.mass[3] = f_iz;
+  s.mass[4] = f_ex; s.mass[5] = f_ey; s.mass[6] = f_ez;
+  return bad;
+}
+
+struct CollideSmem {
+  size_t axes, keys, tabs, gtab, total;
+};
+
+__host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, const CollTables& t) {
+  CollideSmem L;
+  const size_t nsum = static_cast<size_t>(g.nx + g.ny + g.nz);
+  L.axes = 0;
+  L.keys = L.axes + nsum * sizeof(double);
+  L.tabs = L.keys + nsum * sizeof(long long);
+  L.gtab = L.tabs + 3 * static_cast<size_t>(t.nmax) * sizeof(AxisEntry);
+  L.gtab = (L.gtab + 15) & ~static_cast<size_t>(15);  // double2 needs 16-byte alignment
+  L.total = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
+  return L;
+}
+
 __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
-  extern __shared__ double s_axes[];
+  extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
-  double* sx = s_axes;
-  double* sy = sx + g.nx;
-  double* sz = sy + g.ny;
-  for (int t = threadIdx.x; t < g.nx; t += blockDim.x) sx[t] = g.x[t];
-  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) sy[t] = g.y[t];
-  for (int t = threadIdx.x; t < g.nz; t += blockDim.x) sz[t] = g.z[t];
+  const CollideSmem L = collide_smem_layout(g, a.t);
+  double* sv = reinterpret_cast<double*>(s_raw + L.axes);
+  long long* sk = reinterpret_cast<long long*>(s_raw + L.keys);
+  AxisEntry* st = reinterpret_cast<AxisEntry*>(s_raw + L.tabs);
+  double2* sg = reinterpret_cast<double2*>(s_raw + L.gtab);
+  const int nsum = g.nx + g.ny + g.nz;
+  for (int t = threadIdx.x; t < nsum; t += blockDim.x) {
+    const double* ax = t < g.nx ? g.x : (t < g.nx + g.ny ? g.y : g.z);
+    const int n = t < g.nx ? g.nx : (t < g.nx + g.ny ? g.ny : g.nz);
+    const int i = t < g.nx ? t : (t < g.nx + g.ny ? t - g.nx : t - g.nx - g.ny);
+    sv[t] = ax[i];
+    sk[t] = (i + 1 < n) ? okey(0.5 * (ax[i] + ax[i + 1])) : 0x7FFFFFFFFFFFFFFFLL;
+  }
+  {
+    const double* src = reinterpret_cast<const double*>(a.t.axis);
+    double* dst = reinterpret_cast<double*>(st);
+    const int n = 3 * a.t.nmax * static_cast<int>(sizeof(AxisEntry) / sizeof(double));
+    for (int t = threadIdx.x; t < n; t += blockDim.x) dst[t] = src[t];
+  }
+  if (a.t.gtab_smem)
+    for (int t = threadIdx.x; t < a.t.gtab_n; t += blockDim.x) sg[t] = a.t.gtab[t];
   __syncthreads();
+  SmemAxes A;
+  A.v[0] = sv; A.v[1] = sv + g.nx; A.v[2] = sv + g.nx + g.ny;
+  A.mid[0] = sk; A.mid[1] = sk + g.nx; A.mid[2] = sk + g.nx + g.ny;
+  A.tab[0] = st; A.tab[1] = st + a.t.nmax; A.tab[2] = st + 2 * a.t.nmax;
+  A.n[0] = g.nx; A.n[1] = g.ny; A.n[2] = g.nz;
+  const double2* gtab = a.t.gtab_smem ? sg : a.t.gtab;
 
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const int nent = 3 * a.ncells;
@@ -290,7 +501,8 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   const double alpha = 0.5 * (a.cp.alpha + a.cp.alpha);
   const double ralpha = 1.0 / alpha;
   const bool vss = fabs(ralpha - 1.0) > kDoubleTol;
-  const double mf = a.cp.mass / (a.cp.mass + a.cp.mass);
+  // like-species pair: mass fractions m/(m+m) are exactly 1/2
+  constexpr double mf = 0.5;
   uint32_t bad = 0;
 
   for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
@@ -318,41 +530,48 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
     } else {
       if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
       const bool aeq = vr && q == 0, beq = vr && q == 1;
-      lA = referenced_search((aeq ? a.cum_eq : a.cum_dev) + cs,
-                             (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                             nv, rA, bad);
-      lB = referenced_search((beq ? a.cum_eq : a.cum_dev) + cs,
-                             (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                             nv, rB, bad);
+      lA = referenced_search_keys((aeq ? a.cum_eq : a.cum_dev) + cs,
+                                  (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
+                                  nv, rA, bad);
+      lB = referenced_search_keys((beq ? a.cum_eq : a.cum_dev) + cs,
+                                  (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
+                                  nv, rB, bad);
     }
     const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
     const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
-    const double xA = sx[iA], yA = sy[jA], zA = sz[kA];
-    const double xB = sx[iB], yB = sy[jB], zB = sz[kB];
-    // compute_relative_velocity (collision_utilities.f90:188-218)
-    const double gx = xB - xA, gy = yB - yA, gz = zB - zA;
-    const double gg = sqrt(gx * gx + gy * gy + gz * gz);
-    if (gg < kDoubleTol) continue;  // variance_reduction.f90:697
-    const double g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
+    const double xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
+    const double xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
+    // compute_relative_velocity (collision_utilities.f90:188-218) and g^(2-2 omega)
+    double gg, g_sigma;
+    if (gtab) {
+      const int di = iB - iA, dj = jB - jA, dk = kB - kA;
+      const int s2 = di * di + dj * dj + dk * dk;
+      if (s2 == 0) continue;  // g < double_tol, variance_reduction.f90:697
+      const double2 e = gtab[s2];
+      gg = e.x;
+      g_sigma = e.y;
+    } else {
+      const double gx = xB - xA, gy = yB - yA, gz = zB - zA;
+      gg = sqrt(gx * gx + gy * gy + gz * gz);
+      if (gg < kDoubleTol) continue;
+      g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
+    }
     // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old
     const double* kc = a.kin + cs;
-    const double sA = (vr && q == 0) ? 1.0 : dsgn(kc[lA + 1]);
-    const double sB = (vr && q == 1) ? 1.0 : dsgn(kc[lB + 1]);
+    const double sA = (vr && q == 0) ? 1.0 : dsgn(__ldg(kc + lA + 1));
+    const double sB = (vr && q == 1) ? 1.0 : dsgn(__ldg(kc + lB + 1));
     // vr_depletion_routine elastic part (variance_reduction.f90:1157-1166)
-    const double depl1 = sB * 1.0 * factor * g_sigma;
-    const double depl2 = sA * 1.0 * factor * g_sigma;
-    const double kin1 = sA * depl1, kin2 = sB * depl2;
+    const double kin1 = sA * (sB * factor * g_sigma);
+    const double kin2 = sB * (sA * factor * g_sigma);
     atomicAdd(f + lA, -kin1);
     atomicAdd(f + lB, -kin2);
     // replenish_collision elastic branch (replenishing_collisions.f90:206-249)
-    const double kr1 = kin1 / static_cast<double>(NR), kr2 = kin2 / static_cast<double>(NR);
+    const double kr1 = (NR == 1) ? kin1 : kin1 / static_cast<double>(NR);
+    const double kr2 = (NR == 1) ? kin2 : kin2 / static_cast<double>(NR);
     const double vc0 = mf * xA + mf * xB, vc1 = mf * yA + mf * yB, vc2 = mf * zA + mf * zB;
-    const double ax0 = fabs(xA - vc0), ax1 = fabs(xB - vc0);
-    const double ay0 = fabs(yA - vc1), ay1 = fabs(yB - vc1);
-    const double az0 = fabs(zA - vc2), az1 = fabs(zB - vc2);
-    const double gp1 = sqrt(ax0 * ax0 + ay0 * ay0 + az0 * az0);
-    const double gp2 = sqrt(ax1 * ax1 + ay1 * ay1 + az1 * az1);
-    const double gr1 = gp1 / gg, gr2 = gp2 / gg;
+    // g_part(1)/g = g_part(2)/g = 1/2 for equal masses (pick_random_velocity_on_sphere
+    // :343-351); the VSS branch also needs the summed |xi - v_com| components.
+    const double hg = 0.5 * gg;
     for (int r = 0; r < NR; ++r) {
       double rphi, rcos;
       if (rec) {
@@ -361,16 +580,18 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
       } else {
         philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, a.step, q, 1u + r, rphi, rcos);
       }
-      // pick_random_velocity_on_sphere (collision_utilities.f90:284-352)
-      const double phi = 2.0 * a.cp.pi * rphi;
+      // pick_random_velocity_on_sphere (collision_utilities.f90:284-352); phi = 2 pi R
       double sphi, cphi;
-      sincos(phi, &sphi, &cphi);
-      double rx, ry, rz;
+      sincospi(a.t.phi_scale * rphi, &sphi, &cphi);
+      double ux, uy, uz;  // r / g: unit direction of the post-collision relative velocity
       if (vss) {
-        const double ur = ax0 + ax1, vr_ = ay0 + ay1, wr = az0 + az1;
+        const double ur = fabs(xA - vc0) + fabs(xB - vc0);
+        const double vr_ = fabs(yA - vc1) + fabs(yB - vc1);
+        const double wr = fabs(zA - vc2) + fabs(zB - vc2);
         const double ct = 2.0 * pow(rcos, ralpha) - 1.0;
         const double st = sqrt(1.0 - ct * ct);
         const double den = sqrt(vr_ * vr_ + wr * wr);
+        double rx, ry, rz;
         if (den > kDoubleTol * gg) {
           rx = ct * ur + st * sphi * den;
           ry = ct * vr_ + st * (gg * wr * cphi - ur * vr_ * sphi) / den;
@@ -380,18 +601,19 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
           ry = st * cphi * ur;
           rz = st * sphi * ur;
         }
+        ux = 0.5 * rx; uy = 0.5 * ry; uz = 0.5 * rz;
       } else {
         const double ct = 2.0 * rcos - 1.0;
         const double st = sqrt(1.0 - ct * ct);
-        rx = gg * st * cphi;
-        ry = gg * st * sphi;
-        rz = gg * ct;
+        ux = hg * st * cphi;
+        uy = hg * st * sphi;
+        uz = hg * ct;
       }
       Stencil s;
-      int rb = remap(g, sx, sy, sz, vc0 + gr1 * rx, vc1 + gr1 * ry, vc2 + gr1 * rz, 1.0, s);
+      int rb = remap_fast(g, A, vc0 + ux, vc1 + uy, vc2 + uz, 1.0, s);
       if (rb & 2) bad |= DVM_EW_REMAP; else scatter(f, s, kr1);
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap(g, sx, sy, sz, vc0 + (-gr2 * rx), vc1 + (-gr2 * ry), vc2 + (-gr2 * rz), 1.0, s);
+      rb = remap_fast(g, A, vc0 - ux, vc1 - uy, vc2 - uz, 1.0, s);
       if (rb & 2) bad |= DVM_EW_REMAP; else scatter(f, s, kr2);
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
@@ -399,12 +621,15 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   if (bad) atomicOr(a.err, bad);
 }
 
-size_t collide_smem_bytes(const GridInfo& g) {
-  return sizeof(double) * static_cast<size_t>(g.nx + g.ny + g.nz);
+size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
+  return collide_smem_layout(g, t).total;
 }
 
 int collide_blocks_per_sm(size_t smem) {
   int n = 0;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_collide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide, kCollideChunk, smem) !=
       cudaSuccess)
     n = 1;
@@ -412,7 +637,13 @@ int collide_blocks_per_sm(size_t smem) {
 }
 
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s) {
-  k_collide<<<grid, kCollideChunk, collide_smem_bytes(a.g), s>>>(a);
+  const size_t smem = collide_smem_bytes(a.g, a.t);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_collide, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
+  k_collide<<<grid, kCollideChunk, smem, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@ DVM_ABI_VERSION = 1
 
 # status codes
 DVM_OK, DVM_ERR_PARAM, DVM_ERR_OOM, DVM_ERR_CUDA, DVM_ERR_NUMERIC, DVM_ERR_TIMEOUT, \
-    DVM_ERR_NODEVICE = range(7)
+    DVM_ERR_NODEVICE, DVM_ERR_TOO_LARGE = range(8)
 
 # device error word bits
 DVM_EW_SEARCH, DVM_EW_REMAP, DVM_EW_NONFINITE, DVM_EW_NEGDENS = 1, 2, 4, 8
@@ -90,6 +90,8 @@ ENTRY_POINTS = {
     "dvm_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dvm_time_steps": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_double)]),
     "dvm_flush_l2": (C.c_int, [_P]),
+    "dvm_collide_noalloc": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), _P, _P,
+                                      C.c_int, C.c_uint64, _P, C.POINTER(C.c_int64)]),
 }
 
 

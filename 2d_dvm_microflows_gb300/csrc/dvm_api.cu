@@ -300,6 +300,7 @@ const char* dvm_strerror(int status) {
     case DVM_ERR_NUMERIC: return "device error word set";
     case DVM_ERR_TIMEOUT: return "device wait timed out";
     case DVM_ERR_NODEVICE: return "no CUDA device";
+    case DVM_ERR_TOO_LARGE: return "problem exceeds the 32 MiB no-allocation scratch array";
     default: return "unknown status";
   }
 }

@@ -39,7 +39,8 @@ enum {
   DVM_ERR_CUDA = 3,       /* CUDA runtime / launch error                             */
   DVM_ERR_NUMERIC = 4,    /* device error word set (see dvm_get_error_word)          */
   DVM_ERR_TIMEOUT = 5,    /* a bounded device wait ran out                           */
-  DVM_ERR_NODEVICE = 6    /* no CUDA device                                          */
+  DVM_ERR_NODEVICE = 6,   /* no CUDA device                                          */
+  DVM_ERR_TOO_LARGE = 7   /* problem exceeds dvm_collide_noalloc's fixed scratch      */
 };
 
 /* Bits of the device error word. */
@@ -199,6 +200,27 @@ int dvm_launch_count(dvm_ctx* ctx, int64_t* launches);
 int dvm_time_steps(dvm_ctx* ctx, uint64_t first_step, int nsteps, double* ms);
 /* Writes a buffer of bytes > L2 on the context's stream (cold-cache timing). */
 int dvm_flush_l2(dvm_ctx* ctx);
+
+/* ---- collisions without device allocation ------------------------------------------ */
+/* No counterpart in the reference. The collision integral of dvm_compute_collision_integral
+ * for callers that cannot allocate device memory -- a host that owns all device memory and
+ * forbids allocation behind its back, a memory pool held at a fixed budget, a real-time loop
+ * that must not enter the allocator. It allocates nothing: the caller passes, in device
+ * memory, f[ncells][Nv] (updated in place) and props[ncells][DVM_NPROP] (the cell
+ * properties, e.g. from dvm_get_properties); every intermediate lives in one fixed 32 MiB
+ * device array that the library holds on each GPU that loads it, until exit.
+ *   Limit: the grid tables plus 4*(Nv+1)*8 + 16064 bytes per cell must fit in 32 MiB
+ *   (about 70 cells of 24^3 or 30 cells of 32^3); larger problems get DVM_ERR_TOO_LARGE.
+ *   The first call on a device looks up that array's address (cudaGetSymbolAddress) with
+ *   the device current; make that first call before any stream capture.
+ *   Every call shares the array and rebuilds what it needs (the equilibrium is recomputed,
+ *   as on a new context's first call); calls that overlap on the GPU race on it.
+ *   Work is queued on `stream` (a cudaStream_t; NULL = default stream). If `collisions` is
+ *   not NULL the call synchronises that stream, stores the samples drawn and returns
+ *   DVM_ERR_NUMERIC if the device error word was set. */
+int dvm_collide_noalloc(const dvm_params* params, const dvm_vgrid* grid, double* f,
+                        const double* props, int ncells, uint64_t step, void* stream,
+                        int64_t* collisions);
 
 #ifdef __cplusplus
 }

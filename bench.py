@@ -175,6 +175,7 @@ def cpu_rate(oracle, pkg, cfg, g, f0, threads, budget_s, cells_cap=NCELLS):
     n cells of the shock (n sized to the time budget), full steps (collisions, convection,
     moments) run with `threads` OpenMP threads."""
     import dataclasses
+    cells_cap = min(cells_cap, len(f0))
     probe_cells = min(8, cells_cap)
     sub = dataclasses.replace(cfg, nx_space=probe_cells)
     s = oracle.OracleSolver(sub, g, threads=threads)

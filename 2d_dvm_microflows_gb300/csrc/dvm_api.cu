@@ -48,6 +48,7 @@ struct dvm_ctx {
   size_t flush_n = 0;
   AxisEntry* d_axis_tab = nullptr;
   double2* d_gtab = nullptr;
+  double2* d_trig = nullptr;
   CollTables tabs{};
   int wall_base[4] = {-1, -1, -1, -1};
   int wall_entries = 0;
@@ -153,7 +154,7 @@ void release(dvm_ctx* c) {
   void* bufs[] = {c->d_axes, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
-                  c->d_axis_tab, c->d_gtab};
+                  c->d_axis_tab, c->d_gtab, c->d_trig};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -239,6 +240,18 @@ int build_collision_tables(dvm_ctx* c) {
   c->tabs.axis = c->d_axis_tab;
   c->tabs.nmax = nmax;
   c->tabs.phi_scale = 2.0 * c->pi / kPiExact;
+  c->tabs.two_pi = 2.0 * c->pi;
+  {
+    std::vector<double2> tr(kTrigN);
+    for (int k = 0; k < kTrigN; ++k) {
+      const double ang = 2.0 * c->pi * (static_cast<double>(k) / kTrigN);
+      tr[k].x = std::cos(ang);
+      tr[k].y = std::sin(ang);
+    }
+    if ((st = dalloc(&c->d_trig, tr.size()))) return st;
+    cudaMemcpy(c->d_trig, tr.data(), tr.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    c->tabs.trig = c->d_trig;
+  }
   // cubic uniform grid: the same uniform axis three times
   bool cubic = (g.nx == g.ny && g.ny == g.nz && c->hx == c->hy && c->hy == c->hz);
   const int n = g.nx;

@@ -76,7 +76,11 @@ struct CollTables {
   int gtab_n;              //   cubic and uniform
   int gtab_smem;           // stage gtab in shared memory
   double phi_scale;        // 2*pi_used/pi: phi/pi for sincospi
+  const double2* trig;     // (cos, sin) of 2*pi_used*k/kTrigN, k < kTrigN
+  double two_pi;           // 2*pi_used
 };
+
+constexpr int kTrigN = 1024;
 
 struct CollideArgs {
   GridInfo g;

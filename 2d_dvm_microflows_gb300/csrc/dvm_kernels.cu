@@ -332,7 +332,9 @@ __device__ __forceinline__ int nearest(const SmemAxes& A, int ax, double u, doub
   const int mx = A.n[ax] - 1;
   const long long* mid = A.mid[ax];
   const long long vk = okey(u);
-  int o = __double2int_rn(factor * (u - vmin));
+  // the guess only starts the walk, so FP32 is enough for it
+  int o = __float2int_rn(static_cast<float>(factor) *
+                         (static_cast<float>(u) - static_cast<float>(vmin)));
   o = o < 0 ? 0 : (o > mx ? mx : o);
   if (u != u) bad |= 1;  // NaN velocity: the reference's search would not return
   int it = 0;
@@ -445,7 +447,7 @@ __device__ __forceinline__ int remap_fast(const GridInfo& g, const SmemAxes& A, 
 }
 
 struct CollideSmem {
-  size_t axes, keys, tabs, gtab, total;
+  size_t axes, keys, tabs, gtab, trig, total;
 };
 
 __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, const CollTables& t) {
@@ -456,7 +458,8 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   L.tabs = L.keys + nsum * sizeof(long long);
   L.gtab = L.tabs + 3 * static_cast<size_t>(t.nmax) * sizeof(AxisEntry);
   L.gtab = (L.gtab + 15) & ~static_cast<size_t>(15);  // double2 needs 16-byte alignment
-  L.total = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
+  L.trig = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
+  L.total = L.trig + static_cast<size_t>(kTrigN) * sizeof(double2);
   return L;
 }
 
@@ -484,6 +487,8 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   }
   if (a.t.gtab_smem)
     for (int t = threadIdx.x; t < a.t.gtab_n; t += blockDim.x) sg[t] = a.t.gtab[t];
+  double2* strig = reinterpret_cast<double2*>(s_raw + L.trig);
+  for (int t = threadIdx.x; t < kTrigN; t += blockDim.x) strig[t] = a.t.trig[t];
   __syncthreads();
   SmemAxes A;
   A.v[0] = sv; A.v[1] = sv + g.nx; A.v[2] = sv + g.nx + g.ny;
@@ -580,9 +585,22 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
       } else {
         philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, a.step, q, 1u + r, rphi, rcos);
       }
-      // pick_random_velocity_on_sphere (collision_utilities.f90:284-352); phi = 2 pi R
+      // pick_random_velocity_on_sphere (collision_utilities.f90:284-352); phi = 2 pi R:
+      // R = k/kTrigN + t exactly, cos/sin of 2 pi k/kTrigN from the table, of
+      // th = 2 pi t (< 0.0062) by Taylor series (next terms below 1e-17), then the
+      // angle-addition formulas.
       double sphi, cphi;
-      sincospi(a.t.phi_scale * rphi, &sphi, &cphi);
+      {
+        const double rk = floor(rphi * static_cast<double>(kTrigN));
+        const int k = min(max(static_cast<int>(rk), 0), kTrigN - 1);
+        const double th = a.t.two_pi * (rphi - rk * (1.0 / kTrigN));
+        const double t2 = th * th;
+        const double st = th * (1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0)));
+        const double ct = 1.0 - t2 * 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0)));
+        const double2 cs = strig[k];
+        cphi = cs.x * ct - cs.y * st;
+        sphi = cs.y * ct + cs.x * st;
+      }
       double ux, uy, uz;  // r / g: unit direction of the post-collision relative velocity
       if (vss) {
         const double ur = fabs(xA - vc0) + fabs(xB - vc0);

@@ -40,7 +40,7 @@ size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
 // Offsets of every buffer inside the scratch array.
 struct Layout {
-  size_t axes, tabs, gtab, eq_pre, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
+  size_t axes, tabs, gtab, trig, eq_pre, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
       chunk_off, total, err, end;
 };
 
@@ -53,6 +53,7 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   L.axes = o; o = align256(o + 2 * sizeof(double) * (nx + ny + nz));
   L.tabs = o; o = align256(o + 3 * sizeof(AxisEntry) * nmax);
   L.gtab = o; o = align256(o + sizeof(double2) * gtab_n);
+  L.trig = o; o = align256(o + sizeof(double2) * kTrigN);
   L.eq_pre = o; o = align256(o + sizeof(double) * C * nv1);
   L.eq_cache = o; o = align256(o + sizeof(double) * C * 4);
   L.cum_eq = o; o = align256(o + sizeof(double) * C * nv1);
@@ -71,7 +72,8 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
 // The remap tables of build_collision_tables (dvm_api.cu), built on the device so that
 // no host buffer is needed either.
 __global__ void k_noalloc_tables(GridInfo g, AxisEntry* tab, int nmax, double2* gtab,
-                                 int gtab_n, double h, double vhs) {
+                                 int gtab_n, double h, double vhs, double2* trig,
+                                 double two_pi) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const double nan = __longlong_as_double(0x7FF8000000000000LL);
   if (t < 3 * nmax) {
@@ -97,6 +99,10 @@ __global__ void k_noalloc_tables(GridInfo g, AxisEntry* tab, int nmax, double2* 
   if (t < gtab_n) {
     const double gg = sqrt(static_cast<double>(t)) * h;
     gtab[t] = make_double2(gg, (vhs == 1.0) ? gg : pow(gg, vhs));
+  }
+  if (t < kTrigN) {
+    const double ang = two_pi * (static_cast<double>(t) / kTrigN);
+    trig[t] = make_double2(cos(ang), sin(ang));
   }
 }
 
@@ -227,9 +233,12 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   const int nmax = nx > ny ? (nx > nz ? nx : nz) : (ny > nz ? ny : nz);
   AxisEntry* d_tab = reinterpret_cast<AxisEntry*>(base + L.tabs);
   double2* d_gtab = reinterpret_cast<double2*>(base + L.gtab);
+  double2* d_trig = reinterpret_cast<double2*>(base + L.trig);
   {
-    const int n = (3 * nmax > gtab_n) ? 3 * nmax : gtab_n;
-    k_noalloc_tables<<<(n + 255) / 256, 256, 0, s>>>(g, d_tab, nmax, d_gtab, gtab_n, h, vhs);
+    int n = (3 * nmax > gtab_n) ? 3 * nmax : gtab_n;
+    n = n > kTrigN ? n : kTrigN;
+    k_noalloc_tables<<<(n + 255) / 256, 256, 0, s>>>(g, d_tab, nmax, d_gtab, gtab_n, h, vhs,
+                                                     d_trig, 2.0 * pi);
     if ((e = cudaGetLastError()) != cudaSuccess) return status_of(e);
   }
   // state that must start from zero: the equilibrium cache (so every call builds the
@@ -274,6 +283,8 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   a.t.gtab_n = gtab_n;
   a.t.gtab_smem = (cubic && static_cast<size_t>(gtab_n) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
   a.t.phi_scale = 2.0 * pi / kPiExact;
+  a.t.trig = d_trig;
+  a.t.two_pi = 2.0 * pi;
   a.f = f; a.cum_eq = ca.cum_eq; a.cum_dev = ca.cum_dev; a.kin = ca.kin;
   a.ref_eq = ca.ref_eq; a.ref_dev = ca.ref_dev; a.plan = ca.plan; a.chunk_off = d_chunk;
   a.err = d_err;

@@ -88,6 +88,7 @@ class DVMConfig:
     walls: tuple = ((1.0, 0.0, 0.0, 0.0, 1.0),) * 4
     pi_mode: int = DVM_PI_REFERENCE
     seed: int = 0
+    precision: int = DVM_PREC_FP64
 
     def to_params(self):
         p = dvm_params()
@@ -107,6 +108,7 @@ class DVMConfig:
         p.mass, p.omega, p.alpha, p.sigma = self.mass, self.omega, self.alpha, self.sigma
         p.coln_rms, p.cdf_tolerance = self.ColnRMS, self.cdf_tolerance
         p.acc_coeff = self.acc_coeff
+        p.precision = self.precision
         return p
 
 

@@ -5,7 +5,7 @@ sizes against the compiled library (dvm_abi_version) and the header text.
 """
 import ctypes as C
 
-DVM_ABI_VERSION = 1
+DVM_ABI_VERSION = 2
 
 # status codes
 DVM_OK, DVM_ERR_PARAM, DVM_ERR_OOM, DVM_ERR_CUDA, DVM_ERR_NUMERIC, DVM_ERR_TIMEOUT, \
@@ -23,6 +23,7 @@ DVM_BC2D_WALL, DVM_BC2D_INOUT, DVM_BC2D_ZEROGRAD, DVM_BC2D_COUETTE = 1, 2, 3, 4
 DVM_BC1D_SPECULAR, DVM_BC1D_DIFFUSE, DVM_BC1D_INOUT, DVM_BC1D_ZEROGRAD = 1, 2, 3, 4
 DVM_PI_REFERENCE, DVM_PI_EXACT = 0, 1
 DVM_SAMPLES_FORMULA, DVM_SAMPLES_FIXED = 0, 1
+DVM_PREC_FP64, DVM_PREC_FP32 = 0, 1
 DVM_WALL_LEFT, DVM_WALL_RIGHT, DVM_WALL_BOTTOM, DVM_WALL_TOP = 0, 1, 2, 3
 DVM_WP_DENS, DVM_WP_U, DVM_WP_V, DVM_WP_W, DVM_WP_TEMP = 0, 1, 2, 3, 4
 
@@ -34,7 +35,7 @@ DVM_NPROP = 20
 
 # kernel ids for instrumentation
 KERNEL_NAMES = ["cdf_build", "collide_plan", "collide", "wall_flux", "wall_ghost",
-                "convect", "bc_1d", "moments"]
+                "convect", "bc_1d", "moments", "project"]
 DVM_K_COUNT = len(KERNEL_NAMES)
 
 
@@ -53,7 +54,8 @@ class dvm_params(C.Structure):
                 ("Kn", C.c_double), ("mass", C.c_double), ("omega", C.c_double),
                 ("alpha", C.c_double), ("sigma", C.c_double), ("coln_rms", C.c_double),
                 ("cdf_tolerance", C.c_double), ("acc_coeff", C.c_double),
-                ("wall", (C.c_double * 5) * 4)]
+                ("wall", (C.c_double * 5) * 4), ("precision", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class dvm_pairlist(C.Structure):

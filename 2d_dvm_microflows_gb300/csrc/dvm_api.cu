@@ -29,6 +29,7 @@ struct dvm_ctx {
   std::vector<double> hx, hy, hz, hbx, hby, hbz;
   // device buffers
   double* d_axes = nullptr;   // x, y, z, bx, by, bz
+  double* d_speed = nullptr;  // |xi| per node
   double* d_f = nullptr;
   double* d_fconv = nullptr;
   double* d_props = nullptr;
@@ -50,6 +51,13 @@ struct dvm_ctx {
   double2* d_gtab = nullptr;
   double2* d_trig = nullptr;
   CollTables tabs{};
+  // precision form: FP32 increment and FP32 tables
+  float* d_df = nullptr;
+  AxisEntryF* d_axis_tab_f = nullptr;
+  float2* d_gtab_f = nullptr;
+  float2* d_trig_f = nullptr;
+  CollTablesF tabs_f{};
+  int collide_f32_grid = 0;
   int wall_base[4] = {-1, -1, -1, -1};
   int wall_entries = 0;
   int collide_grid = 0;
@@ -66,7 +74,8 @@ struct dvm_ctx {
 namespace {
 
 const char* kKernelNames[DVM_K_COUNT] = {"cdf_build", "collide_plan", "collide", "wall_flux",
-                                         "wall_ghost", "convect", "bc_1d", "moments"};
+                                         "wall_ghost", "convect", "bc_1d", "moments",
+                                         "project"};
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return DVM_OK;
@@ -151,10 +160,11 @@ void release(dvm_ctx* c) {
   if (!c) return;
   harvest(c);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {c->d_axes, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
+  void* bufs[] = {c->d_axes, c->d_speed, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
-                  c->d_axis_tab, c->d_gtab, c->d_trig};
+                  c->d_axis_tab, c->d_gtab, c->d_trig, c->d_df, c->d_axis_tab_f,
+                  c->d_gtab_f, c->d_trig_f};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -182,6 +192,7 @@ int validate(const dvm_params* p, const dvm_vgrid* vg) {
   if (p->samples_mode != DVM_SAMPLES_FORMULA && p->samples_mode != DVM_SAMPLES_FIXED)
     return DVM_ERR_PARAM;
   if (p->samples_per_step < 0) return DVM_ERR_PARAM;
+  if (p->precision != DVM_PREC_FP64 && p->precision != DVM_PREC_FP32) return DVM_ERR_PARAM;
   if (!(p->dt > 0.0) || !(p->Kn > 0.0) || !(p->mass > 0.0)) return DVM_ERR_PARAM;
   if (p->coll_method != DVM_COLL_NONE && !(p->alpha > 0.0)) return DVM_ERR_PARAM;
   if (p->samples_mode == DVM_SAMPLES_FORMULA && p->coll_method != DVM_COLL_NONE &&
@@ -275,6 +286,48 @@ int build_collision_tables(dvm_ctx* c) {
     c->tabs.gtab = c->d_gtab;
     c->tabs.gtab_n = ns;
     c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
+  }
+  if (c->p.precision == DVM_PREC_FP32) {
+    // FP32 copies of the same tables for k_collide_f32
+    std::vector<AxisEntryF> tf(tab.size());
+    for (size_t e = 0; e < tab.size(); ++e)
+      for (int q = 0; q < kTabW; ++q) {
+        tf[e].D[q] = static_cast<float>(tab[e].D[q]);
+        tf[e].invD[q] = static_cast<float>(tab[e].invD[q]);
+        tf[e].T[q] = static_cast<float>(tab[e].T[q]);
+      }
+    if ((st = dalloc(&c->d_axis_tab_f, tf.size()))) return st;
+    cudaMemcpy(c->d_axis_tab_f, tf.data(), tf.size() * sizeof(AxisEntryF), cudaMemcpyHostToDevice);
+    std::vector<float2> trf(kTrigN);
+    for (int k = 0; k < kTrigN; ++k) {
+      const double ang = 2.0 * c->pi * (static_cast<double>(k) / kTrigN);
+      trf[k] = make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
+    }
+    if ((st = dalloc(&c->d_trig_f, trf.size()))) return st;
+    cudaMemcpy(c->d_trig_f, trf.data(), trf.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    c->tabs_f.axis = c->d_axis_tab_f;
+    c->tabs_f.trig = c->d_trig_f;
+    c->tabs_f.two_pi = static_cast<float>(2.0 * c->pi);
+    c->tabs_f.gtab = nullptr;
+    c->tabs_f.gtab_smem = 0;
+    if (c->tabs.gtab) {
+      const int ns = c->tabs.gtab_n;
+      const double vhs = 2.0 - 2.0 * (0.5 * (c->p.omega + c->p.omega));
+      std::vector<float2> gf(ns);
+      for (int s2 = 0; s2 < ns; ++s2) {
+        const double gg = std::sqrt(static_cast<double>(s2)) * h;
+        gf[s2] = make_float2(static_cast<float>(gg),
+                             static_cast<float>((vhs == 1.0) ? gg : std::pow(gg, vhs)));
+      }
+      if ((st = dalloc(&c->d_gtab_f, gf.size()))) return st;
+      cudaMemcpy(c->d_gtab_f, gf.data(), gf.size() * sizeof(float2), cudaMemcpyHostToDevice);
+      c->tabs_f.gtab = c->d_gtab_f;
+      c->tabs_f.gtab_smem = (static_cast<size_t>(ns) * sizeof(float2) <= 48 * 1024) ? 1 : 0;
+    }
+    const size_t n = static_cast<size_t>(c->ncells) * c->g.nv;
+    if ((st = dalloc(&c->d_df, n))) return st;
+    cudaMemset(c->d_df, 0, n * sizeof(float));
+    c->collide_f32_grid = c->num_sms * collide_f32_blocks_per_sm(c->g, c->tabs);
   }
   return DVM_OK;
 }
@@ -399,6 +452,20 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
   g.bx = g.z + g.nz;
   g.by = g.bx + g.nx;
   g.bz = g.by + g.ny;
+  {
+    std::vector<double> sp(nv);
+    size_t l = 0;
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i, ++l)
+          sp[l] = std::sqrt(c->hx[i] * c->hx[i] + c->hy[j] * c->hy[j] + c->hz[k] * c->hz[k]);
+    if ((st = dalloc(&c->d_speed, nv))) {
+      release(c);
+      return st;
+    }
+    cudaMemcpy(c->d_speed, sp.data(), nv * sizeof(double), cudaMemcpyHostToDevice);
+    g.speed = c->d_speed;
+  }
   cudaMemset(c->d_err, 0, sizeof(uint32_t));
   cudaMemset(c->d_f, 0, C * nv * sizeof(double));
   cudaMemset(c->d_props, 0, C * DVM_NPROP * sizeof(double));
@@ -549,7 +616,17 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
     a.chunk_off = c->d_chunk_off; a.pairs = pd; a.err = c->d_err;
-    st = launch(c, DVM_K_COLLIDE, [&] { return launch_collide(a, c->collide_grid, c->stream); });
+    if (c->p.precision == DVM_PREC_FP32) {
+      st = launch(c, DVM_K_COLLIDE, [&] {
+        return launch_collide_f32(a, c->tabs_f, c->d_df, c->collide_f32_grid, c->stream);
+      });
+      if (!st) {
+        ProjectArgs pa{c->g, c->ncells, c->d_f, c->d_df, c->d_props};
+        st = launch(c, DVM_K_PROJECT, [&] { return launch_project(pa, c->stream); });
+      }
+    } else {
+      st = launch(c, DVM_K_COLLIDE, [&] { return launch_collide(a, c->collide_grid, c->stream); });
+    }
   }
   if (!tmp.empty()) {
     cudaStreamSynchronize(c->stream);

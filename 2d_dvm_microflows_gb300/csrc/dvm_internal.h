@@ -82,6 +82,29 @@ struct CollTables {
 
 constexpr int kTrigN = 1024;
 
+// FP32 copies of the collision tables for the precision form.
+struct AxisEntryF {
+  float D[kTabW];
+  float invD[kTabW];
+  float T[kTabW];
+};
+
+struct CollTablesF {
+  const AxisEntryF* axis;  // [3][nmax]
+  const float2* gtab;      // (g, g^(2-2 omega)), as CollTables::gtab
+  int gtab_smem;
+  const float2* trig;      // (cos, sin) of 2*pi_used*k/kTrigN
+  float two_pi;
+};
+
+struct ProjectArgs {
+  GridInfo g;
+  int ncells;
+  double* f;               // [C][nv], FP64 state
+  float* df;               // [C][nv], FP32 collision increment (zeroed on exit)
+  const double* props;     // [C][DVM_NPROP], for the centring velocity
+};
+
 struct CollideArgs {
   GridInfo g;
   CollParams cp;
@@ -150,6 +173,10 @@ cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s);
 cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
                         long long* total_samples, cudaStream_t s);
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
+cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, float* df, int grid,
+                               cudaStream_t s);
+cudaError_t launch_project(const ProjectArgs& a, cudaStream_t s);
+int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t);
 cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_wall_specular(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s);

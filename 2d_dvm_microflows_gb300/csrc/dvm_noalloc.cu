@@ -146,6 +146,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   if (!p || !vg || !f || !props || ncells < 1 || !vg->x || !vg->y || !vg->z)
     return DVM_ERR_PARAM;
   if (p->coll_method != DVM_COLL_VR && p->coll_method != DVM_COLL_FMC) return DVM_ERR_PARAM;
+  if (p->precision != DVM_PREC_FP64) return DVM_ERR_PARAM;  // FP64 plain method only
   if (p->num_repl < 1 || p->num_repl > kMaxRepl || !(p->dt > 0.0) || !(p->Kn > 0.0) ||
       !(p->mass > 0.0) || !(p->alpha > 0.0) || p->samples_per_step < 0)
     return DVM_ERR_PARAM;

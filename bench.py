@@ -241,6 +241,110 @@ def run_reference(args):
     return 0
 
 
+def time_steps(s, steps, warmup, kernels=None):
+    """Device time of `steps` steps (L2 flushed before each, warm-up first): returns
+    (collisions per second, ms per step); per-kernel event times go into `kernels`."""
+    for _ in range(warmup):
+        s.solve(1)
+    s.synchronize()
+    s.profile_reset()
+    t, colls = 0.0, 0
+    for _ in range(steps):
+        s.profile(False)
+        s.flush_l2()
+        s.synchronize()
+        s.profile(True)
+        t += s.time_steps(1)
+        colls += s.collision_count()
+    s.profile(False)
+    if kernels is not None:
+        kernels.update({k: round(v[0] / max(v[1], 1), 4)
+                        for k, v in s.profile_read().items() if v[1]})
+    return colls / (t * 1e-3), t / steps
+
+
+def moment_error(p_test, p_ref):
+    """Per moment field, max over cells of |test - ref| / the field's physical scale
+    (n; sqrt(T) for velocities; T; p for stresses; n T^1.5 for heat flux)."""
+    n, T = np.abs(p_ref[:, 0]).max(), np.abs(p_ref[:, 4]).max()
+    pr = 0.5 * n * T
+    sc = np.array([n, T ** 0.5, T ** 0.5, T ** 0.5, T, T, T ** 0.5, pr] + [n * T ** 1.5] * 3 +
+                  [pr] * 6)
+    e = np.abs(p_test[:, :17] - p_ref[:, :17]).max(0) / sc
+    return {"max": float(e.max()),
+            "per_field": {k: float(v) for k, v in zip(
+                ["dens", "u", "v", "w", "temp", "species_temp", "avg_speed", "pressure", "qx",
+                 "qy", "qz", "txx", "tyy", "tzz", "txy", "txz", "tyz"], e)}}
+
+
+def cavity_config(pkg):
+    """2-D microcavity: 64 x 64 cells (unit side), 24^3 grid on [-5, 5], hard sphere,
+    Kn = 0.1, three diffuse walls at T = 1, lid diffuse at T = 1 moving at u = 0.3,
+    rest Maxwellian start, samples per cell-step from the reference formula (ColnRMS 0.001)."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(24, -5.0, 5.0)
+    mol = ph.molecule("Ar", ph.CSECTION_HS)
+    n = 64
+    walls = ((1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0.3, 0, 0, 1.0))
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_2D, nx_space=n, ny_space=n, dx=1.0 / n,
+                        dy=1.0 / n, deltat=0.0025, Kn=0.1, mass=1.0, omega=mol["omega"],
+                        alpha=mol["alpha"], sigma=ph.cross_section(mol, ph.CSECTION_BIRD),
+                        iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1, ColnRMS=0.001,
+                        samples_mode=pkg.DVM_SAMPLES_FORMULA, acc_coeff=1.0, walls=walls,
+                        seed=SEED)
+    f0 = np.tile(ph.maxwellian(g, 1.0, 0.0, 0.0, 0.0, 1.0), (n * n, 1))
+    return cfg, g, f0
+
+
+def run_forms(pkg, args, fp64_value):
+    """The precision form (FP32 sampling/scatter + FP64 projection) on the shock workload
+    and on the 2-D cavity, each beside the FP64 plain method from the same start and seed."""
+    import dataclasses
+    out = {}
+    cfg, g, f0 = workload_config(pkg, args.cells)
+    res = {}
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec), g)
+        s.initialize_dist_func(f0)
+        rate, ms = time_steps(s, args.steps, args.warmup)
+        res[prec] = (rate, ms, s.properties())
+        s.close()
+    out["fp32_shock"] = {
+        "value": res[pkg.DVM_PREC_FP32][0], "unit": "collisions/s",
+        "ms_per_step": res[pkg.DVM_PREC_FP32][1],
+        "fp64_value_same_run": res[pkg.DVM_PREC_FP64][0],
+        "speedup_vs_fp64": res[pkg.DVM_PREC_FP32][0] / res[pkg.DVM_PREC_FP64][0],
+        "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
+        "steps_compared": args.steps + args.warmup}
+    cfg, g, f0 = cavity_config(pkg)
+    res = {}
+    kern = {}
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec), g)
+        s.initialize_dist_func(f0)
+        kern[prec] = {}
+        rate, ms = time_steps(s, args.steps, args.warmup, kern[prec])
+        res[prec] = (rate, ms, s.properties(), s.collision_count())
+        s.close()
+    cells = cfg.nx_space * cfg.ny_space
+    out["cavity"] = {
+        "workload": "2-D microcavity 64x64 cells, 24^3 on [-5,5], hard sphere, Kn=0.1, "
+                    "diffuse walls T=1, lid u=0.3, samples from the reference formula "
+                    "(ColnRMS 0.001), dt=0.0025",
+        "collisions_per_step": res[pkg.DVM_PREC_FP32][3],
+        "fp32": {"value": res[pkg.DVM_PREC_FP32][0], "unit": "collisions/s",
+                 "ms_per_step": res[pkg.DVM_PREC_FP32][1],
+                 "cell_updates_per_s": cells / (res[pkg.DVM_PREC_FP32][1] * 1e-3),
+                 "ms_per_launch": kern[pkg.DVM_PREC_FP32]},
+        "fp64": {"value": res[pkg.DVM_PREC_FP64][0], "unit": "collisions/s",
+                 "ms_per_step": res[pkg.DVM_PREC_FP64][1],
+                 "cell_updates_per_s": cells / (res[pkg.DVM_PREC_FP64][1] * 1e-3),
+                 "ms_per_launch": kern[pkg.DVM_PREC_FP64]},
+        "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
+        "steps_compared": args.steps + args.warmup}
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -333,6 +437,8 @@ def run_gpu(args):
         "clocks": clk,
         "error_word": err,
     }
+    if ws == 1 and not args.no_forms:
+        line["forms"] = run_forms(pkg, args, value)
     if ws == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle as O
@@ -353,6 +459,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the precision-form and cavity measurements")
     ap.add_argument("--cells", type=int, default=None,
                     help="smaller case of the same workload (profiling only)")
     args = ap.parse_args()

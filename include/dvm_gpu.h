@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define DVM_ABI_VERSION 1
+#define DVM_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------------------ */
 enum {
@@ -67,6 +67,11 @@ enum { DVM_PI_REFERENCE = 0, DVM_PI_EXACT = 1 };
 enum { DVM_SAMPLES_FORMULA = 0,   /* compute_num_coll_pairs, collision_utilities.f90:106-140 */
        DVM_SAMPLES_FIXED = 1 };   /* samples_per_step total per cell-step, split over the
                                      sub-integrals in proportion to densA*densB             */
+/* arithmetic of the collision sampling and scatter (not in the reference) */
+enum { DVM_PREC_FP64 = 0,         /* plain method: everything in FP64                       */
+       DVM_PREC_FP32 = 1 };       /* sampling and scatter in FP32 into an FP32 increment,
+                                     then a per-cell FP64 projection that restores mass,
+                                     momentum and energy conservation; f, CDFs, moments FP64 */
 /* wall index in dvm_params.bc / .wall */
 enum { DVM_WALL_LEFT = 0, DVM_WALL_RIGHT = 1, DVM_WALL_BOTTOM = 2, DVM_WALL_TOP = 3 };
 /* wall property index in dvm_params.wall[w][...] */
@@ -122,6 +127,8 @@ typedef struct dvm_params {
   double cdf_tolerance;    /* variance_reduction.f90:316-322                       */
   double acc_coeff;        /* accommodation coefficient                            */
   double wall[4][5];       /* per wall: density, u, v, w, temperature              */
+  int32_t precision;       /* DVM_PREC_*                                           */
+  int32_t reserved;        /* zero                                                 */
 } dvm_params;
 
 /* Recorded collision list for one cell-step (same list applied to every cell).
@@ -189,7 +196,8 @@ int dvm_get_error_word(dvm_ctx* ctx, uint32_t* word);
 int dvm_profile_enable(dvm_ctx* ctx, int enable);
 /* kernel ids */
 enum { DVM_K_CDF = 0, DVM_K_PLAN = 1, DVM_K_COLLIDE = 2, DVM_K_WALL = 3, DVM_K_GHOST = 4,
-       DVM_K_CONVECT = 5, DVM_K_BC1D = 6, DVM_K_MOMENTS = 7, DVM_K_COUNT = 8 };
+       DVM_K_CONVECT = 5, DVM_K_BC1D = 6, DVM_K_MOMENTS = 7, DVM_K_PROJECT = 8,
+       DVM_K_COUNT = 9 };
 const char* dvm_kernel_name(int kernel_id);
 /* Sums the event-timed durations (ms) and launch counts since the last reset; synchronises. */
 int dvm_profile_read(dvm_ctx* ctx, int kernel_id, double* total_ms, int64_t* launches);

@@ -22,8 +22,8 @@ namespace dvm {
 // ----------------------------------------------------------------------------------------
 // k_cdf: one CTA per cell.
 // VR: collisions/variance_reduction.f90:234-496. FMC: collisions/full_mc.f90:110-180.
-constexpr int kCdfThreads = 1024;
-constexpr int kCdfPer = 4;
+constexpr int kCdfThreads = 512;
+constexpr int kCdfPer = 8;
 
 __device__ long long num_coll_pairs(const CollParams& cp, double beta3_min, double densA,
                                     double densB, double temp) {
@@ -1063,42 +1063,76 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
 // k_project: one CTA per cell. With phi = (1, c_x, c_y, c_z, |c|^2), c = xi - u_cell, and
 // weights w = |df|, the increment df - w * sum_k lambda_k phi_k with M lambda = r,
 // M_kl = sum w phi_k phi_l, r_k = sum df phi_k, has zero mass, momentum and energy; it is
-// the smallest such change in the w-weighted norm and vanishes where df does.
+// the smallest such change in the w-weighted norm and vanishes where df does. The sums
+// are taken column by column: per (i, j), sum_k of df z^p (p < 3) and of w z^p (p < 5).
 constexpr int kProjThreads = 256;
 
 __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
   __shared__ double s_red[20 * 32];
   __shared__ double s_lam[5];
+  __shared__ double s_ax[2 * kMaxAxis];
+  __shared__ double s_z[4 * kMaxAxis];
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
-  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
+  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
   float* df = a.df + static_cast<size_t>(cell) * nv;
   double* f = a.f + static_cast<size_t>(cell) * nv;
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
   const double u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
+  for (int t = threadIdx.x; t < NX; t += blockDim.x) s_ax[t] = g.x[t] - u;
+  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) s_ax[kMaxAxis + t] = g.y[t] - v;
+  for (int t = threadIdx.x; t < NZ; t += blockDim.x) {
+    const double z = g.z[t] - w;
+    s_z[t] = z;
+    s_z[kMaxAxis + t] = z * z;
+    s_z[2 * kMaxAxis + t] = z * z * z;
+    s_z[3 * kMaxAxis + t] = (z * z) * (z * z);
+  }
+  __syncthreads();
+  // 0-4: r; 5-19: M (row-major upper triangle)
   double acc[20];
 #pragma unroll
   for (int q = 0; q < 20; ++q) acc[q] = 0.0;
-  for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-    const double d = static_cast<double>(df[l]);
-    if (d == 0.0) continue;
-    const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
-    const double ph[5] = {1.0, g.x[i] - u, g.y[j] - v, g.z[k] - w, 0.0};
-    const double c2 = ph[1] * ph[1] + ph[2] * ph[2] + ph[3] * ph[3];
-    const double p4[5] = {ph[0], ph[1], ph[2], ph[3], c2};
-    const double wt = fabs(d);
-    int m = 5;
-#pragma unroll
-    for (int r = 0; r < 5; ++r) {
-      acc[r] += d * p4[r];
-#pragma unroll
-      for (int c = r; c < 5; ++c) acc[m++] += wt * p4[r] * p4[c];
+  for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
+    double D0 = 0.0, D1 = 0.0, D2 = 0.0, W0 = 0.0, W1 = 0.0, W2 = 0.0, W3 = 0.0, W4 = 0.0;
+    for (int k = 0; k < NZ; ++k) {
+      const float dfl = df[col + NXY * k];
+      if (dfl == 0.f) continue;
+      const double d = static_cast<double>(dfl), wt = fabs(d);
+      const double z = s_z[k], z2 = s_z[kMaxAxis + k];
+      D0 += d; D1 += d * z; D2 += d * z2;
+      W0 += wt; W1 += wt * z; W2 += wt * z2;
+      W3 += wt * s_z[2 * kMaxAxis + k]; W4 += wt * s_z[3 * kMaxAxis + k];
     }
+    const int j = col / NX, i = col - j * NX;
+    const double X = s_ax[i], Y = s_ax[kMaxAxis + j];
+    const double R = X * X + Y * Y;
+    const double E0 = R * W0 + W2;  // sum w |c|^2
+    acc[0] += D0;
+    acc[1] += X * D0;
+    acc[2] += Y * D0;
+    acc[3] += D1;
+    acc[4] += R * D0 + D2;
+    acc[5] += W0;                    // M00
+    acc[6] += X * W0;                // M01
+    acc[7] += Y * W0;                // M02
+    acc[8] += W1;                    // M03
+    acc[9] += E0;                    // M04
+    acc[10] += X * X * W0;           // M11
+    acc[11] += X * Y * W0;           // M12
+    acc[12] += X * W1;               // M13
+    acc[13] += X * E0;               // M14
+    acc[14] += Y * Y * W0;           // M22
+    acc[15] += Y * W1;               // M23
+    acc[16] += Y * E0;               // M24
+    acc[17] += W2;                   // M33
+    acc[18] += R * W1 + W3;          // M34
+    acc[19] += R * R * W0 + 2.0 * R * W2 + W4;  // M44
   }
   block_sum<20>(acc, s_red);
   if (threadIdx.x == 0) {
-    // M (packed upper triangle, row-major) lambda = r by Cholesky; no correction if M is
-    // not positive definite (e.g. no collisions landed in this cell)
+    // Cholesky of M; no correction if M is not positive definite (e.g. no collisions
+    // landed in this cell)
     double M[5][5], L[5][5] = {{0}}, y[5], lam[5];
     int m = 5;
     for (int r = 0; r < 5; ++r)
@@ -1134,15 +1168,19 @@ __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
   }
   __syncthreads();
   const double l0 = s_lam[0], l1 = s_lam[1], l2 = s_lam[2], l3 = s_lam[3], l4 = s_lam[4];
-  for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-    const double d = static_cast<double>(df[l]);
-    if (d == 0.0) continue;
-    const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
-    const double cx = g.x[i] - u, cy = g.y[j] - v, cz = g.z[k] - w;
-    const double c2 = cx * cx + cy * cy + cz * cz;
-    const double corr = fabs(d) * (l0 + l1 * cx + l2 * cy + l3 * cz + l4 * c2);
-    f[l] += d - corr;
-    df[l] = 0.f;
+  for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
+    const int j = col / NX, i = col - j * NX;
+    const double X = s_ax[i], Y = s_ax[kMaxAxis + j];
+    const double base = l0 + l1 * X + l2 * Y + l4 * (X * X + Y * Y);
+    for (int k = 0; k < NZ; ++k) {
+      const int l = col + NXY * k;
+      const float dfl = df[l];
+      if (dfl == 0.f) continue;
+      const double d = static_cast<double>(dfl);
+      const double poly = base + l3 * s_z[k] + l4 * s_z[kMaxAxis + k];
+      f[l] += d - fabs(d) * poly;
+      df[l] = 0.f;
+    }
   }
 }
 

@@ -237,6 +237,12 @@ class DVMSolver:
     def synchronize(self):
         _check(self.lib.dvm_synchronize(self.ctx), "dvm_synchronize")
 
+    def residual(self):
+        """Largest relative change of the moments in the last step (dvm_get_residual)."""
+        v = C.c_double()
+        _check(self.lib.dvm_get_residual(self.ctx, C.byref(v)), "dvm_get_residual")
+        return v.value
+
     # -- instrumentation -----------------------------------------------------------------
     def profile(self, enable=True):
         _check(self.lib.dvm_profile_enable(self.ctx, int(enable)), "dvm_profile_enable")
@@ -267,3 +273,139 @@ class DVMSolver:
 
     def flush_l2(self):
         _check(self.lib.dvm_flush_l2(self.ctx), "dvm_flush_l2")
+
+
+class DVMBatch:
+    """Many independent 0-D relaxations stepped together (dvm_batch_*): instances on the same
+    velocity grid share one context, one step of all of them is one CUDA-graph replay, and
+    the persistent collision launch of each grid is sized by a timing autotuner."""
+
+    def __init__(self, config, grids, instance_grid, samples_per_grid, lib=None):
+        self.lib = lib or load_library()
+        self.config = config
+        self.grids = list(grids)
+        self.instance_grid = np.ascontiguousarray(instance_grid, dtype=np.int32)
+        self.samples = np.ascontiguousarray(samples_per_grid, dtype=np.int64)
+        if len(self.samples) != len(self.grids):
+            raise ValueError("one sample count per grid")
+        self._params = config.to_params()
+        vgs = (dvm_vgrid * len(self.grids))()
+        for i, g in enumerate(self.grids):
+            vgs[i] = make_vgrid(g)
+        b = C.c_void_p()
+        _check(self.lib.dvm_batch_create(
+            C.byref(self._params), vgs, len(self.grids),
+            self.instance_grid.ctypes.data_as(C.POINTER(C.c_int32)), len(self.instance_grid),
+            self.samples.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(b)), "dvm_batch_create")
+        self.b = b
+        self.ninstances = len(self.instance_grid)
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.dvm_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_f(self, instance, f):
+        g = self.grids[self.instance_grid[instance]]
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(g.nv)
+        _check(self.lib.dvm_batch_upload_f(self.b, int(instance), _dptr(f)), "dvm_batch_upload_f")
+
+    def download_f(self, instance):
+        g = self.grids[self.instance_grid[instance]]
+        out = np.empty(g.nv)
+        _check(self.lib.dvm_batch_download_f(self.b, int(instance), _dptr(out)),
+               "dvm_batch_download_f")
+        return out
+
+    def step(self, nsteps=1):
+        _check(self.lib.dvm_batch_step(self.b, int(nsteps)), "dvm_batch_step")
+
+    def properties(self):
+        out = np.empty((self.ninstances, DVM_NPROP))
+        _check(self.lib.dvm_batch_get_properties(self.b, _dptr(out)), "dvm_batch_get_properties")
+        return out
+
+    def time_steps(self, nsteps):
+        ms, n = C.c_double(), C.c_int64()
+        _check(self.lib.dvm_batch_time_steps(self.b, int(nsteps), C.byref(ms), C.byref(n)),
+               "dvm_batch_time_steps")
+        return ms.value, n.value
+
+
+def footprint_bytes(config, grid, lib=None):
+    """Device bytes a context for (config, grid) allocates (dvm_footprint_bytes)."""
+    lib = lib or load_library()
+    p = config.to_params()
+    vg = make_vgrid(grid)
+    v = C.c_uint64()
+    _check(lib.dvm_footprint_bytes(C.byref(p), C.byref(vg), C.byref(v)), "dvm_footprint_bytes")
+    return v.value
+
+
+class DVMServer:
+    """Continuous-batching request server (dvm_server_*): submit solves of any geometry and
+    grid; a native worker thread admits them by HBM footprint, keeps their state on the
+    device and advances them concurrently until each reaches its residual or step limit."""
+
+    def __init__(self, hbm_budget_bytes, max_active=16, steps_per_turn=2, lib=None):
+        self.lib = lib or load_library()
+        sv = C.c_void_p()
+        _check(self.lib.dvm_server_create(C.c_uint64(int(hbm_budget_bytes)), int(max_active),
+                                          int(steps_per_turn), C.byref(sv)), "dvm_server_create")
+        self.sv = sv
+        self._shape = {}
+
+    def close(self):
+        if getattr(self, "sv", None):
+            self.lib.dvm_server_destroy(self.sv)
+            self.sv = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, config, grid, f0, max_steps, residual_tol=0.0):
+        p = config.to_params()
+        vg = make_vgrid(grid)
+        cells = config.nx_space * config.ny_space
+        f0 = np.ascontiguousarray(f0, dtype=np.float64).reshape(cells, grid.nv)
+        rid = C.c_int64()
+        _check(self.lib.dvm_server_submit(self.sv, C.byref(p), C.byref(vg), _dptr(f0),
+                                          int(max_steps), float(residual_tol), C.byref(rid)),
+               "dvm_server_submit")
+        self._shape[rid.value] = (cells, grid.nv)
+        return rid.value
+
+    def wait(self, rid):
+        info = dvm_request_info()
+        _check(self.lib.dvm_server_wait(self.sv, C.c_int64(rid), C.byref(info)), "dvm_server_wait")
+        return {k: getattr(info, k) for k, _ in dvm_request_info._fields_ if k != "reserved"}
+
+    def result(self, rid):
+        """(properties[cells, DVM_NPROP], f[cells, nv]) of a finished request."""
+        cells, nv = self._shape.pop(rid)
+        props = np.empty((cells, DVM_NPROP))
+        f = np.empty((cells, nv))
+        _check(self.lib.dvm_server_result(self.sv, C.c_int64(rid), _dptr(props), _dptr(f)),
+               "dvm_server_result")
+        return props, f
+
+    def stats(self):
+        n, a, b = C.c_int64(), C.c_int32(), C.c_uint64()
+        _check(self.lib.dvm_server_stats(self.sv, C.byref(n), C.byref(a), C.byref(b)),
+               "dvm_server_stats")
+        return {"completed": n.value, "peak_active": a.value, "peak_bytes": b.value}

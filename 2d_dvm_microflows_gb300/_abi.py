@@ -65,6 +65,13 @@ class dvm_pairlist(C.Structure):
                 ("r_phi", C.POINTER(C.c_double) * 3), ("r_cos", C.POINTER(C.c_double) * 3)]
 
 
+class dvm_request_info(C.Structure):
+    _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("steps", C.c_int32),
+                ("reserved", C.c_int32), ("residual", C.c_double), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double), ("collisions", C.c_int64),
+                ("device_bytes", C.c_uint64)]
+
+
 # Entry points declared in include/dvm_gpu.h: name -> (restype, argtypes)
 _P = C.c_void_p
 ENTRY_POINTS = {
@@ -92,6 +99,29 @@ ENTRY_POINTS = {
     "dvm_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dvm_time_steps": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_double)]),
     "dvm_flush_l2": (C.c_int, [_P]),
+    "dvm_get_residual": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "dvm_batch_create": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), C.c_int,
+                                   C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_int64),
+                                   C.POINTER(_P)]),
+    "dvm_batch_destroy": (C.c_int, [_P]),
+    "dvm_batch_upload_f": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "dvm_batch_download_f": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "dvm_batch_step": (C.c_int, [_P, C.c_int]),
+    "dvm_batch_get_properties": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "dvm_batch_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int64)]),
+    "dvm_footprint_bytes": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid),
+                                      C.POINTER(C.c_uint64)]),
+    "dvm_server_create": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(_P)]),
+    "dvm_server_destroy": (C.c_int, [_P]),
+    "dvm_server_submit": (C.c_int, [_P, C.POINTER(dvm_params), C.POINTER(dvm_vgrid),
+                                    C.POINTER(C.c_double), C.c_int32, C.c_double,
+                                    C.POINTER(C.c_int64)]),
+    "dvm_server_wait": (C.c_int, [_P, C.c_int64, C.POINTER(dvm_request_info)]),
+    "dvm_server_result": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]),
+    "dvm_server_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_uint64)]),
     "dvm_collide_noalloc": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), _P, _P,
                                       C.c_int, C.c_uint64, _P, C.POINTER(C.c_int64)]),
 }

@@ -20,7 +20,7 @@ HOST = os.path.join(HERE, "dvm_host")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
-SOURCES = ["dvm_kernels.cu", "dvm_api.cu", "dvm_noalloc.cu"]
+SOURCES = ["dvm_kernels.cu", "dvm_api.cu", "dvm_noalloc.cu", "dvm_server.cu"]
 
 
 def nvcc():

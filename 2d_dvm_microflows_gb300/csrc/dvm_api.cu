@@ -61,6 +61,11 @@ struct dvm_ctx {
   int wall_base[4] = {-1, -1, -1, -1};
   int wall_entries = 0;
   int collide_grid = 0;
+  bool own_stream = true;
+  bool async_alloc = false;                    // stream-ordered allocation on `stream`
+  size_t device_bytes = 0;                     // bytes this context allocated
+  const uint32_t* step_dev = nullptr;          // set when a batch owns the step counter
+  unsigned long long* d_residual = nullptr;    // convergence residual of the last moments
   // instrumentation
   bool profile = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -156,6 +161,24 @@ int dalloc(T** p, size_t count) {
   return cuda_status(cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T)));
 }
 
+// Context allocation: stream-ordered for server-owned contexts, so that creating or freeing
+// one never waits for the work of others.
+template <typename T>
+int dalloc(dvm_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return DVM_OK;
+  const size_t bytes = count * sizeof(T);
+  cudaError_t e = c->async_alloc
+                      ? cudaMallocAsync(reinterpret_cast<void**>(p), bytes, c->stream)
+                      : cudaMalloc(reinterpret_cast<void**>(p), bytes);
+  if (e == cudaSuccess) c->device_bytes += bytes;
+  return cuda_status(e);
+}
+
+int h2d(dvm_ctx* c, void* dst, const void* src, size_t bytes) {
+  return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+}
+
 void release(dvm_ctx* c) {
   if (!c) return;
   harvest(c);
@@ -164,10 +187,13 @@ void release(dvm_ctx* c) {
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
                   c->d_axis_tab, c->d_gtab, c->d_trig, c->d_df, c->d_axis_tab_f,
-                  c->d_gtab_f, c->d_trig_f};
+                  c->d_gtab_f, c->d_trig_f, c->d_residual};
   for (void* b : bufs)
-    if (b) cudaFree(b);
-  if (c->stream) cudaStreamDestroy(c->stream);
+    if (b) {
+      if (c->async_alloc) cudaFreeAsync(b, c->stream);
+      else cudaFree(b);
+    }
+  if (c->stream && c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
 }
 
@@ -245,9 +271,9 @@ int build_collision_tables(dvm_ctx* c) {
       }
     }
   }
-  int st = dalloc(&c->d_axis_tab, tab.size());
+  int st = dalloc(c, &c->d_axis_tab, tab.size());
   if (st) return st;
-  cudaMemcpy(c->d_axis_tab, tab.data(), tab.size() * sizeof(AxisEntry), cudaMemcpyHostToDevice);
+  h2d(c, c->d_axis_tab, tab.data(), tab.size() * sizeof(AxisEntry));
   c->tabs.axis = c->d_axis_tab;
   c->tabs.nmax = nmax;
   c->tabs.phi_scale = 2.0 * c->pi / kPiExact;
@@ -259,8 +285,8 @@ int build_collision_tables(dvm_ctx* c) {
       tr[k].x = std::cos(ang);
       tr[k].y = std::sin(ang);
     }
-    if ((st = dalloc(&c->d_trig, tr.size()))) return st;
-    cudaMemcpy(c->d_trig, tr.data(), tr.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if ((st = dalloc(c, &c->d_trig, tr.size()))) return st;
+    h2d(c, c->d_trig, tr.data(), tr.size() * sizeof(double2));
     c->tabs.trig = c->d_trig;
   }
   // cubic uniform grid: the same uniform axis three times
@@ -281,8 +307,8 @@ int build_collision_tables(dvm_ctx* c) {
       gt[s2].x = gg;
       gt[s2].y = (vhs == 1.0) ? gg : std::pow(gg, vhs);
     }
-    if ((st = dalloc(&c->d_gtab, gt.size()))) return st;
-    cudaMemcpy(c->d_gtab, gt.data(), gt.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    if ((st = dalloc(c, &c->d_gtab, gt.size()))) return st;
+    h2d(c, c->d_gtab, gt.data(), gt.size() * sizeof(double2));
     c->tabs.gtab = c->d_gtab;
     c->tabs.gtab_n = ns;
     c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
@@ -296,15 +322,15 @@ int build_collision_tables(dvm_ctx* c) {
         tf[e].invD[q] = static_cast<float>(tab[e].invD[q]);
         tf[e].T[q] = static_cast<float>(tab[e].T[q]);
       }
-    if ((st = dalloc(&c->d_axis_tab_f, tf.size()))) return st;
-    cudaMemcpy(c->d_axis_tab_f, tf.data(), tf.size() * sizeof(AxisEntryF), cudaMemcpyHostToDevice);
+    if ((st = dalloc(c, &c->d_axis_tab_f, tf.size()))) return st;
+    h2d(c, c->d_axis_tab_f, tf.data(), tf.size() * sizeof(AxisEntryF));
     std::vector<float2> trf(kTrigN);
     for (int k = 0; k < kTrigN; ++k) {
       const double ang = 2.0 * c->pi * (static_cast<double>(k) / kTrigN);
       trf[k] = make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
     }
-    if ((st = dalloc(&c->d_trig_f, trf.size()))) return st;
-    cudaMemcpy(c->d_trig_f, trf.data(), trf.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if ((st = dalloc(c, &c->d_trig_f, trf.size()))) return st;
+    h2d(c, c->d_trig_f, trf.data(), trf.size() * sizeof(float2));
     c->tabs_f.axis = c->d_axis_tab_f;
     c->tabs_f.trig = c->d_trig_f;
     c->tabs_f.two_pi = static_cast<float>(2.0 * c->pi);
@@ -319,17 +345,18 @@ int build_collision_tables(dvm_ctx* c) {
         gf[s2] = make_float2(static_cast<float>(gg),
                              static_cast<float>((vhs == 1.0) ? gg : std::pow(gg, vhs)));
       }
-      if ((st = dalloc(&c->d_gtab_f, gf.size()))) return st;
-      cudaMemcpy(c->d_gtab_f, gf.data(), gf.size() * sizeof(float2), cudaMemcpyHostToDevice);
+      if ((st = dalloc(c, &c->d_gtab_f, gf.size()))) return st;
+      h2d(c, c->d_gtab_f, gf.data(), gf.size() * sizeof(float2));
       c->tabs_f.gtab = c->d_gtab_f;
       c->tabs_f.gtab_smem = (static_cast<size_t>(ns) * sizeof(float2) <= 48 * 1024) ? 1 : 0;
     }
     const size_t n = static_cast<size_t>(c->ncells) * c->g.nv;
-    if ((st = dalloc(&c->d_df, n))) return st;
-    cudaMemset(c->d_df, 0, n * sizeof(float));
+    if ((st = dalloc(c, &c->d_df, n))) return st;
+    cudaMemsetAsync(c->d_df, 0, n * sizeof(float), c->stream);
     c->collide_f32_grid = c->num_sms * collide_f32_blocks_per_sm(c->g, c->tabs);
   }
-  return DVM_OK;
+  // the host tables above are staged before they go out of scope
+  return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
 CollParams coll_params(const dvm_ctx* c) {
@@ -352,6 +379,9 @@ CollParams coll_params(const dvm_ctx* c) {
 }
 
 }  // namespace
+
+int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t stream,
+                   bool async_alloc, dvm_ctx** out);
 
 extern "C" {
 
@@ -376,6 +406,14 @@ const char* dvm_kernel_name(int kid) {
 }
 
 int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
+  return create_context(params, vg, nullptr, false, out);
+}
+
+}  // extern "C"
+
+// A context on the caller's stream (stream != null: batches share one stream).
+int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t stream,
+                   bool async_alloc, dvm_ctx** out) {
   if (!out) return DVM_ERR_PARAM;
   *out = nullptr;
   int st = validate(params, vg);
@@ -389,7 +427,11 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
   c->ncells = params->nx_space * params->ny_space;
   cudaGetDevice(&c->device);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
-  if ((st = cuda_status(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)))) {
+  c->async_alloc = async_alloc;
+  if (stream) {
+    c->stream = stream;
+    c->own_stream = false;
+  } else if ((st = cuda_status(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)))) {
     release(c);
     return st;
   }
@@ -421,18 +463,18 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
 
   const size_t C = c->ncells, nv = g.nv;
   const size_t naxes = 2 * (g.nx + g.ny + g.nz);
-  if ((st = dalloc(&c->d_axes, naxes)) || (st = dalloc(&c->d_f, C * nv)) ||
-      (st = dalloc(&c->d_fconv, C * nv)) || (st = dalloc(&c->d_props, C * DVM_NPROP)) ||
-      (st = dalloc(&c->d_err, 1))) {
+  if ((st = dalloc(c, &c->d_axes, naxes)) || (st = dalloc(c, &c->d_f, C * nv)) ||
+      (st = dalloc(c, &c->d_fconv, C * nv)) || (st = dalloc(c, &c->d_props, C * DVM_NPROP)) ||
+      (st = dalloc(c, &c->d_err, 1))) {
     release(c);
     return st;
   }
   if (params->coll_method != DVM_COLL_NONE) {
-    if ((st = dalloc(&c->d_eq_pre, C * (nv + 1))) || (st = dalloc(&c->d_eq_cache, C * 4)) ||
-        (st = dalloc(&c->d_cum_eq, C * (nv + 1))) || (st = dalloc(&c->d_cum_dev, C * (nv + 1))) ||
-        (st = dalloc(&c->d_kin, C * (nv + 1))) || (st = dalloc(&c->d_ref_eq, C * kNRef)) ||
-        (st = dalloc(&c->d_ref_dev, C * kNRef)) || (st = dalloc(&c->d_plan, C)) ||
-        (st = dalloc(&c->d_chunk_off, 3 * C + 1)) || (st = dalloc(&c->d_total_samples, 1))) {
+    if ((st = dalloc(c, &c->d_eq_pre, C * (nv + 1))) || (st = dalloc(c, &c->d_eq_cache, C * 4)) ||
+        (st = dalloc(c, &c->d_cum_eq, C * (nv + 1))) || (st = dalloc(c, &c->d_cum_dev, C * (nv + 1))) ||
+        (st = dalloc(c, &c->d_kin, C * (nv + 1))) || (st = dalloc(c, &c->d_ref_eq, C * kNRef)) ||
+        (st = dalloc(c, &c->d_ref_dev, C * kNRef)) || (st = dalloc(c, &c->d_plan, C)) ||
+        (st = dalloc(c, &c->d_chunk_off, 3 * C + 1)) || (st = dalloc(c, &c->d_total_samples, 1))) {
       release(c);
       return st;
     }
@@ -445,7 +487,7 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
   axes.insert(axes.end(), c->hbx.begin(), c->hbx.end());
   axes.insert(axes.end(), c->hby.begin(), c->hby.end());
   axes.insert(axes.end(), c->hbz.begin(), c->hbz.end());
-  cudaMemcpy(c->d_axes, axes.data(), naxes * sizeof(double), cudaMemcpyHostToDevice);
+  h2d(c, c->d_axes, axes.data(), naxes * sizeof(double));
   g.x = c->d_axes;
   g.y = g.x + g.nx;
   g.z = g.y + g.ny;
@@ -459,19 +501,20 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
       for (int j = 0; j < g.ny; ++j)
         for (int i = 0; i < g.nx; ++i, ++l)
           sp[l] = std::sqrt(c->hx[i] * c->hx[i] + c->hy[j] * c->hy[j] + c->hz[k] * c->hz[k]);
-    if ((st = dalloc(&c->d_speed, nv))) {
+    if ((st = dalloc(c, &c->d_speed, nv))) {
       release(c);
       return st;
     }
-    cudaMemcpy(c->d_speed, sp.data(), nv * sizeof(double), cudaMemcpyHostToDevice);
+    h2d(c, c->d_speed, sp.data(), nv * sizeof(double));
     g.speed = c->d_speed;
+    cudaStreamSynchronize(c->stream);
   }
-  cudaMemset(c->d_err, 0, sizeof(uint32_t));
-  cudaMemset(c->d_f, 0, C * nv * sizeof(double));
-  cudaMemset(c->d_props, 0, C * DVM_NPROP * sizeof(double));
+  cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream);
+  cudaMemsetAsync(c->d_f, 0, C * nv * sizeof(double), c->stream);
+  cudaMemsetAsync(c->d_props, 0, C * DVM_NPROP * sizeof(double), c->stream);
   if (c->d_eq_pre) {
-    cudaMemset(c->d_eq_pre, 0, C * (nv + 1) * sizeof(double));
-    cudaMemset(c->d_eq_cache, 0, C * 4 * sizeof(double));
+    cudaMemsetAsync(c->d_eq_pre, 0, C * (nv + 1) * sizeof(double), c->stream);
+    cudaMemsetAsync(c->d_eq_cache, 0, C * 4 * sizeof(double), c->stream);
   }
   // 2-D wall ghost entries: left/right walls (if walls), bottom and top (always walls)
   if (params->geometry == DVM_GEOM_2D && params->conv_method == DVM_CONV_UPWIND1) {
@@ -482,7 +525,7 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
     c->wall_base[2] = n; n += NXS;
     c->wall_base[3] = n; n += NXS;
     c->wall_entries = n;
-    if ((st = dalloc(&c->d_ghost, static_cast<size_t>(n) * nv))) {
+    if ((st = dalloc(c, &c->d_ghost, static_cast<size_t>(n) * nv))) {
       release(c);
       return st;
     }
@@ -495,13 +538,21 @@ int dvm_create(const dvm_params* params, const dvm_vgrid* vg, dvm_ctx** out) {
     const int bps = collide_blocks_per_sm(collide_smem_bytes(g, c->tabs));
     c->collide_grid = c->num_sms * bps;
   }
-  if ((st = cuda_status(cudaDeviceSynchronize()))) {
+  if ((st = dalloc(c, &c->d_residual, 1))) {
+    release(c);
+    return st;
+  }
+  cudaMemsetAsync(c->d_residual, 0, sizeof(unsigned long long), c->stream);
+  // host staging vectors above outlive this synchronisation
+  if ((st = cuda_status(cudaStreamSynchronize(c->stream)))) {
     release(c);
     return st;
   }
   *out = c;
   return DVM_OK;
 }
+
+extern "C" {
 
 int dvm_destroy(dvm_ctx* c) {
   if (!c) return DVM_ERR_PARAM;
@@ -533,7 +584,9 @@ int dvm_download_f(dvm_ctx* c, double* f) {
 
 int dvm_calculate_physical_properties(dvm_ctx* c) {
   if (!c) return DVM_ERR_PARAM;
-  MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err};
+  MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, c->d_residual};
+  int st = cuda_status(cudaMemsetAsync(c->d_residual, 0, sizeof(unsigned long long), c->stream));
+  if (st) return st;
   return launch(c, DVM_K_MOMENTS, [&] { return launch_moments(a, c->stream); });
 }
 
@@ -613,6 +666,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     CollideArgs a{};
     a.g = c->g; a.cp = coll_params(c); a.t = c->tabs; a.ncells = c->ncells;
     a.step = static_cast<uint32_t>(step);
+    a.step_dev = c->step_dev;
     a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
     a.chunk_off = c->d_chunk_off; a.pairs = pd; a.err = c->d_err;
@@ -753,14 +807,310 @@ int dvm_time_steps(dvm_ctx* c, uint64_t first_step, int nsteps, double* ms) {
   return st;
 }
 
+int dvm_get_residual(dvm_ctx* c, double* residual) {
+  if (!c || !residual) return DVM_ERR_PARAM;
+  unsigned long long v = 0;
+  int st = cuda_status(cudaMemcpyAsync(&v, c->d_residual, sizeof(v), cudaMemcpyDeviceToHost,
+                                       c->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  double r;
+  std::memcpy(&r, &v, sizeof(r));
+  *residual = r;
+  return st;
+}
+
 int dvm_flush_l2(dvm_ctx* c) {
   if (!c) return DVM_ERR_PARAM;
   if (!c->d_flush) {
     c->flush_n = (size_t(256) << 20) / sizeof(double);  // 256 MiB > 129 MB of L2
-    int st = dalloc(&c->d_flush, c->flush_n);
+    int st = dalloc(c, &c->d_flush, c->flush_n);
     if (st) return st;
   }
   return cuda_status(launch_flush(c->d_flush, c->flush_n, c->stream));
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------------------------------
+// Batched homogeneous instances (dvm_batch_*).
+struct dvm_batch {
+  std::vector<dvm_ctx*> groups;
+  std::vector<int> group_grid;          // grid index of each group
+  std::vector<int> inst_group, inst_cell;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint32_t* d_step = nullptr;
+  bool props_stale = true;
+  int64_t collisions_per_step = 0;
+};
+
+namespace {
+
+void batch_release(dvm_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (dvm_ctx* c : b->groups) release(c);
+  if (b->d_step) cudaFree(b->d_step);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// Launch-shape autotuner: for each group, time the persistent collision kernel at 1..4
+// CTAs per SM (bounded by occupancy) on a saved copy of the state, keep the fastest, and
+// restore the state.
+int autotune(dvm_batch* b) {
+  for (dvm_ctx* c : b->groups) {
+    const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+    // 0-D contexts never use f_conv: it holds the saved f
+    int st = cuda_status(cudaMemcpyAsync(c->d_fconv, c->d_f, bytes, cudaMemcpyDeviceToDevice,
+                                         c->stream));
+    std::vector<double> cache(static_cast<size_t>(c->ncells) * 4);
+    if (!st && c->d_eq_cache)
+      st = cuda_status(cudaMemcpyAsync(cache.data(), c->d_eq_cache, cache.size() * sizeof(double),
+                                       cudaMemcpyDeviceToHost, c->stream));
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+    if (st) return st;
+    const bool fp32 = (c->p.precision == DVM_PREC_FP32);
+    const int max_bps = fp32 ? collide_f32_blocks_per_sm(c->g, c->tabs)
+                             : collide_blocks_per_sm(collide_smem_bytes(c->g, c->tabs));
+    int best = c->num_sms * max_bps;
+    float best_ms = 1e30f;
+    for (int bps = 1; bps <= std::min(4, max_bps); ++bps) {
+      const int grid = c->num_sms * bps;
+      if (fp32) c->collide_f32_grid = grid; else c->collide_grid = grid;
+      cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {  // first pass warms up
+        cudaMemcpyAsync(c->d_f, c->d_fconv, bytes, cudaMemcpyDeviceToDevice, c->stream);
+        cudaEventRecord(e0, c->stream);
+        st = dvm_compute_collision_integral(c, 0, nullptr);
+        cudaEventRecord(e1, c->stream);
+        if (st) return st;
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+      }
+      c->ev_pool.push_back(e0);
+      c->ev_pool.push_back(e1);
+      if (ms < best_ms) { best_ms = ms; best = grid; }
+    }
+    if (fp32) c->collide_f32_grid = best; else c->collide_grid = best;
+    st = cuda_status(cudaMemcpyAsync(c->d_f, c->d_fconv, bytes, cudaMemcpyDeviceToDevice,
+                                     c->stream));
+    if (!st && c->d_eq_cache)
+      st = cuda_status(cudaMemcpyAsync(c->d_eq_cache, cache.data(), cache.size() * sizeof(double),
+                                       cudaMemcpyHostToDevice, c->stream));
+    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+    if (st) return st;
+  }
+  return DVM_OK;
+}
+
+int batch_prepare(dvm_batch* b) {
+  if (b->props_stale) {
+    for (dvm_ctx* c : b->groups) {
+      int st = dvm_calculate_physical_properties(c);
+      if (st) return st;
+    }
+    int st = cuda_status(cudaStreamSynchronize(b->stream));
+    if (st) return st;
+    b->props_stale = false;
+  }
+  if (b->exec) return DVM_OK;
+  int st = autotune(b);
+  if (st) return st;
+  // one step of every group, then the step counter, captured into one graph
+  cudaGraph_t graph = nullptr;
+  st = cuda_status(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+  if (st) return st;
+  for (dvm_ctx* c : b->groups) {
+    st = dvm_compute_collision_integral(c, 0, nullptr);
+    if (!st) st = dvm_calculate_physical_properties(c);
+    if (st) break;
+  }
+  if (!st) st = cuda_status(launch_step_end(b->d_step, nullptr, nullptr, b->stream));
+  const int st2 = cuda_status(cudaStreamEndCapture(b->stream, &graph));
+  if (st || st2) {
+    if (graph) cudaGraphDestroy(graph);
+    return st ? st : st2;
+  }
+  st = cuda_status(cudaGraphInstantiate(&b->exec, graph, 0));
+  cudaGraphDestroy(graph);
+  return st;
+}
+
+}  // namespace
+
+namespace dvm {
+
+int ctx_create(const dvm_params* p, const dvm_vgrid* vg, bool async_alloc, dvm_ctx** out) {
+  return create_context(p, vg, nullptr, async_alloc, out);
+}
+void ctx_destroy(dvm_ctx* c) { release(c); }
+cudaStream_t ctx_stream(const dvm_ctx* c) { return c->stream; }
+const unsigned long long* ctx_residual(const dvm_ctx* c) { return c->d_residual; }
+const long long* ctx_total_samples(const dvm_ctx* c) { return c->d_total_samples; }
+void ctx_set_step_dev(dvm_ctx* c, const uint32_t* step) { c->step_dev = step; }
+size_t ctx_device_bytes(const dvm_ctx* c) { return c->device_bytes; }
+
+size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
+  const size_t C = static_cast<size_t>(p->nx_space) * p->ny_space;
+  const size_t nv = static_cast<size_t>(vg->nx) * vg->ny * vg->nz;
+  const size_t d = sizeof(double);
+  size_t b = 2 * (vg->nx + vg->ny + vg->nz) * d            // axes
+             + 2 * C * nv * d + C * DVM_NPROP * d           // f, f_conv, properties
+             + sizeof(uint32_t) + nv * d                    // error word, speeds
+             + sizeof(unsigned long long);                  // residual
+  if (p->coll_method != DVM_COLL_NONE) {
+    b += 4 * C * (nv + 1) * d + C * 4 * d;                  // eq_pre, cum_eq, cum_dev, kin, cache
+    b += 2 * C * kNRef * sizeof(int2) + C * sizeof(CellPlan) +
+         (3 * C + 1) * sizeof(long long) + sizeof(long long);
+    const size_t nmax = std::max(vg->nx, std::max(vg->ny, vg->nz));
+    b += 3 * nmax * sizeof(AxisEntry) + kTrigN * sizeof(double2);
+    const bool cubic = (vg->nx == vg->ny && vg->ny == vg->nz);
+    const size_t ns = cubic ? 3 * static_cast<size_t>(vg->nx - 1) * (vg->nx - 1) + 1 : 0;
+    b += ns * sizeof(double2);
+    if (p->precision == DVM_PREC_FP32)
+      b += 3 * nmax * sizeof(AxisEntryF) + kTrigN * sizeof(float2) + ns * sizeof(float2) +
+           C * nv * sizeof(float);
+  }
+  if (p->geometry == DVM_GEOM_2D && p->conv_method == DVM_CONV_UPWIND1) {
+    size_t n = 2 * static_cast<size_t>(p->nx_space);
+    if (p->bc[DVM_WALL_LEFT] == DVM_BC2D_WALL) n += p->ny_space;
+    if (p->bc[DVM_WALL_RIGHT] == DVM_BC2D_WALL) n += p->ny_space;
+    b += n * nv * d;
+  }
+  return b;
+}
+
+}  // namespace dvm
+
+extern "C" {
+
+int dvm_footprint_bytes(const dvm_params* params, const dvm_vgrid* vgrid, uint64_t* bytes) {
+  if (!bytes) return DVM_ERR_PARAM;
+  const int st = validate(params, vgrid);
+  if (st) return st;
+  *bytes = dvm::context_bytes(params, vgrid);
+  return DVM_OK;
+}
+
+int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrids,
+                     const int32_t* instance_grid, int ninstances,
+                     const int64_t* samples_per_grid, dvm_batch** out) {
+  if (!params || !grids || !instance_grid || !samples_per_grid || !out || ngrids < 1 ||
+      ninstances < 1)
+    return DVM_ERR_PARAM;
+  if (params->coll_method == DVM_COLL_NONE) return DVM_ERR_PARAM;
+  *out = nullptr;
+  for (int i = 0; i < ninstances; ++i)
+    if (instance_grid[i] < 0 || instance_grid[i] >= ngrids) return DVM_ERR_PARAM;
+  dvm_batch* b = new (std::nothrow) dvm_batch();
+  if (!b) return DVM_ERR_OOM;
+  int st = cuda_status(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  if (!st) st = dalloc(&b->d_step, 1);
+  if (!st) st = cuda_status(cudaMemset(b->d_step, 0, sizeof(uint32_t)));
+  if (st) { batch_release(b); return st; }
+  b->inst_group.assign(ninstances, -1);
+  b->inst_cell.assign(ninstances, -1);
+  for (int gidx = 0; gidx < ngrids; ++gidx) {
+    int count = 0;
+    for (int i = 0; i < ninstances; ++i)
+      if (instance_grid[i] == gidx) {
+        b->inst_group[i] = static_cast<int>(b->groups.size());
+        b->inst_cell[i] = count++;
+      }
+    if (count == 0) continue;
+    dvm_params p = *params;
+    p.geometry = DVM_GEOM_0D;
+    p.nx_space = count;
+    p.ny_space = 1;
+    p.conv_method = DVM_CONV_NONE;
+    p.samples_mode = DVM_SAMPLES_FIXED;
+    p.samples_per_step = samples_per_grid[gidx];
+    dvm_ctx* c = nullptr;
+    st = create_context(&p, &grids[gidx], b->stream, false, &c);
+    if (st) { batch_release(b); return st; }
+    c->step_dev = b->d_step;
+    b->groups.push_back(c);
+    b->group_grid.push_back(gidx);
+    b->collisions_per_step += static_cast<int64_t>(count) * samples_per_grid[gidx];
+  }
+  *out = b;
+  return DVM_OK;
+}
+
+int dvm_batch_destroy(dvm_batch* b) {
+  if (!b) return DVM_ERR_PARAM;
+  batch_release(b);
+  return DVM_OK;
+}
+
+int dvm_batch_upload_f(dvm_batch* b, int instance, const double* f) {
+  if (!b || !f || instance < 0 || instance >= static_cast<int>(b->inst_group.size()))
+    return DVM_ERR_PARAM;
+  dvm_ctx* c = b->groups[b->inst_group[instance]];
+  const size_t nv = c->g.nv;
+  int st = cuda_status(cudaMemcpyAsync(c->d_f + b->inst_cell[instance] * nv, f,
+                                       nv * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
+  b->props_stale = true;
+  return st;
+}
+
+int dvm_batch_download_f(dvm_batch* b, int instance, double* f) {
+  if (!b || !f || instance < 0 || instance >= static_cast<int>(b->inst_group.size()))
+    return DVM_ERR_PARAM;
+  dvm_ctx* c = b->groups[b->inst_group[instance]];
+  const size_t nv = c->g.nv;
+  int st = cuda_status(cudaMemcpyAsync(f, c->d_f + b->inst_cell[instance] * nv,
+                                       nv * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
+  return st;
+}
+
+int dvm_batch_step(dvm_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return DVM_ERR_PARAM;
+  int st = batch_prepare(b);
+  if (st) return st;
+  for (int s = 0; s < nsteps; ++s) {
+    st = cuda_status(cudaGraphLaunch(b->exec, b->stream));
+    if (st) return st;
+  }
+  return DVM_OK;
+}
+
+int dvm_batch_get_properties(dvm_batch* b, double* props) {
+  if (!b || !props) return DVM_ERR_PARAM;
+  int st = cuda_status(cudaStreamSynchronize(b->stream));
+  if (st) return st;
+  for (size_t i = 0; i < b->inst_group.size(); ++i) {
+    dvm_ctx* c = b->groups[b->inst_group[i]];
+    st = cuda_status(cudaMemcpy(props + i * DVM_NPROP, c->d_props + b->inst_cell[i] * DVM_NPROP,
+                                DVM_NPROP * sizeof(double), cudaMemcpyDeviceToHost));
+    if (st) return st;
+  }
+  return DVM_OK;
+}
+
+int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisions) {
+  if (!b || !ms || nsteps < 0) return DVM_ERR_PARAM;
+  int st = batch_prepare(b);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, b->stream);
+  for (int s = 0; s < nsteps && !st; ++s) st = cuda_status(cudaGraphLaunch(b->exec, b->stream));
+  cudaEventRecord(e1, b->stream);
+  if (!st) st = cuda_status(cudaEventSynchronize(e1));
+  float t = 0.f;
+  if (!st) cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  if (collisions) *collisions = b->collisions_per_step * nsteps;
+  return st;
 }
 
 }  // extern "C"

@@ -39,6 +39,9 @@ struct CollParams {
   uint64_t seed;
 };
 
+cudaError_t launch_step_end(uint32_t* counter, long long* acc, const long long* total,
+                            cudaStream_t s);
+
 struct CdfArgs {
   GridInfo g;
   CollParams cp;
@@ -111,6 +114,7 @@ struct CollideArgs {
   CollTables t;
   int ncells;
   uint32_t step;
+  const uint32_t* step_dev;  // if set, the Philox step is read here (graph replays)
   double* f;
   const double* cum_eq;
   const double* cum_dev;
@@ -166,6 +170,9 @@ struct MomentArgs {
   const double* f;
   double* props;
   uint32_t* err;
+  // max over cells of the relative change of n, u and T since the previous moments
+  // (the convergence residual); nonnegative doubles, compared as integers
+  unsigned long long* residual;
 };
 
 // Launch wrappers (dvm_kernels.cu). Each returns the cudaGetLastError of its launch.
@@ -187,4 +194,22 @@ cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s);
 int collide_blocks_per_sm(size_t smem);
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t);
 
+}  // namespace dvm
+
+// Context hooks for the request server (dvm_server.cu); defined in dvm_api.cu.
+struct dvm_ctx;
+struct dvm_params;
+struct dvm_vgrid;
+namespace dvm {
+// A context on its own stream; async_alloc makes its buffers stream-ordered.
+int ctx_create(const dvm_params* p, const dvm_vgrid* vg, bool async_alloc, dvm_ctx** out);
+void ctx_destroy(dvm_ctx* c);
+cudaStream_t ctx_stream(const dvm_ctx* c);
+const unsigned long long* ctx_residual(const dvm_ctx* c);
+const long long* ctx_total_samples(const dvm_ctx* c);
+void ctx_set_step_dev(dvm_ctx* c, const uint32_t* step);
+size_t ctx_device_bytes(const dvm_ctx* c);
+// Device bytes a context for (p, vg) allocates (an upper bound where the grid is cubic in
+// shape but not uniform).
+size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg);
 }  // namespace dvm

@@ -544,6 +544,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   const bool vss = fabs(ralpha - 1.0) > kDoubleTol;
   // like-species pair: mass fractions m/(m+m) are exactly 1/2
   constexpr double mf = 0.5;
+  const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
 
   for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
@@ -563,7 +564,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
     double rA = 0.0, rB = 0.0;
     const bool rec = a.pairs.active;
-    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, a.step, q, 0u, rA, rB);
+    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, rA, rB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
       lA = a.pairs.glA[q][i];
@@ -619,7 +620,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
         rphi = a.pairs.rphi[q][i * NR + r];
         rcos = a.pairs.rcos[q][i * NR + r];
       } else {
-        philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, a.step, q, 1u + r, rphi, rcos);
+        philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 1u + r, rphi, rcos);
       }
       // pick_random_velocity_on_sphere (collision_utilities.f90:284-352); phi = 2 pi R:
       // R = k/kTrigN + t exactly, cos/sin of 2 pi k/kTrigN from the table, of
@@ -906,6 +907,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, Co
   const float alpha = static_cast<float>(0.5 * (a.cp.alpha + a.cp.alpha));
   const float ralpha = 1.f / alpha;
   const bool vss = fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol;
+  const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
 
   for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
@@ -924,7 +926,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, Co
 
     double rA = 0.0, rB = 0.0;
     const bool rec = a.pairs.active;
-    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, a.step, q, 0u, rA, rB);
+    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, rA, rB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
       lA = a.pairs.glA[q][i];
@@ -974,7 +976,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, Co
       } else {
         // the top 24 bits of the two uniforms the FP64 form draws from this counter
         uint32_t o[4];
-        philox4x32_10(static_cast<uint32_t>(i), cell, a.step, (q & 3u) | ((1u + r) << 2),
+        philox4x32_10(static_cast<uint32_t>(i), cell, step, (q & 3u) | ((1u + r) << 2),
                       static_cast<uint32_t>(a.cp.seed), static_cast<uint32_t>(a.cp.seed >> 32), o);
         rphi = static_cast<float>(o[1] >> 8) * 0x1.0p-24f;
         rcos = static_cast<float>(o[3] >> 8) * 0x1.0p-24f;
@@ -1597,6 +1599,10 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
   }
   block_sum<kMomAcc>(acc, s_red);
   if (threadIdx.x == 0) {
+    // the previous moments, for the residual (only this thread writes P)
+    const double n_old = P[DVM_P_DENS], t_old = P[DVM_P_TEMP];
+    const double txx_old = P[DVM_P_TXX], tyy_old = P[DVM_P_TYY];
+    const double txy_old = P[DVM_P_TXY], txz_old = P[DVM_P_TXZ], tyz_old = P[DVM_P_TYZ];
     const double n = acc[0];
     if (n == 0.0) {
       for (int q = 0; q < DVM_NPROP; ++q) P[q] = 0.0;
@@ -1638,6 +1644,25 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
     if (!isfinite(n) || !isfinite(t)) bad |= DVM_EW_NONFINITE;
     if (!(n > 0.0)) bad |= DVM_EW_NEGDENS;
     if (bad) atomicOr(a.err, bad);
+    if (a.residual) {
+      // relative change of n, u (on the thermal speed) and T since the last moments
+      const double su = sqrt(fabs(t) / m) + 1e-300;
+      double r = fabs(n - n_old) / fabs(n);
+      r = fmax(r, fabs(dx) / su);
+      r = fmax(r, fabs(dy) / su);
+      r = fmax(r, fabs(dz) / su);
+      r = fmax(r, fabs(t - t_old) / (fabs(t) + 1e-300));
+      // and of the shear stresses on the pressure (the only moments a homogeneous
+      // relaxation changes)
+      const double ip = 1.0 / (fabs(p) + 1e-300);
+      r = fmax(r, fabs(P[DVM_P_TXY] - txy_old) * ip);
+      r = fmax(r, fabs(P[DVM_P_TXZ] - txz_old) * ip);
+      r = fmax(r, fabs(P[DVM_P_TYZ] - tyz_old) * ip);
+      r = fmax(r, fabs(P[DVM_P_TXX] - txx_old) * ip);
+      r = fmax(r, fabs(P[DVM_P_TYY] - tyy_old) * ip);
+      if (!(r >= 0.0)) r = 1e300;
+      atomicMax(a.residual, static_cast<unsigned long long>(__double_as_longlong(r)));
+    }
   }
 }
 
@@ -1651,6 +1676,19 @@ __global__ void k_flush(double* buf, size_t n) {
   for (size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; t < n;
        t += static_cast<size_t>(gridDim.x) * blockDim.x)
     buf[t] = static_cast<double>(t);
+}
+
+// End of a device-counted step: advance the Philox step counter and, when asked, add the
+// step's sample total to a running count.
+__global__ void k_step_end(uint32_t* counter, long long* acc, const long long* total) {
+  *counter += 1u;
+  if (acc && total) *acc += *total;
+}
+
+cudaError_t launch_step_end(uint32_t* counter, long long* acc, const long long* total,
+                            cudaStream_t s) {
+  k_step_end<<<1, 1, 0, s>>>(counter, acc, total);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s) {

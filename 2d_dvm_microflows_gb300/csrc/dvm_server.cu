@@ -1,0 +1,405 @@
+// dvm_server.cu -- request server for independent solves (dvm_server_* in include/dvm_gpu.h).
+//
+// Continuous batching: a worker thread admits queued requests in arrival order whenever the
+// sum of the admitted requests' device footprints stays within the budget and a slot is
+// free, keeps every admitted request's f, CDFs and moments resident in its own context on
+// its own stream, and advances all admitted requests in turns of a few steps, each turn one
+// replay of a CUDA graph captured for that request. The turns of different requests run on
+// different streams, so their kernels overlap on the device. After every turn the worker
+// reads the request's convergence residual (an asynchronous 8-byte copy to pinned memory,
+// polled with an event) and retires the request once the residual reaches its tolerance or
+// its step limit is reached; its memory then goes back to the stream-ordered pool and the
+// next queued request is admitted. A request's result depends only on its own parameters,
+// seed and step count, never on what else is in the mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/dvm_gpu.h"
+#include "dvm_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+int cuda_st(cudaError_t e) {
+  if (e == cudaSuccess) return DVM_OK;
+  if (e == cudaErrorMemoryAllocation) return DVM_ERR_OOM;
+  return DVM_ERR_CUDA;
+}
+
+struct Request {
+  int64_t id = 0;
+  dvm_params p{};
+  std::vector<double> x, y, z, f0;
+  int max_steps = 0;
+  double tol = 0.0;
+  size_t bytes = 0;
+  Clock::time_point t_submit, t_admit, t_done;
+  // while admitted
+  dvm_ctx* ctx = nullptr;
+  cudaStream_t stream = nullptr;
+  uint32_t* d_step = nullptr;
+  long long* d_acc = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int quantum = 0;
+  cudaEvent_t ev = nullptr;
+  int slot = -1;
+  bool inflight = false;
+  int steps_issued = 0;
+  int steps_done = 0;
+  bool eager_tail = false;  // an odd last step was issued outside the graph
+  // result
+  int status = DVM_OK;
+  int converged = 0;
+  double residual = 0.0;
+  long long collisions = 0;
+  uint64_t device_bytes = 0;
+  std::vector<double> props, f;
+  bool done = false;
+
+  dvm_vgrid vgrid() const {
+    dvm_vgrid v;
+    v.nx = static_cast<int32_t>(x.size());
+    v.ny = static_cast<int32_t>(y.size());
+    v.nz = static_cast<int32_t>(z.size());
+    v.x = x.data();
+    v.y = y.data();
+    v.z = z.data();
+    return v;
+  }
+  size_t ncells() const { return static_cast<size_t>(p.nx_space) * p.ny_space; }
+  size_t nv() const { return x.size() * y.size() * z.size(); }
+};
+
+}  // namespace
+
+struct dvm_server {
+  uint64_t budget = 0;
+  int max_active = 1;
+  int quantum = 2;
+  int device = 0;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<Request>> pending;  // submitted, not yet admitted
+  std::map<int64_t, std::shared_ptr<Request>> all;
+  std::vector<std::shared_ptr<Request>> active;  // worker thread only
+  int64_t next_id = 1;
+  bool stop = false;
+  std::thread worker;
+  double* h_slots = nullptr;  // pinned, one residual per slot
+  std::vector<int> free_slots;
+  uint64_t used = 0;          // worker thread only
+  // statistics
+  int64_t completed = 0;
+  int peak_active = 0;
+  uint64_t peak_bytes = 0;
+};
+
+namespace {
+
+// One request step outside any graph: collision, convection, moments, step counter.
+int eager_step(Request& r) {
+  int st = dvm_compute_collision_integral(r.ctx, 0, nullptr);
+  if (!st) st = dvm_compute_convection(r.ctx);
+  if (!st) st = dvm_calculate_physical_properties(r.ctx);
+  if (!st)
+    st = cuda_st(dvm::launch_step_end(r.d_step, r.d_acc, dvm::ctx_total_samples(r.ctx),
+                                      r.stream));
+  return st;
+}
+
+int capture_quantum(Request& r) {
+  cudaGraph_t graph = nullptr;
+  int st = cuda_st(cudaStreamBeginCapture(r.stream, cudaStreamCaptureModeRelaxed));
+  if (st) return st;
+  for (int s = 0; s < r.quantum && !st; ++s) st = eager_step(r);
+  const int st2 = cuda_st(cudaStreamEndCapture(r.stream, &graph));
+  if (!st) st = st2;
+  if (!st) st = cuda_st(cudaGraphInstantiate(&r.exec, graph, 0));
+  if (graph) cudaGraphDestroy(graph);
+  return st;
+}
+
+int admit(dvm_server* sv, Request& r) {
+  dvm_vgrid vg = r.vgrid();
+  int st = dvm::ctx_create(&r.p, &vg, true, &r.ctx);
+  if (st) return st;
+  r.stream = dvm::ctx_stream(r.ctx);
+  r.device_bytes = dvm::ctx_device_bytes(r.ctx);
+  st = cuda_st(cudaMallocAsync(reinterpret_cast<void**>(&r.d_step), sizeof(uint32_t), r.stream));
+  if (!st)
+    st = cuda_st(cudaMallocAsync(reinterpret_cast<void**>(&r.d_acc), sizeof(long long), r.stream));
+  if (st) return st;
+  cudaMemsetAsync(r.d_step, 0, sizeof(uint32_t), r.stream);
+  cudaMemsetAsync(r.d_acc, 0, sizeof(long long), r.stream);
+  dvm::ctx_set_step_dev(r.ctx, r.d_step);
+  st = dvm_upload_f(r.ctx, r.f0.data());  // also computes the initial moments
+  if (st) return st;
+  std::vector<double>().swap(r.f0);
+  // an even number of steps per graph when convection swaps f and f_conv
+  r.quantum = sv->quantum;
+  if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) ++r.quantum;
+  r.quantum = std::min(r.quantum, std::max(1, r.max_steps));
+  if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) r.quantum = 0;  // eager only
+  if (r.quantum > 0) st = capture_quantum(r);
+  if (!st) st = cuda_st(cudaEventCreateWithFlags(&r.ev, cudaEventDisableTiming));
+  return st;
+}
+
+// Issues the next turn of a request: one graph replay, or single eager steps for a tail
+// shorter than the graph (after which the graph is not replayed again).
+int issue(dvm_server* sv, Request& r) {
+  const int left = r.max_steps - r.steps_issued;
+  int n = 0, st = DVM_OK;
+  if (r.quantum > 0 && !r.eager_tail && left >= r.quantum) {
+    st = cuda_st(cudaGraphLaunch(r.exec, r.stream));
+    n = r.quantum;
+  } else {
+    r.eager_tail = true;
+    st = eager_step(r);
+    n = 1;
+  }
+  if (!st)
+    st = cuda_st(cudaMemcpyAsync(sv->h_slots + r.slot, dvm::ctx_residual(r.ctx), sizeof(double),
+                                 cudaMemcpyDeviceToHost, r.stream));
+  if (!st) st = cuda_st(cudaEventRecord(r.ev, r.stream));
+  if (!st) {
+    r.steps_issued += n;
+    r.inflight = true;
+  }
+  return st;
+}
+
+void retire(dvm_server* sv, Request& r) {
+  if (r.ctx) {
+    if (r.status == DVM_OK) {
+      r.props.resize(r.ncells() * DVM_NPROP);
+      r.f.resize(r.ncells() * r.nv());
+      int st = dvm_get_properties(r.ctx, r.props.data());
+      if (!st) st = dvm_download_f(r.ctx, r.f.data());
+      uint32_t err = 0;
+      if (!st) st = dvm_get_error_word(r.ctx, &err);
+      if (!st && err) st = DVM_ERR_NUMERIC;
+      if (!st)
+        st = cuda_st(cudaMemcpyAsync(&r.collisions, r.d_acc, sizeof(long long),
+                                     cudaMemcpyDeviceToHost, r.stream));
+      r.status = st;
+    }
+    cudaStreamSynchronize(r.stream);
+    if (r.exec) cudaGraphExecDestroy(r.exec);
+    if (r.ev) cudaEventDestroy(r.ev);
+    if (r.d_step) cudaFreeAsync(r.d_step, r.stream);
+    if (r.d_acc) cudaFreeAsync(r.d_acc, r.stream);
+    dvm::ctx_destroy(r.ctx);
+    r.ctx = nullptr;
+  }
+  if (r.slot >= 0) sv->free_slots.push_back(r.slot);
+  r.slot = -1;
+  sv->used -= r.bytes;
+  r.t_done = Clock::now();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  r.done = true;
+  sv->completed++;
+  sv->cv_done.notify_all();
+}
+
+void worker_loop(dvm_server* sv) {
+  cudaSetDevice(sv->device);
+  for (;;) {
+    // admission, in arrival order, while the footprint budget and a slot allow
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      if (sv->active.empty() && sv->pending.empty()) {
+        if (sv->stop) return;
+        sv->cv_work.wait(lk, [&] { return sv->stop || !sv->pending.empty(); });
+        if (sv->pending.empty()) return;
+      }
+      while (!sv->pending.empty() && static_cast<int>(sv->active.size()) < sv->max_active &&
+             sv->used + sv->pending.front()->bytes <= sv->budget) {
+        std::shared_ptr<Request> r = sv->pending.front();
+        sv->pending.pop_front();
+        lk.unlock();
+        r->t_admit = Clock::now();
+        r->slot = sv->free_slots.back();
+        sv->free_slots.pop_back();
+        sv->used += r->bytes;
+        r->status = admit(sv, *r);
+        if (r->status) {
+          retire(sv, *r);
+          lk.lock();
+        } else {
+          sv->active.push_back(r);
+          lk.lock();
+          sv->peak_active = std::max(sv->peak_active, static_cast<int>(sv->active.size()));
+          sv->peak_bytes = std::max(sv->peak_bytes, sv->used);
+        }
+      }
+    }
+    bool progress = false;
+    for (auto& rp : sv->active) {
+      Request& r = *rp;
+      if (r.inflight) {
+        const cudaError_t q = cudaEventQuery(r.ev);
+        if (q == cudaErrorNotReady) continue;
+        r.inflight = false;
+        progress = true;
+        r.steps_done = r.steps_issued;
+        if (q != cudaSuccess) {
+          r.status = DVM_ERR_CUDA;
+        } else {
+          r.residual = sv->h_slots[r.slot];
+          if (r.residual <= r.tol) r.converged = 1;
+        }
+        if (r.status || r.converged || r.steps_done >= r.max_steps) {
+          retire(sv, r);
+          continue;
+        }
+      }
+      if (!r.done && !r.inflight) {
+        r.status = issue(sv, r);
+        if (r.status) retire(sv, r);
+        progress = true;
+      }
+    }
+    sv->active.erase(std::remove_if(sv->active.begin(), sv->active.end(),
+                                    [](const std::shared_ptr<Request>& r) { return r->done; }),
+                     sv->active.end());
+    if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+int dvm_server_create(uint64_t hbm_budget_bytes, int max_active, int steps_per_turn,
+                      dvm_server** out) {
+  if (!out || hbm_budget_bytes == 0 || max_active < 1 || steps_per_turn < 1)
+    return DVM_ERR_PARAM;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return DVM_ERR_NODEVICE;
+  dvm_server* sv = new (std::nothrow) dvm_server();
+  if (!sv) return DVM_ERR_OOM;
+  sv->budget = hbm_budget_bytes;
+  sv->max_active = max_active;
+  sv->quantum = steps_per_turn;
+  cudaGetDevice(&sv->device);
+  if (cudaHostAlloc(reinterpret_cast<void**>(&sv->h_slots), sizeof(double) * max_active,
+                    cudaHostAllocDefault) != cudaSuccess) {
+    delete sv;
+    return DVM_ERR_OOM;
+  }
+  for (int i = max_active - 1; i >= 0; --i) sv->free_slots.push_back(i);
+  // freed request memory stays in this process's stream-ordered pool for the next request
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, sv->device) == cudaSuccess) {
+    uint64_t keep = hbm_budget_bytes;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  sv->worker = std::thread(worker_loop, sv);
+  *out = sv;
+  return DVM_OK;
+}
+
+int dvm_server_destroy(dvm_server* sv) {
+  if (!sv) return DVM_ERR_PARAM;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+  }
+  sv->cv_work.notify_all();
+  if (sv->worker.joinable()) sv->worker.join();
+  cudaFreeHost(sv->h_slots);
+  delete sv;
+  return DVM_OK;
+}
+
+int dvm_server_submit(dvm_server* sv, const dvm_params* params, const dvm_vgrid* vgrid,
+                      const double* f0, int32_t max_steps, double residual_tol, int64_t* id) {
+  if (!sv || !params || !vgrid || !f0 || !id || max_steps < 1) return DVM_ERR_PARAM;
+  uint64_t bytes = 0;
+  int st = dvm_footprint_bytes(params, vgrid, &bytes);
+  if (st) return st;
+  bytes += sizeof(uint32_t) + sizeof(long long);
+  if (bytes > sv->budget) return DVM_ERR_TOO_LARGE;
+  auto r = std::make_shared<Request>();
+  r->t_submit = Clock::now();
+  r->p = *params;
+  r->x.assign(vgrid->x, vgrid->x + vgrid->nx);
+  r->y.assign(vgrid->y, vgrid->y + vgrid->ny);
+  r->z.assign(vgrid->z, vgrid->z + vgrid->nz);
+  r->f0.assign(f0, f0 + r->ncells() * r->nv());
+  r->max_steps = max_steps;
+  r->tol = residual_tol;
+  r->bytes = bytes;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop) return DVM_ERR_PARAM;
+    r->id = sv->next_id++;
+    sv->all[r->id] = r;
+    sv->pending.push_back(r);
+  }
+  sv->cv_work.notify_one();
+  *id = r->id;
+  return DVM_OK;
+}
+
+int dvm_server_wait(dvm_server* sv, int64_t id, dvm_request_info* info) {
+  if (!sv || !info) return DVM_ERR_PARAM;
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->all.find(id);
+  if (it == sv->all.end()) return DVM_ERR_PARAM;
+  std::shared_ptr<Request> r = it->second;
+  sv->cv_done.wait(lk, [&] { return r->done; });
+  std::memset(info, 0, sizeof(*info));
+  info->status = r->status;
+  info->converged = r->converged;
+  info->steps = r->steps_done;
+  info->residual = r->residual;
+  info->queue_ms = ms_between(r->t_submit, r->t_admit);
+  info->latency_ms = ms_between(r->t_submit, r->t_done);
+  info->collisions = r->collisions;
+  info->device_bytes = r->device_bytes;
+  return DVM_OK;
+}
+
+int dvm_server_result(dvm_server* sv, int64_t id, double* props, double* f) {
+  if (!sv) return DVM_ERR_PARAM;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  auto it = sv->all.find(id);
+  if (it == sv->all.end() || !it->second->done) return DVM_ERR_PARAM;
+  Request& r = *it->second;
+  if (r.status) return r.status;
+  if (props) std::memcpy(props, r.props.data(), r.props.size() * sizeof(double));
+  if (f) std::memcpy(f, r.f.data(), r.f.size() * sizeof(double));
+  sv->all.erase(it);
+  return DVM_OK;
+}
+
+int dvm_server_stats(dvm_server* sv, int64_t* completed, int32_t* peak_active,
+                     uint64_t* peak_bytes) {
+  if (!sv) return DVM_ERR_PARAM;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (completed) *completed = sv->completed;
+  if (peak_active) *peak_active = sv->peak_active;
+  if (peak_bytes) *peak_bytes = sv->peak_bytes;
+  return DVM_OK;
+}
+
+}  // extern "C"

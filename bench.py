@@ -345,6 +345,228 @@ def run_forms(pkg, args, fp64_value):
     return out
 
 
+BATCH_GRIDS = (16, 24, 32, 40)
+BATCH_INSTANCES = 256
+BATCH_SAMPLES_24 = 100000  # samples per instance-step on 24^3; proportional to N_v
+
+
+def batch_workload(pkg, ninst=BATCH_INSTANCES, seed=SEED):
+    """256 homogeneous relaxations: grids drawn uniformly from {16,24,32,40}^3 on [-5,5],
+    bimodal starts (weights 1/2, temperature ratio ~U[1,4], x-drift +-U[0,1.5]), samples per
+    step 1e5 * N_v / 24^3."""
+    ph = pkg.physics
+    grids = [ph.VelocityGrid.uniform(n, -5.0, 5.0) for n in BATCH_GRIDS]
+    samples = [int(BATCH_SAMPLES_24 * (n / 24.0) ** 3) for n in BATCH_GRIDS]
+    rng = np.random.default_rng(seed)
+    gid = rng.integers(0, len(grids), ninst).astype(np.int32)
+    f0 = []
+    for i in range(ninst):
+        g = grids[gid[i]]
+        tr, u = rng.uniform(1.0, 4.0), rng.uniform(0.0, 1.5)
+        f0.append(0.5 * ph.maxwellian(g, 1.0, u, 0.0, 0.0, 1.0) +
+                  0.5 * ph.maxwellian(g, 1.0, -u, 0.0, 0.0, tr))
+    cfg = pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, deltat=0.01, seed=seed)
+    return cfg, grids, gid, samples, f0
+
+
+def run_batch(pkg, args):
+    """The batched form (one CUDA-graph replay per step over all instances, autotuned
+    persistent launches) in FP32+projection and FP64, beside the plain FP64 path that steps
+    each instance through its own context, one dvm_step call per instance-step."""
+    import dataclasses
+    cfg, grids, gid, samples, f0 = batch_workload(pkg)
+    per_step = int(sum(samples[q] for q in gid))
+    out = {"workload": "%d homogeneous relaxations, grids {16,24,32,40}^3 on [-5,5], bimodal "
+                       "T-ratio U[1,4], drift U[0,1.5], VR hard sphere, dt 0.01, samples "
+                       "1e5*N_v/24^3 per instance-step" % len(gid),
+           "collisions_per_step": per_step,
+           "grid_counts": {"%d^3" % n: int((gid == q).sum()) for q, n in enumerate(BATCH_GRIDS)}}
+    props = {}
+    for name, prec in (("fp32_batched", pkg.DVM_PREC_FP32), ("fp64_batched", pkg.DVM_PREC_FP64)):
+        b = pkg.DVMBatch(dataclasses.replace(cfg, precision=prec), grids, gid, samples)
+        for i, f in enumerate(f0):
+            b.upload_f(i, f)
+        b.step(args.warmup)  # capture, autotune and warm up
+        ms_dev, colls = b.time_steps(args.steps)
+        t0 = time.perf_counter()
+        b.step(args.steps)
+        b.properties()
+        wall = time.perf_counter() - t0
+        props[name] = b.properties()
+        out[name] = {"value": colls / (ms_dev * 1e-3), "unit": "collisions/s",
+                     "ms_per_step": ms_dev / args.steps,
+                     "wall_collisions_per_s": per_step * args.steps / wall,
+                     "instance_updates_per_s": len(gid) * args.steps / wall}
+        b.close()
+    out["moment_err_fp32_vs_fp64"] = moment_error(props["fp32_batched"], props["fp64_batched"])
+    out["steps_compared"] = 2 * args.steps + args.warmup
+    # plain FP64: one context per instance, stepped one after another
+    solvers = []
+    for i, f in enumerate(f0):
+        c = dataclasses.replace(cfg, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                samples_per_step=samples[gid[i]])
+        s = pkg.DVMSolver(c, grids[gid[i]])
+        s.initialize_dist_func(f)
+        solvers.append(s)
+    for s in solvers:
+        s.solve(1)
+    for s in solvers:
+        s.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in solvers:
+            s.solve(1)
+    for s in solvers:
+        s.synchronize()
+    wall = time.perf_counter() - t0
+    out["fp64_plain"] = {"value": per_step * args.steps / wall, "unit": "collisions/s",
+                         "ms_per_step": wall * 1e3 / args.steps,
+                         "instance_updates_per_s": len(gid) * args.steps / wall}
+    for s in solvers:
+        s.close()
+    out["speedup_fp32_batched_vs_fp64_plain"] = (out["fp32_batched"]["wall_collisions_per_s"] /
+                                                 out["fp64_plain"]["value"])
+    out["timing"] = ("batched value: CUDA events around graph replays; wall_*: host clock "
+                     "around the same replays; fp64_plain: host clock; working set > L2")
+    return out
+
+
+SERVE_REQUESTS = 40
+SERVE_RATE = 50.0        # Poisson arrivals per second
+SERVE_MAX_STEPS = 40
+SERVE_TOL = 1e-6
+SERVE_BUDGET = 64 << 30  # admission budget, bytes of HBM
+SERVE_SLOTS = 16
+
+
+def serving_workload(pkg, nreq=SERVE_REQUESTS, seed=SEED):
+    """Poisson arrivals (50 req/s) of mixed requests: 60% 1-D shocks (Mach ~U[1.2,4],
+    100-400 cells, 24^3-32^3 grids, 2e4 samples per cell-step), 40% 2-D lid-driven cavities
+    (Kn ~logU[0.01,1], 32x32-96x96 cells, 16^3-24^3 grids, 4e3 samples per cell-step).
+    Returns [(arrival_s, config, grid, f0, kind)] in arrival order."""
+    ph = pkg.physics
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    mol = ph.molecule("Ar", ph.CSECTION_VHS)
+    for i in range(nreq):
+        t += rng.exponential(1.0 / SERVE_RATE)
+        if rng.random() < 0.6:
+            mach = rng.uniform(1.2, 4.0)
+            cells = int(rng.integers(100, 401))
+            n = int(rng.choice([24, 28, 32]))
+            vmax = 4.0 + 1.6 * mach
+            g = ph.VelocityGrid.uniform(n, -vmax, vmax)
+            f0, up, dn = ph.shock_profile(g, cells, 0.5, mach, 10.0)
+            walls = ((dn["n"], dn["u"], 0.0, 0.0, dn["T"]), (up["n"], up["u"], 0.0, 0.0, up["T"]),
+                     (1.0, 0.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 0.0, 1.0))
+            cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=cells, dx=0.5,
+                                deltat=0.9 * 0.5 / vmax, Kn=1.0, mass=mol["mass"],
+                                omega=mol["omega"], alpha=mol["alpha"],
+                                sigma=ph.cross_section(mol, ph.CSECTION_BIRD),
+                                iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                                samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=20000,
+                                bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), walls=walls,
+                                seed=seed + i)
+            kind = "shock M=%.2f %d cells %d^3" % (mach, cells, n)
+        else:
+            kn = 10.0 ** rng.uniform(-2.0, 0.0)
+            side = int(rng.choice([32, 48, 64, 80, 96]))
+            n = int(rng.choice([16, 20, 24]))
+            g = ph.VelocityGrid.uniform(n, -5.0, 5.0)
+            f0 = np.tile(ph.maxwellian(g, 1.0, 0.0, 0.0, 0.0, 1.0), (side * side, 1))
+            walls = ((1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0.3, 0, 0, 1.0))
+            cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_2D, nx_space=side, ny_space=side,
+                                dx=1.0 / side, dy=1.0 / side, deltat=0.9 / (side * 5.0 * 2.0),
+                                Kn=kn, iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                                samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=4000,
+                                walls=walls, seed=seed + i)
+            kind = "cavity Kn=%.3f %dx%d %d^3" % (kn, side, side, n)
+        out.append((t, cfg, g, f0, kind))
+    return out
+
+
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v), q))
+
+
+def run_serving(pkg, args):
+    """The served stream through the native request server (FP32+projection, continuous
+    batching, admission by footprint) beside the plain FP64 path (one solve at a time in
+    arrival order, a FIFO queue: latency = wait + service, service timed for real)."""
+    import dataclasses
+    reqs = serving_workload(pkg)
+    # served: submissions at their arrival times
+    served = []
+    with pkg.DVMServer(SERVE_BUDGET, max_active=SERVE_SLOTS, steps_per_turn=2) as sv:
+        t0 = time.perf_counter()
+        ids = []
+        for t, cfg, g, f0, _ in reqs:
+            dt = t0 + t - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(sv.submit(dataclasses.replace(cfg, precision=pkg.DVM_PREC_FP32), g, f0,
+                                 SERVE_MAX_STEPS, SERVE_TOL))
+        for rid in ids:
+            info = sv.wait(rid)
+            props, _ = sv.result(rid)
+            served.append((info, props))
+        t_end = time.perf_counter()
+        stats = sv.stats()
+    window = t_end - t0
+    colls = sum(i["collisions"] for i, _ in served)
+    cells = sum((c.nx_space * c.ny_space) * i["steps"] for (_, c, _, _, _), (i, _) in
+                zip(reqs, served))
+    lat = [i["latency_ms"] for i, _ in served]
+    out = {"workload": "%d requests, Poisson %.0f req/s: 60%% 1-D shocks (Mach U[1.2,4], "
+                       "100-400 cells, 24^3-32^3, 2e4 samples/cell-step), 40%% 2-D cavities "
+                       "(Kn logU[0.01,1], 32^2-96^2 cells, 16^3-24^3, 4e3 samples/cell-step); "
+                       "each to residual %g or %d steps" % (len(reqs), SERVE_RATE, SERVE_TOL,
+                                                            SERVE_MAX_STEPS),
+           "served_fp32": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+                           "collisions_per_s": colls / window,
+                           "cell_updates_per_s": cells / window,
+                           "requests_per_s": len(reqs) / window,
+                           "converged": sum(i["converged"] for i, _ in served),
+                           "peak_active": stats["peak_active"],
+                           "peak_bytes": stats["peak_bytes"], "budget_bytes": SERVE_BUDGET,
+                           "statuses": sorted(set(i["status"] for i, _ in served))}}
+    # plain FP64: one solve at a time, per-step residual check
+    finish, lat_p, colls_p, cells_p, err = 0.0, [], 0, 0, []
+    first = reqs[0][0]
+    for (t, cfg, g, f0, _), (info, props32) in zip(reqs, served):
+        ts = time.perf_counter()
+        s = pkg.DVMSolver(cfg, g)
+        s.initialize_dist_func(f0)
+        steps = 0
+        while steps < SERVE_MAX_STEPS:
+            s.solve(1)
+            steps += 1
+            colls_p += s.collision_count()
+            if s.residual() <= SERVE_TOL:
+                break
+        props64 = s.properties()
+        s.close()
+        service = time.perf_counter() - ts
+        finish = max(finish, t) + service
+        lat_p.append((finish - t) * 1e3)
+        cells_p += cfg.nx_space * cfg.ny_space * steps
+        err.append(moment_error(props32, props64))
+    span = finish - min(first, 0.0)
+    out["plain_fp64"] = {"p50_ms": _pct(lat_p, 50), "p99_ms": _pct(lat_p, 99),
+                         "collisions_per_s": colls_p / span, "cell_updates_per_s": cells_p / span,
+                         "requests_per_s": len(reqs) / span}
+    fields = err[0]["per_field"].keys()
+    out["moment_err_served_fp32_vs_plain_fp64"] = {
+        "max": max(e["max"] for e in err),
+        "per_field": {k: max(e["per_field"][k] for e in err) for k in fields}}
+    out["speedup_collisions"] = (out["served_fp32"]["collisions_per_s"] /
+                                 out["plain_fp64"]["collisions_per_s"])
+    out["speedup_cell_updates"] = (out["served_fp32"]["cell_updates_per_s"] /
+                                   out["plain_fp64"]["cell_updates_per_s"])
+    return out
+
+
 def run_gpu(args):
     ws, rank, local = dist_env()
     if ws > 1:
@@ -439,6 +661,8 @@ def run_gpu(args):
     }
     if ws == 1 and not args.no_forms:
         line["forms"] = run_forms(pkg, args, value)
+        line["forms"]["batched"] = run_batch(pkg, args)
+        line["forms"]["served"] = run_serving(pkg, args)
     if ws == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle as O

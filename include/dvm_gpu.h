@@ -40,7 +40,7 @@ enum {
   DVM_ERR_NUMERIC = 4,    /* device error word set (see dvm_get_error_word)          */
   DVM_ERR_TIMEOUT = 5,    /* a bounded device wait ran out                           */
   DVM_ERR_NODEVICE = 6,   /* no CUDA device                                          */
-  DVM_ERR_TOO_LARGE = 7   /* problem exceeds dvm_collide_noalloc's fixed scratch      */
+  DVM_ERR_TOO_LARGE = 7   /* problem exceeds a fixed scratch or a server's budget     */
 };
 
 /* Bits of the device error word. */
@@ -187,6 +187,77 @@ int dvm_set_properties(dvm_ctx* ctx, const double* props);
 int dvm_step(dvm_ctx* ctx, uint64_t first_step, int nsteps);
 /* Collision samples drawn by the last collision call, summed over cells (tot_colls). */
 int dvm_last_collision_count(dvm_ctx* ctx, int64_t* count);
+
+/* Convergence residual of the last dvm_calculate_physical_properties: the largest, over
+ * cells, relative change of n, u (on the thermal speed), T and the stress tensor (on the
+ * pressure) since the moments before it.
+ * No reference counterpart (the reference runs a fixed number of steps). */
+int dvm_get_residual(dvm_ctx* ctx, double* residual);
+
+/* ---- batched homogeneous instances --------------------------------------------------- */
+/* Many independent 0-D relaxations (the reference's homogeneous case, nx_space = ny_space =
+ * 1, run for many initial states and grids at once). No reference counterpart. Instances on
+ * the same velocity grid form one group (one context whose cells are the instances); every
+ * group shares one stream, and one step of all groups is captured into a single CUDA graph
+ * on the first dvm_batch_step and replayed after. The persistent collision launch of each
+ * group is sized by a timing autotuner at that point. params gives the common settings
+ * (collision method, dt, Kn, species, precision, seed); samples_per_grid[g] is the fixed
+ * sample count per instance-step on grid g. */
+typedef struct dvm_batch dvm_batch;
+int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrids,
+                     const int32_t* instance_grid, int ninstances,
+                     const int64_t* samples_per_grid, dvm_batch** out);
+int dvm_batch_destroy(dvm_batch* b);
+/* f of one instance ([Nv] of its grid); properties are computed at the next step. */
+int dvm_batch_upload_f(dvm_batch* b, int instance, const double* f);
+int dvm_batch_download_f(dvm_batch* b, int instance, double* f);
+int dvm_batch_step(dvm_batch* b, int nsteps);
+/* props[ninstances][DVM_NPROP] */
+int dvm_batch_get_properties(dvm_batch* b, double* props);
+/* Device time of nsteps graph replays (ms) and the samples they drew. */
+int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisions);
+
+/* ---- request server ------------------------------------------------------------------ */
+/* Device bytes a context for (params, vgrid) allocates; the server admits by this figure.
+ * No reference counterpart. */
+int dvm_footprint_bytes(const dvm_params* params, const dvm_vgrid* vgrid, uint64_t* bytes);
+
+/* Independent solves (any geometry, grid, Knudsen or Mach number) served with continuous
+ * batching. No reference counterpart: the reference runs one solve per process. A worker
+ * thread admits submitted requests in arrival order while the admitted footprints fit in
+ * hbm_budget_bytes and fewer than max_active run; each admitted request keeps its state on
+ * the device in its own context and stream and advances steps_per_turn steps per turn (one
+ * CUDA-graph replay), so the turns of different requests overlap on the device. A request
+ * ends when the convergence residual (dvm_get_residual) is <= residual_tol or after
+ * max_steps steps. Its result depends only on its own parameters, seed and step count. */
+typedef struct dvm_server dvm_server;
+typedef struct dvm_request_info {
+  int32_t status;         /* DVM_OK or the status that ended the request               */
+  int32_t converged;      /* 1: the residual reached the tolerance                     */
+  int32_t steps;          /* steps taken                                               */
+  int32_t reserved;
+  double residual;        /* residual after the last step                              */
+  double queue_ms;        /* submission to admission                                   */
+  double latency_ms;      /* submission to result ready on the host                    */
+  int64_t collisions;     /* Monte Carlo samples drawn                                 */
+  uint64_t device_bytes;  /* bytes the request's context allocated                     */
+} dvm_request_info;
+
+int dvm_server_create(uint64_t hbm_budget_bytes, int max_active, int steps_per_turn,
+                      dvm_server** out);
+/* Waits for every submitted request to finish, then frees the server. */
+int dvm_server_destroy(dvm_server* server);
+/* f0[cells][Nv] is copied; returns DVM_ERR_TOO_LARGE if the request alone exceeds the
+ * budget. */
+int dvm_server_submit(dvm_server* server, const dvm_params* params, const dvm_vgrid* vgrid,
+                      const double* f0, int32_t max_steps, double residual_tol, int64_t* id);
+/* Blocks until request id has finished. */
+int dvm_server_wait(dvm_server* server, int64_t id, dvm_request_info* info);
+/* Copies the finished request's properties [cells][DVM_NPROP] and f [cells][Nv] (either may
+ * be NULL) and forgets the request. */
+int dvm_server_result(dvm_server* server, int64_t id, double* props, double* f);
+int dvm_server_stats(dvm_server* server, int64_t* completed, int32_t* peak_active,
+                     uint64_t* peak_bytes);
 
 /* ---- errors, synchronisation, instrumentation -------------------------------------- */
 int dvm_synchronize(dvm_ctx* ctx);

@@ -46,10 +46,11 @@ def test_struct_layout_matches_header(tmp_path, pkg):
 #include <stddef.h>
 #include "dvm_gpu.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(dvm_params), sizeof(dvm_vgrid),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(dvm_params), sizeof(dvm_vgrid),
          sizeof(dvm_pairlist), offsetof(dvm_params, samples_per_step),
          offsetof(dvm_params, dx), offsetof(dvm_params, wall), offsetof(dvm_pairlist, r_cos),
-         offsetof(dvm_params, precision));
+         offsetof(dvm_params, precision), sizeof(dvm_request_info),
+         offsetof(dvm_request_info, collisions));
   return 0;
 }''')
     exe = tmp_path / "sz"
@@ -61,7 +62,8 @@ int main(void) {
     want = [C.sizeof(a.dvm_params), C.sizeof(a.dvm_vgrid), C.sizeof(a.dvm_pairlist),
             a.dvm_params.samples_per_step.offset, a.dvm_params.dx.offset,
             a.dvm_params.wall.offset, a.dvm_pairlist.r_cos.offset,
-            a.dvm_params.precision.offset]
+            a.dvm_params.precision.offset, C.sizeof(a.dvm_request_info),
+            a.dvm_request_info.collisions.offset]
     assert got == want
 
 

@@ -1,0 +1,92 @@
+"""Batched homogeneous relaxations (dvm_batch_*): instances on several velocity grids, one
+CUDA-graph replay per step, autotuned persistent launches. Each instance must evolve exactly
+as it does in a plain multi-cell 0-D context holding its grid's instances (same kernels, same
+Philox counters), the autotuner must leave the state untouched, and the FP32 form must stay
+within 1e-3 of FP64 per moment field."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(ph, grids, ninst, seed):
+    rng = np.random.default_rng(seed)
+    gid = rng.integers(0, len(grids), ninst).astype(np.int32)
+    f0 = []
+    for i in range(ninst):
+        g = grids[gid[i]]
+        tr = rng.uniform(1.0, 4.0)
+        u = rng.uniform(0.0, 1.5)
+        f0.append(0.5 * ph.maxwellian(g, 1.0, u, 0.0, 0.0, 1.0) +
+                  0.5 * ph.maxwellian(g, 1.0, -u, 0.0, 0.0, tr))
+    return gid, f0
+
+
+def _cfg(pkg, prec, seed=5):
+    return pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, deltat=0.01, seed=seed, precision=prec)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_batch_matches_grouped_contexts(gpulib, pkg, prec):
+    ph = pkg.physics
+    prec = pkg.DVM_PREC_FP64 if prec == "fp64" else pkg.DVM_PREC_FP32
+    grids = [ph.VelocityGrid.uniform(12, -5.0, 5.0), ph.VelocityGrid.uniform(16, -5.0, 5.0)]
+    samples = [20000, 40000]
+    gid, f0 = _instances(ph, grids, 9, 1)
+    batch = pkg.DVMBatch(_cfg(pkg, prec), grids, gid, samples)
+    for i, f in enumerate(f0):
+        batch.upload_f(i, f)
+    batch.step(3)
+    pb = batch.properties()
+    for q, g in enumerate(grids):
+        members = np.flatnonzero(gid == q)
+        cfg = _cfg(pkg, prec)
+        cfg.nx_space = len(members)
+        cfg.samples_mode = pkg.DVM_SAMPLES_FIXED
+        cfg.samples_per_step = samples[q]
+        s = pkg.DVMSolver(cfg, g)
+        s.initialize_dist_func(np.stack([f0[i] for i in members]))
+        s.solve(3)
+        ps, fs = s.properties(), s.phi()
+        # FP64 scatters in FP64 atomics (order effects at round-off); the FP32 form's FP32
+        # atomics round in arrival order, so two runs agree to FP32 rounding of the increment
+        ftol, ptol = (1e-12, 1e-11) if prec == pkg.DVM_PREC_FP64 else (1e-5, 1e-6)
+        for c, i in enumerate(members):
+            fb = batch.download_f(i)
+            assert np.abs(fb - fs[c]).max() <= ftol * np.abs(fs[c]).max(), (q, i)
+            assert np.abs(pb[i, :17] - ps[c, :17]).max() <= ptol * max(1.0, np.abs(ps[c]).max())
+
+
+def test_batch_fp32_moments_within_bar(gpulib, pkg):
+    ph = pkg.physics
+    grids = [ph.VelocityGrid.uniform(n, -5.0, 5.0) for n in (16, 24)]
+    samples = [int(1e5 * (n / 24.0) ** 3) for n in (16, 24)]
+    gid, f0 = _instances(ph, grids, 12, 2)
+    out = []
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        b = pkg.DVMBatch(_cfg(pkg, prec, seed=11), grids, gid, samples)
+        for i, f in enumerate(f0):
+            b.upload_f(i, f)
+        b.step(10)
+        out.append(b.properties())
+    p64, p32 = out
+    n, T = p64[:, 0:1], p64[:, 4:5]
+    scale = np.concatenate([n, np.sqrt(T).repeat(3, 1), T.repeat(2, 1), np.sqrt(T),
+                            0.5 * n * T, (n * T ** 1.5).repeat(3, 1), (0.5 * n * T).repeat(6, 1)],
+                           axis=1)
+    err = (np.abs(p32[:, :17] - p64[:, :17]) / scale).max(0)
+    assert err.max() <= 1e-3, dict(zip(pkg.PROP_NAMES, err))
+    # mass conserved per instance by both forms
+    assert np.abs(p32[:, 0] - p64[:, 0]).max() <= 1e-12
+
+
+def test_batch_rejects_bad_instances(gpulib, pkg):
+    ph = pkg.physics
+    grids = [ph.VelocityGrid.uniform(8, -4.0, 4.0)]
+    with pytest.raises(pkg.DVMError):
+        pkg.DVMBatch(_cfg(pkg, pkg.DVM_PREC_FP64), grids, [0, 1], [1000])
+    b = pkg.DVMBatch(_cfg(pkg, pkg.DVM_PREC_FP64), grids, [0, 0], [1000])
+    f = np.zeros(grids[0].nv)
+    ptr = f.ctypes.data_as(pkg._abi.C.POINTER(pkg._abi.C.c_double))
+    assert b.lib.dvm_batch_upload_f(b.b, 2, ptr) == pkg.DVM_ERR_PARAM
+    assert b.lib.dvm_batch_step(b.b, -1) == pkg.DVM_ERR_PARAM

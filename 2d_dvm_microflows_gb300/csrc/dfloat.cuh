@@ -1,0 +1,150 @@
+// dfloat.cuh -- FP64-accurate arithmetic on the FP32 pipe.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, so the streaming kernels keep their values in
+// FP64 memory but do their arithmetic on unevaluated sums of two floats (hi + lo), with the
+// error-free transformations of Knuth (TwoSum), Dekker (Fast2Sum) and the FMA product
+// error (TwoProd). A double enters by an integer split of its bit pattern (no FP64
+// instruction) into hi = its leading 24 significant bits and lo = the next 24 bits, rounded
+// (relative error at most 2^-47, about 7e-15); values below 2^-126 enter as zero (their
+// absolute size, under 1.2e-38, is far below the FP64 rounding of any cell total). A result
+// leaves as hi + lo converted bit-exactly to doubles and added with one FP64 add.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dvm {
+
+struct dfl {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfl dfl_make(float h, float l) {
+  dfl r;
+  r.hi = h;
+  r.lo = l;
+  return r;
+}
+
+// Split of a double into hi + lo by integer operations on its bits.
+__device__ __forceinline__ dfl dfl_from_double(double x) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const uint32_t bh = static_cast<uint32_t>(b >> 32), bl = static_cast<uint32_t>(b);
+  const uint32_t sign = bh & 0x80000000u;
+  const int e = static_cast<int>((bh >> 20) & 0x7ffu);  // biased FP64 exponent
+  const int ef = e - 896;                                // biased FP32 exponent of hi
+  // mantissa bits 51..29 -> hi, bits 28..5 -> lo (23 bits plus the rounding bit 5)
+  const uint32_t mhi = ((bh & 0xfffffu) << 3) | (bl >> 29);
+  const uint32_t mlo = ((bl >> 6) & 0x7fffffu) + ((bl >> 5) & 1u);
+  dfl r;
+  if (ef <= 0) {             // |x| < 2^-126 (zero, FP64 subnormals, tiny values)
+    r.hi = 0.f;
+    r.lo = 0.f;
+    return r;
+  }
+  if (ef >= 255) {           // |x| >= 2^128 or inf / NaN: carry to FP32 inf / NaN
+    r.hi = static_cast<float>(x);
+    r.lo = 0.f;
+    return r;
+  }
+  r.hi = __int_as_float(static_cast<int>(sign | (static_cast<uint32_t>(ef) << 23) | mhi));
+  const int el = ef - 23;    // exponent of the lo magic number
+  if (el <= 0) {
+    r.lo = 0.f;
+  } else {
+    // (1 + mlo 2^-23) 2^(E-23) - 2^(E-23) = mlo 2^(E-46), exact; a carry of the rounding
+    // into the exponent field gives 2^(E-22) - 2^(E-23) = 2^23 2^(E-46), also exact
+    const float magic = __int_as_float(static_cast<int>((static_cast<uint32_t>(el) << 23) + mlo));
+    const float base = __int_as_float(static_cast<int>(static_cast<uint32_t>(el) << 23));
+    const float l = __fsub_rn(magic, base);
+    r.lo = sign ? -l : l;
+  }
+  return r;
+}
+
+// Exact float -> double by integer operations; the rare FP32 subnormals (the lo part of
+// values below about 2^-102) take the hardware conversion.
+__device__ __forceinline__ double dbl_from_float(float v) {
+  const uint32_t u = static_cast<uint32_t>(__float_as_int(v));
+  const uint32_t ex = (u >> 23) & 0xffu;
+  if (ex == 0u) return (u & 0x7fffffu) ? static_cast<double>(v) : 0.0;
+  const uint32_t hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  const uint32_t lo = u << 29;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
+__device__ __forceinline__ double dfl_to_double(dfl a) {
+  return dbl_from_float(a.hi) + dbl_from_float(a.lo);
+}
+
+// Knuth's TwoSum: s + e = a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Dekker's Fast2Sum (|a| >= |b| or a == 0): s + e = a + b exactly.
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ dfl dfl_norm(float h, float l) {
+  dfl r;
+  fast_two_sum(h, l, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ dfl dfl_add(dfl a, dfl b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return dfl_norm(s, e);
+}
+
+__device__ __forceinline__ dfl dfl_neg(dfl a) { return dfl_make(-a.hi, -a.lo); }
+
+__device__ __forceinline__ dfl dfl_sub(dfl a, dfl b) { return dfl_add(a, dfl_neg(b)); }
+
+// Product with the FMA error term (the lo*lo term, below 2^-48 relative, is dropped).
+__device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return dfl_norm(p, e);
+}
+
+// A running sum, renormalised after every term so that lo stays within half an ulp of hi
+// and each term adds at most about 2^-48 of the sum in rounding.
+struct dacc {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void dacc_zero(dacc& s) {
+  s.hi = 0.f;
+  s.lo = 0.f;
+}
+
+__device__ __forceinline__ void dacc_add(dacc& s, dfl x) {
+  float t, e;
+  two_sum(s.hi, x.hi, t, e);
+  fast_two_sum(t, __fadd_rn(e, __fadd_rn(s.lo, x.lo)), s.hi, s.lo);
+}
+
+// s += x * c (c a constant pair).
+__device__ __forceinline__ void dacc_fma(dacc& s, dfl x, dfl c) {
+  const float p = __fmul_rn(x.hi, c.hi);
+  float e = __fmaf_rn(x.hi, c.hi, -p);
+  e = __fmaf_rn(x.hi, c.lo, e);
+  e = __fmaf_rn(x.lo, c.hi, e);
+  float t, e2;
+  two_sum(s.hi, p, t, e2);
+  fast_two_sum(t, __fadd_rn(e2, __fadd_rn(s.lo, e)), s.hi, s.lo);
+}
+
+__device__ __forceinline__ double dacc_to_double(const dacc& s) {
+  return dbl_from_float(s.hi) + dbl_from_float(s.lo);
+}
+
+}  // namespace dvm

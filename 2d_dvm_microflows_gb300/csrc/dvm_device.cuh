@@ -55,9 +55,13 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+// m 2^-53 from the top 53 bits of (hi, lo), built from the bits (exact; no FP64 op).
 __device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
   const uint64_t m = ((static_cast<uint64_t>(hi) << 32) | lo) >> 11;
-  return static_cast<double>(m) * 0x1.0p-53;
+  if (m == 0) return 0.0;
+  const int p = 63 - __clzll(static_cast<long long>(m));  // top bit, 0..52
+  const uint64_t mant = (m << (52 - p)) & ((1ull << 52) - 1);
+  return __longlong_as_double(static_cast<long long>((static_cast<uint64_t>(p + 970) << 52) | mant));
 }
 
 __device__ __forceinline__ void philox_uniform2(uint64_t seed, uint32_t sample, uint32_t cell,

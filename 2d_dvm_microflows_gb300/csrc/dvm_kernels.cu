@@ -15,6 +15,7 @@
 // of the cell-step, so delta_phi = phi + sum(contributions) needs no copy of phi.
 #include <cuda_runtime.h>
 
+#include "dfloat.cuh"
 #include "dvm_internal.h"
 
 namespace dvm {
@@ -301,18 +302,14 @@ cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
 // k_collide: persistent; a chunk is kCollideChunk consecutive samples of one
 // (cell, sub-integral). One thread per sample.
 //
-// GB300 runs FP64 at 1/64 of its FP32 rate and this kernel is bound by that pipe, so it
-// keeps the reference's arithmetic where it decides a result and moves the rest off the
-// FP64 pipe: order-preserving integer keys for every search compare, tables of node
-// differences / reciprocals / remap denominator terms, a table of g and g^(2-2 omega)
-// on cubic uniform grids, and the exact 1/2 mass ratios of like-species pairs. Each of
-// these changes a value by at most a few ulps; the parity bar (1e-12 of max|f| against
-// the restatement) checks the sum.
-__device__ __forceinline__ void scatter(double* f, const Stencil& s, double w) {
-#pragma unroll
-  for (int q = 0; q < 7; ++q)
-    if (s.node[q] >= 0) atomicAdd(f + s.node[q], w * s.mass[q]);
-}
+// GB300 runs FP64 at 1/64 of its FP32 rate, so this kernel keeps FP64 only where the
+// reference's FP64 rounding decides a discrete outcome (the partner search) and moves
+// the rest off the FP64 pipe: order-preserving integer keys for every search compare,
+// tables of node differences / reciprocals / remap denominator terms, a table of g and
+// g^(2-2 omega) on cubic uniform grids, the exact 1/2 mass ratios of like-species pairs,
+// and hi + lo float pairs for the post-collision velocities, the remap weights and the
+// contributions. Each of these changes a value by at most about 2^-46 relative; the
+// parity bar (1e-12 of max|f| against the restatement) checks the sum.
 
 // Integer key with the order of the doubles (-0.0 folded onto +0.0).
 __device__ __forceinline__ long long okey(double d) {
@@ -350,29 +347,77 @@ __device__ __forceinline__ int referenced_search_keys(const double* __restrict__
   return lo;
 }
 
-struct SmemAxes {
-  const double* v[3];
-  const long long* mid[3];   // keys of the midpoints between consecutive nodes
-  const AxisEntry* tab[3];
+// ---- the FP64 collide arithmetic on the FP32 pipe ---------------------------------------
+// Post-collision velocities, remap weights and contributions are formed in hi + lo float
+// pairs (dfloat.cuh, about 47 significant bits); the few steps whose outcome the reference's
+// FP64 rounding decides stay in FP64: the bucket choice ceil(1000 R) and the search target
+// R * cum(n) of each partner pick. The contributions go to the FP64 atomics as doubles.
+__device__ __forceinline__ int okeyf(float d);
+
+struct AxisEntryD {
+  dfl D[kTabW];
+  dfl invD[kTabW];
+  dfl T[kTabW];
+};
+
+struct SmemAxesD {
+  const double* vd[3];      // FP64 nodes (the rare boundary-stencil path)
+  const dfl* v[3];          // nodes as pairs
+  const long long* mid[3];  // pair keys of the midpoints between consecutive nodes
+  const AxisEntryD* tab[3];
   int n[3];
 };
 
-// One axis of compute_remapping_quantities: nearest node (:146-183). The reference's
-// binary_search_with_first_guess returns the node nearest to u, the lower one on a tie,
-// and the first or last node outside the grid; here the guess nint(factor*(u - v_min)) is
-// walked to that node with integer compares against the keys of the midpoints between
-// nodes (mid[i] = (v[i] + v[i+1])/2). The choice can differ from the reference's only for
-// u within an ulp of a midpoint.
-__device__ __forceinline__ int nearest(const SmemAxes& A, int ax, double u, double vmin,
-                                       double factor, int& corner, int& bad) {
+struct StencilD {
+  int node[7];
+  dfl mass[7];
+};
+
+// Order-preserving key of a normalised pair (|lo| at most half an ulp of hi).
+__device__ __forceinline__ long long dkey(dfl a) {
+  const uint32_t h = static_cast<uint32_t>(okeyf(a.hi));
+  const uint32_t l = static_cast<uint32_t>(okeyf(a.lo)) ^ 0x80000000u;
+  return static_cast<long long>((static_cast<uint64_t>(h) << 32) | l);
+}
+
+__device__ __forceinline__ int dfl_isgn(dfl a) {
+  return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? -1 : 1;
+}
+
+__device__ __forceinline__ dfl dfl_scale(dfl a, float s) {  // s a power of two
+  return dfl_make(a.hi * s, a.lo * s);
+}
+
+// Division with one correction step (Karp-Markstein style): q1 = a/b in FP32, the
+// remainder a - q1 b formed exactly by FMA, divided again.
+__device__ __forceinline__ dfl dfl_div(dfl a, dfl b) {
+  const float rb = __frcp_rn(b.hi);
+  const float q1 = __fmul_rn(a.hi, rb);
+  const float p = __fmul_rn(q1, b.hi);
+  const float e = __fmaf_rn(q1, b.hi, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), __fmaf_rn(q1, b.lo, e)), a.lo);
+  const float q2 = __fmul_rn(r, rb);
+  return dfl_norm(q1, q2);
+}
+
+__device__ __forceinline__ dfl dfl_sqrt(dfl a) {
+  if (!(a.hi > 0.f)) return dfl_make(0.f, 0.f);
+  const float s = __fsqrt_rn(a.hi);
+  const float p = __fmul_rn(s, s);
+  const float e = __fmaf_rn(s, s, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
+  return dfl_norm(s, __fmul_rn(r, __fdiv_rn(0.5f, s)));
+}
+
+// Nearest node, as nearest() but on pair keys.
+__device__ __forceinline__ int nearest_d(const SmemAxesD& A, int ax, dfl u, float vmin,
+                                         float factor, int& corner, int& bad) {
   const int mx = A.n[ax] - 1;
   const long long* mid = A.mid[ax];
-  const long long vk = okey(u);
-  // the guess only starts the walk, so FP32 is enough for it
-  int o = __float2int_rn(static_cast<float>(factor) *
-                         (static_cast<float>(u) - static_cast<float>(vmin)));
+  const long long vk = dkey(u);
+  int o = __float2int_rn(factor * (u.hi - vmin));
   o = o < 0 ? 0 : (o > mx ? mx : o);
-  if (u != u) bad |= 1;  // NaN velocity: the reference's search would not return
+  if (u.hi != u.hi) bad |= 1;
   int it = 0;
   while (o > 0 && vk <= mid[o - 1] && it++ < kMaxAxis) --o;
   while (o < mx && vk > mid[o] && it++ < kMaxAxis) ++o;
@@ -381,93 +426,86 @@ __device__ __forceinline__ int nearest(const SmemAxes& A, int ax, double u, doub
   return o;
 }
 
-// Reciprocal from an FP32 seed and two Newton steps (within an ulp or two of 1/d).
-__device__ __forceinline__ double fast_rcp(double d) {
-  const double ad = fabs(d);
-  if (!(ad > 1e-30 && ad < 1e30)) return 1.0 / d;
-  double r = static_cast<double>(__frcp_rn(static_cast<float>(d)));
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
+// Per-axis terms of the remap: interior difference, its reciprocal, exterior difference
+// and denominator term.
+__device__ __forceinline__ void axis_terms(const SmemAxesD& A, int ax, int o, int s, int avail,
+                                           dfl& int_d, dfl& inv_d, dfl& ext_d, dfl& t_d) {
+  const dfl zero = dfl_make(0.f, 0.f);
+  ext_d = zero;
+  t_d = zero;
+  if (s >= -kTabS && s <= kTabS) {
+    const AxisEntryD& e = A.tab[ax][o];
+    int_d = e.D[kTabS + s];
+    inv_d = e.invD[kTabS + s];
+    if (avail) { ext_d = e.D[kTabS - s]; t_d = e.T[kTabS + s]; }
+  } else {
+    const dfl* v = A.v[ax];
+    int_d = dfl_sub(v[o + s], v[o]);
+    inv_d = dfl_div(dfl_make(1.f, 0.f), int_d);
+    if (avail) {
+      ext_d = dfl_sub(v[o - s], v[o]);
+      t_d = dfl_mul(ext_d, dfl_sub(ext_d, int_d));
+    }
+  }
 }
 
-// compute_remapping_quantities (collisions/remapping.f90:92-394) with tabulated
-// differences, reciprocals and denominator terms.
-__device__ __forceinline__ int remap_fast(const GridInfo& g, const SmemAxes& A, double u,
-                                          double v, double w, double f_off, Stencil& s) {
+// compute_remapping_quantities (collisions/remapping.f90:92-394), f_off = 1, in pairs.
+__device__ __forceinline__ int remap_dfl(const GridInfo& g, const SmemAxesD& A, dfl u, dfl v,
+                                         dfl w, float xmin, float ymin, float zmin, float xfac,
+                                         float yfac, float zfac, StencilD& s) {
   int corner = 0, bad = 0;
-  int o_i = nearest(A, 0, u, g.xv_min, g.xv_factor, corner, bad);
-  int o_j = nearest(A, 1, v, g.yv_min, g.yv_factor, corner, bad);
-  int o_k = nearest(A, 2, w, g.zv_min, g.zv_factor, corner, bad);
+  int o_i = nearest_d(A, 0, u, xmin, xfac, corner, bad);
+  int o_j = nearest_d(A, 1, v, ymin, yfac, corner, bad);
+  int o_k = nearest_d(A, 2, w, zmin, zfac, corner, bad);
   const int i_max = g.nx - 1, j_max = g.ny - 1, k_max = g.nz - 1;
   if (corner == 3) {
     o_i -= isign1(o_i - 1);
     o_j -= isign1(o_j - 1);
     o_k -= isign1(o_k - 1);
   }
-  const double* x = A.v[0];
-  const double* y = A.v[1];
-  const double* z = A.v[2];
-  const double ox = x[o_i], oy = y[o_j], oz = z[o_k];
-  const double a = u - ox, b = v - oy, c = w - oz;
-  int sa = isgn(a), sb = isgn(b), sc = isgn(c);
+  const dfl a = dfl_sub(u, A.v[0][o_i]), b = dfl_sub(v, A.v[1][o_j]), c = dfl_sub(w, A.v[2][o_k]);
+  int sa = dfl_isgn(a), sb = dfl_isgn(b), sc = dfl_isgn(c);
   if (o_i + sa > i_max || o_i + sa < 0) {
     sa = -1 * sa;
-    find_boundary_stencil(sa, sb, sc, a, o_i, o_j, o_k, x, y, z, 0, i_max, 0, j_max, 0, k_max);
+    find_boundary_stencil(sa, sb, sc, dfl_to_double(a), o_i, o_j, o_k, A.vd[0], A.vd[1], A.vd[2],
+                          0, i_max, 0, j_max, 0, k_max);
   }
   if (o_j + sb > j_max || o_j + sb < 0) {
     sb = -1 * sb;
-    find_boundary_stencil(sb, sa, sc, b, o_j, o_i, o_k, y, x, z, 0, j_max, 0, i_max, 0, k_max);
+    find_boundary_stencil(sb, sa, sc, dfl_to_double(b), o_j, o_i, o_k, A.vd[1], A.vd[0], A.vd[2],
+                          0, j_max, 0, i_max, 0, k_max);
   }
   if (o_k + sc > k_max || o_k + sc < 0) {
     sc = -1 * sc;
-    find_boundary_stencil(sc, sb, sa, c, o_k, o_j, o_i, z, y, x, 0, k_max, 0, j_max, 0, i_max);
+    find_boundary_stencil(sc, sb, sa, dfl_to_double(c), o_k, o_j, o_i, A.vd[2], A.vd[1], A.vd[0],
+                          0, k_max, 0, j_max, 0, i_max);
   }
   const int fx = (o_i - sa <= i_max && o_i - sa >= 0);
   const int fy = (o_j - sb <= j_max && o_j - sb >= 0);
   const int fz = (o_k - sc <= k_max && o_k - sc >= 0);
-  // per-axis differences, reciprocal of the interior difference, denominator term
-  double int_x, inv_x, ext_x = 0.0, t_x = 0.0;
-  if (sa >= -kTabS && sa <= kTabS) {
-    const AxisEntry& e = A.tab[0][o_i];
-    int_x = e.D[kTabS + sa]; inv_x = e.invD[kTabS + sa];
-    if (fx) { ext_x = e.D[kTabS - sa]; t_x = e.T[kTabS + sa]; }
+  dfl int_x, inv_x, ext_x, t_x, int_y, inv_y, ext_y, t_y, int_z, inv_z, ext_z, t_z;
+  axis_terms(A, 0, o_i, sa, fx, int_x, inv_x, ext_x, t_x);
+  axis_terms(A, 1, o_j, sb, fy, int_y, inv_y, ext_y, t_y);
+  axis_terms(A, 2, o_k, sc, fz, int_z, inv_z, ext_z, t_z);
+  const dfl zero = dfl_make(0.f, 0.f);
+  dfl f_e = zero;
+  if (!(fx | fy | fz)) {
+    bad |= 2;
   } else {
-    int_x = x[o_i + sa] - ox; inv_x = 1.0 / int_x;
-    if (fx) { ext_x = x[o_i - sa] - ox; t_x = ext_x * (ext_x - int_x); }
+    // (a^2 + b^2 + c^2 - a int_x - b int_y - c int_z) / den, den = the available T terms
+    const dfl num = dfl_add(dfl_add(dfl_mul(a, dfl_sub(a, int_x)), dfl_mul(b, dfl_sub(b, int_y))),
+                            dfl_mul(c, dfl_sub(c, int_z)));
+    dfl den = fx ? t_x : zero;
+    if (fy) den = dfl_add(den, t_y);
+    if (fz) den = dfl_add(den, t_z);
+    f_e = dfl_div(num, den);
   }
-  double int_y, inv_y, ext_y = 0.0, t_y = 0.0;
-  if (sb >= -kTabS && sb <= kTabS) {
-    const AxisEntry& e = A.tab[1][o_j];
-    int_y = e.D[kTabS + sb]; inv_y = e.invD[kTabS + sb];
-    if (fy) { ext_y = e.D[kTabS - sb]; t_y = e.T[kTabS + sb]; }
-  } else {
-    int_y = y[o_j + sb] - oy; inv_y = 1.0 / int_y;
-    if (fy) { ext_y = y[o_j - sb] - oy; t_y = ext_y * (ext_y - int_y); }
-  }
-  double int_z, inv_z, ext_z = 0.0, t_z = 0.0;
-  if (sc >= -kTabS && sc <= kTabS) {
-    const AxisEntry& e = A.tab[2][o_k];
-    int_z = e.D[kTabS + sc]; inv_z = e.invD[kTabS + sc];
-    if (fz) { ext_z = e.D[kTabS - sc]; t_z = e.T[kTabS + sc]; }
-  } else {
-    int_z = z[o_k + sc] - oz; inv_z = 1.0 / int_z;
-    if (fz) { ext_z = z[o_k - sc] - oz; t_z = ext_z * (ext_z - int_z); }
-  }
-  const int flag = fx + 2 * fy + 4 * fz;
-  double den = 0.0;
-  if (fx) den = t_x;
-  if (fy) den = den + t_y;
-  if (fz) den = den + t_z;
-  double f_e = 0.0;
-  if (flag == 0) bad |= 2;
-  else f_e = f_off * (a * a + b * b + c * c - a * int_x - b * int_y - c * int_z) * fast_rcp(den);
-  const double f_ex = fx ? f_e : 0.0, f_ey = fy ? f_e : 0.0, f_ez = fz ? f_e : 0.0;
-  const double f_ix = (f_off * a - f_ex * ext_x) * inv_x;
-  const double f_iy = (f_off * b - f_ey * ext_y) * inv_y;
-  const double f_iz = (f_off * c - f_ez * ext_z) * inv_z;
-  const double f_o = f_off - f_ix - f_iy - f_iz - f_ex - f_ey - f_ez;
+  const dfl f_ex = fx ? f_e : zero, f_ey = fy ? f_e : zero, f_ez = fz ? f_e : zero;
+  const dfl f_ix = dfl_mul(dfl_sub(a, dfl_mul(f_ex, ext_x)), inv_x);
+  const dfl f_iy = dfl_mul(dfl_sub(b, dfl_mul(f_ey, ext_y)), inv_y);
+  const dfl f_iz = dfl_mul(dfl_sub(c, dfl_mul(f_ez, ext_z)), inv_z);
+  const dfl sum = dfl_add(dfl_add(dfl_add(f_ix, f_iy), dfl_add(f_iz, f_ex)), dfl_add(f_ey, f_ez));
+  const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
   const int NX = g.nx, NXY = g.nx * g.ny;
   const int base = o_i + NX * o_j + NXY * o_k;
   s.node[0] = base;
@@ -482,20 +520,43 @@ __device__ __forceinline__ int remap_fast(const GridInfo& g, const SmemAxes& A, 
   return bad;
 }
 
+__device__ __forceinline__ void scatter_d(double* f, const StencilD& s, dfl w) {
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    if (s.node[q] >= 0) atomicAdd(f + s.node[q], dfl_to_double(dfl_mul(w, s.mass[q])));
+}
+
+// t = R - k/kTrigN (k = the top 10 bits of R) as a pair, and k, from the bits of R in [0, 1).
+__device__ __forceinline__ dfl angle_fraction(double R, int& k) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(R));
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  unsigned long long m = 0;  // R 2^53, truncated
+  if (e > 0 && e <= 1022 && 1022 - e < 64)
+    m = ((b & ((1ull << 52) - 1)) | (1ull << 52)) >> (1022 - e);
+  k = static_cast<int>(m >> 43);
+  const unsigned long long t = m & ((1ull << 43) - 1);
+  const uint32_t th = static_cast<uint32_t>(t >> 20), tl = static_cast<uint32_t>(t & 0xfffffu);
+  // exact floats of the 23- and 20-bit integers: (2^23 + n) - 2^23
+  const float fh = __fsub_rn(__int_as_float(static_cast<int>(0x4B000000u | th)), 8388608.f);
+  const float fl = __fsub_rn(__int_as_float(static_cast<int>(0x4B000000u | tl)), 8388608.f);
+  return dfl_norm(fh * 0x1.0p-33f, fl * 0x1.0p-53f);
+}
+
 struct CollideSmem {
-  size_t axes, keys, tabs, gtab, trig, total;
+  size_t axes, axes_d, keys, tabs, gtab, trig, total;
 };
 
 __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, const CollTables& t) {
   CollideSmem L;
   const size_t nsum = static_cast<size_t>(g.nx + g.ny + g.nz);
   L.axes = 0;
-  L.keys = L.axes + nsum * sizeof(double);
+  L.axes_d = L.axes + nsum * sizeof(double);
+  L.keys = L.axes_d + nsum * sizeof(dfl);
   L.tabs = L.keys + nsum * sizeof(long long);
-  L.gtab = L.tabs + 3 * static_cast<size_t>(t.nmax) * sizeof(AxisEntry);
+  L.gtab = L.tabs + 3 * static_cast<size_t>(t.nmax) * sizeof(AxisEntryD);
   L.gtab = (L.gtab + 15) & ~static_cast<size_t>(15);  // double2 needs 16-byte alignment
   L.trig = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
-  L.total = L.trig + static_cast<size_t>(kTrigN) * sizeof(double2);
+  L.total = L.trig + static_cast<size_t>(kTrigN) * sizeof(float4);
   return L;
 }
 
@@ -504,34 +565,61 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   const GridInfo& g = a.g;
   const CollideSmem L = collide_smem_layout(g, a.t);
   double* sv = reinterpret_cast<double*>(s_raw + L.axes);
+  dfl* svd = reinterpret_cast<dfl*>(s_raw + L.axes_d);
   long long* sk = reinterpret_cast<long long*>(s_raw + L.keys);
-  AxisEntry* st = reinterpret_cast<AxisEntry*>(s_raw + L.tabs);
+  AxisEntryD* st = reinterpret_cast<AxisEntryD*>(s_raw + L.tabs);
   double2* sg = reinterpret_cast<double2*>(s_raw + L.gtab);
+  float4* strig = reinterpret_cast<float4*>(s_raw + L.trig);
   const int nsum = g.nx + g.ny + g.nz;
   for (int t = threadIdx.x; t < nsum; t += blockDim.x) {
     const double* ax = t < g.nx ? g.x : (t < g.nx + g.ny ? g.y : g.z);
     const int n = t < g.nx ? g.nx : (t < g.nx + g.ny ? g.ny : g.nz);
     const int i = t < g.nx ? t : (t < g.nx + g.ny ? t - g.nx : t - g.nx - g.ny);
     sv[t] = ax[i];
-    sk[t] = (i + 1 < n) ? okey(0.5 * (ax[i] + ax[i + 1])) : 0x7FFFFFFFFFFFFFFFLL;
+    const dfl xv = dfl_from_double(ax[i]);
+    svd[t] = dfl_norm(xv.hi, xv.lo);
+    if (i + 1 < n) {
+      const dfl m = dfl_from_double(0.5 * (ax[i] + ax[i + 1]));
+      sk[t] = dkey(dfl_norm(m.hi, m.lo));
+    } else {
+      sk[t] = 0x7FFFFFFFFFFFFFFFLL;
+    }
   }
   {
     const double* src = reinterpret_cast<const double*>(a.t.axis);
-    double* dst = reinterpret_cast<double*>(st);
+    dfl* dst = reinterpret_cast<dfl*>(st);
     const int n = 3 * a.t.nmax * static_cast<int>(sizeof(AxisEntry) / sizeof(double));
-    for (int t = threadIdx.x; t < n; t += blockDim.x) dst[t] = src[t];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      const dfl v = dfl_from_double(src[t]);
+      dst[t] = dfl_norm(v.hi, v.lo);
+    }
   }
   if (a.t.gtab_smem)
     for (int t = threadIdx.x; t < a.t.gtab_n; t += blockDim.x) sg[t] = a.t.gtab[t];
-  double2* strig = reinterpret_cast<double2*>(s_raw + L.trig);
-  for (int t = threadIdx.x; t < kTrigN; t += blockDim.x) strig[t] = a.t.trig[t];
+  for (int t = threadIdx.x; t < kTrigN; t += blockDim.x) {
+    const double2 cs = a.t.trig[t];
+    const dfl c = dfl_from_double(cs.x), sn = dfl_from_double(cs.y);
+    const dfl cn = dfl_norm(c.hi, c.lo), snn = dfl_norm(sn.hi, sn.lo);
+    strig[t] = make_float4(cn.hi, cn.lo, snn.hi, snn.lo);
+  }
   __syncthreads();
-  SmemAxes A;
-  A.v[0] = sv; A.v[1] = sv + g.nx; A.v[2] = sv + g.nx + g.ny;
+  SmemAxesD A;
+  A.vd[0] = sv; A.vd[1] = sv + g.nx; A.vd[2] = sv + g.nx + g.ny;
+  A.v[0] = svd; A.v[1] = svd + g.nx; A.v[2] = svd + g.nx + g.ny;
   A.mid[0] = sk; A.mid[1] = sk + g.nx; A.mid[2] = sk + g.nx + g.ny;
   A.tab[0] = st; A.tab[1] = st + a.t.nmax; A.tab[2] = st + 2 * a.t.nmax;
   A.n[0] = g.nx; A.n[1] = g.ny; A.n[2] = g.nz;
   const double2* gtab = a.t.gtab_smem ? sg : a.t.gtab;
+  const float xmin = static_cast<float>(g.xv_min), ymin = static_cast<float>(g.yv_min);
+  const float zmin = static_cast<float>(g.zv_min);
+  const float xfac = static_cast<float>(g.xv_factor), yfac = static_cast<float>(g.yv_factor);
+  const float zfac = static_cast<float>(g.zv_factor);
+  dfl two_pi;
+  {
+    const dfl t = dfl_from_double(a.t.two_pi);
+    two_pi = dfl_norm(t.hi, t.lo);
+  }
+  const dfl one_sixth = dfl_make(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 to 2^-50
 
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const int nent = 3 * a.ncells;
@@ -542,8 +630,6 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
   const double alpha = 0.5 * (a.cp.alpha + a.cp.alpha);
   const double ralpha = 1.0 / alpha;
   const bool vss = fabs(ralpha - 1.0) > kDoubleTol;
-  // like-species pair: mass fractions m/(m+m) are exactly 1/2
-  constexpr double mf = 0.5;
   const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
 
@@ -581,8 +667,6 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
     }
     const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
     const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
-    const double xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
-    const double xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
     // compute_relative_velocity (collision_utilities.f90:188-218) and g^(2-2 omega)
     double gg, g_sigma;
     if (gtab) {
@@ -593,27 +677,37 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
       gg = e.x;
       g_sigma = e.y;
     } else {
-      const double gx = xB - xA, gy = yB - yA, gz = zB - zA;
+      const double gx = A.vd[0][iB] - A.vd[0][iA], gy = A.vd[1][jB] - A.vd[1][jA];
+      const double gz = A.vd[2][kB] - A.vd[2][kA];
       gg = sqrt(gx * gx + gy * gy + gz * gz);
       if (gg < kDoubleTol) continue;
       g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
     }
     // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old
     const double* kc = a.kin + cs;
-    const double sA = (vr && q == 0) ? 1.0 : dsgn(__ldg(kc + lA + 1));
-    const double sB = (vr && q == 1) ? 1.0 : dsgn(__ldg(kc + lB + 1));
-    // vr_depletion_routine elastic part (variance_reduction.f90:1157-1166)
-    const double kin1 = sA * (sB * factor * g_sigma);
-    const double kin2 = sB * (sA * factor * g_sigma);
-    atomicAdd(f + lA, -kin1);
-    atomicAdd(f + lB, -kin2);
+    const bool negA = (vr && q == 0) ? false : signbit(__ldg(kc + lA + 1));
+    const bool negB = (vr && q == 1) ? false : signbit(__ldg(kc + lB + 1));
+    // vr_depletion_routine elastic part (variance_reduction.f90:1157-1166): kin_depl(1) =
+    // kin_depl(2) = sA sB factor g^(2-2 omega)
+    const double fg = factor * g_sigma;
+    const double kin = (negA != negB) ? -fg : fg;
+    atomicAdd(f + lA, -kin);
+    atomicAdd(f + lB, -kin);
     // replenish_collision elastic branch (replenishing_collisions.f90:206-249)
-    const double kr1 = (NR == 1) ? kin1 : kin1 / static_cast<double>(NR);
-    const double kr2 = (NR == 1) ? kin2 : kin2 / static_cast<double>(NR);
-    const double vc0 = mf * xA + mf * xB, vc1 = mf * yA + mf * yB, vc2 = mf * zA + mf * zB;
-    // g_part(1)/g = g_part(2)/g = 1/2 for equal masses (pick_random_velocity_on_sphere
-    // :343-351); the VSS branch also needs the summed |xi - v_com| components.
-    const double hg = 0.5 * gg;
+    dfl kr;
+    {
+      const dfl t = dfl_from_double((NR == 1) ? kin : kin / static_cast<double>(NR));
+      kr = dfl_norm(t.hi, t.lo);
+    }
+    // v_com of a like-species pair: (xi_A + xi_B) / 2
+    const dfl vc0 = dfl_scale(dfl_add(A.v[0][iA], A.v[0][iB]), 0.5f);
+    const dfl vc1 = dfl_scale(dfl_add(A.v[1][jA], A.v[1][jB]), 0.5f);
+    const dfl vc2 = dfl_scale(dfl_add(A.v[2][kA], A.v[2][kB]), 0.5f);
+    dfl hg;  // g_part(1) = g_part(2) = g/2 (pick_random_velocity_on_sphere :343-351)
+    {
+      const dfl t = dfl_from_double(gg);
+      hg = dfl_scale(dfl_norm(t.hi, t.lo), 0.5f);
+    }
     for (int r = 0; r < NR; ++r) {
       double rphi, rcos;
       if (rec) {
@@ -622,54 +716,70 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
       } else {
         philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 1u + r, rphi, rcos);
       }
-      // pick_random_velocity_on_sphere (collision_utilities.f90:284-352); phi = 2 pi R:
-      // R = k/kTrigN + t exactly, cos/sin of 2 pi k/kTrigN from the table, of
-      // th = 2 pi t (< 0.0062) by Taylor series (next terms below 1e-17), then the
-      // angle-addition formulas.
-      double sphi, cphi;
-      {
-        const double rk = floor(rphi * static_cast<double>(kTrigN));
-        const int k = min(max(static_cast<int>(rk), 0), kTrigN - 1);
-        const double th = a.t.two_pi * (rphi - rk * (1.0 / kTrigN));
-        const double t2 = th * th;
-        const double st = th * (1.0 - t2 * (1.0 / 6.0) * (1.0 - t2 * (1.0 / 20.0)));
-        const double ct = 1.0 - t2 * 0.5 * (1.0 - t2 * (1.0 / 12.0) * (1.0 - t2 * (1.0 / 30.0)));
-        const double2 cs = strig[k];
-        cphi = cs.x * ct - cs.y * st;
-        sphi = cs.y * ct + cs.x * st;
-      }
-      double ux, uy, uz;  // r / g: unit direction of the post-collision relative velocity
+      dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
       if (vss) {
-        const double ur = fabs(xA - vc0) + fabs(xB - vc0);
-        const double vr_ = fabs(yA - vc1) + fabs(yB - vc1);
-        const double wr = fabs(zA - vc2) + fabs(zB - vc2);
+        // VSS branch (pick_random_velocity_on_sphere :314-328) in FP64
+        const double xA = A.vd[0][iA], yA = A.vd[1][jA], zA = A.vd[2][kA];
+        const double xB = A.vd[0][iB], yB = A.vd[1][jB], zB = A.vd[2][kB];
+        const double v0 = 0.5 * xA + 0.5 * xB, v1 = 0.5 * yA + 0.5 * yB, v2 = 0.5 * zA + 0.5 * zB;
+        const double sphi = sin(a.t.two_pi * rphi), cphi = cos(a.t.two_pi * rphi);
+        const double ur = fabs(xA - v0) + fabs(xB - v0);
+        const double vr_ = fabs(yA - v1) + fabs(yB - v1);
+        const double wr = fabs(zA - v2) + fabs(zB - v2);
         const double ct = 2.0 * pow(rcos, ralpha) - 1.0;
-        const double st = sqrt(1.0 - ct * ct);
+        const double stt = sqrt(1.0 - ct * ct);
         const double den = sqrt(vr_ * vr_ + wr * wr);
         double rx, ry, rz;
         if (den > kDoubleTol * gg) {
-          rx = ct * ur + st * sphi * den;
-          ry = ct * vr_ + st * (gg * wr * cphi - ur * vr_ * sphi) / den;
-          rz = ct * wr - st * (gg * vr_ * cphi + ur * wr * sphi) / den;
+          rx = ct * ur + stt * sphi * den;
+          ry = ct * vr_ + stt * (gg * wr * cphi - ur * vr_ * sphi) / den;
+          rz = ct * wr - stt * (gg * vr_ * cphi + ur * wr * sphi) / den;
         } else {
           rx = ct * ur;
-          ry = st * cphi * ur;
-          rz = st * sphi * ur;
+          ry = stt * cphi * ur;
+          rz = stt * sphi * ur;
         }
-        ux = 0.5 * rx; uy = 0.5 * ry; uz = 0.5 * rz;
+        const dfl tx = dfl_from_double(0.5 * rx), ty = dfl_from_double(0.5 * ry);
+        const dfl tz = dfl_from_double(0.5 * rz);
+        ux = dfl_norm(tx.hi, tx.lo); uy = dfl_norm(ty.hi, ty.lo); uz = dfl_norm(tz.hi, tz.lo);
       } else {
-        const double ct = 2.0 * rcos - 1.0;
-        const double st = sqrt(1.0 - ct * ct);
-        ux = hg * st * cphi;
-        uy = hg * st * sphi;
-        uz = hg * ct;
+        // phi = 2 pi R (pick_random_velocity_on_sphere :284-352): R = k/kTrigN + t, cos and
+        // sin of 2 pi k/kTrigN from the table, of th = 2 pi t (< 0.0062) by Taylor series
+        // (the dropped terms are below 1e-17), then the angle-addition formulas
+        int k;
+        const dfl th = dfl_mul(two_pi, angle_fraction(rphi, k));
+        const dfl t2 = dfl_mul(th, th);
+        const float t2h = t2.hi;
+        // sin th = th - th (t2/6 - t2^2/120), cos th = 1 - (t2/2 - t2^2/24 + t2^3/720)
+        const dfl cs1 = dfl_sub(dfl_mul(t2, one_sixth), dfl_make(t2h * t2h * (1.f / 120.f), 0.f));
+        const dfl sth = dfl_sub(th, dfl_mul(th, cs1));
+        const dfl cc1 = dfl_sub(dfl_scale(t2, 0.5f),
+                                dfl_make(t2h * t2h * (1.f / 24.f - t2h * (1.f / 720.f)), 0.f));
+        const dfl cth = dfl_sub(dfl_make(1.f, 0.f), cc1);
+        const float4 tb = strig[min(max(k, 0), kTrigN - 1)];
+        const dfl C = dfl_make(tb.x, tb.y), S = dfl_make(tb.z, tb.w);
+        const dfl cphi = dfl_sub(dfl_mul(C, cth), dfl_mul(S, sth));
+        const dfl sphi = dfl_add(dfl_mul(S, cth), dfl_mul(C, sth));
+        // cos theta = 2 R - 1 (exact in FP64), sin theta = sqrt(1 - cos^2)
+        dfl ct;
+        {
+          const dfl t = dfl_from_double(fma(2.0, rcos, -1.0));
+          ct = dfl_norm(t.hi, t.lo);
+        }
+        const dfl stt = dfl_sqrt(dfl_sub(dfl_make(1.f, 0.f), dfl_mul(ct, ct)));
+        const dfl hs = dfl_mul(hg, stt);
+        ux = dfl_mul(hs, cphi);
+        uy = dfl_mul(hs, sphi);
+        uz = dfl_mul(hg, ct);
       }
-      Stencil s;
-      int rb = remap_fast(g, A, vc0 + ux, vc1 + uy, vc2 + uz, 1.0, s);
-      if (rb & 2) bad |= DVM_EW_REMAP; else scatter(f, s, kr1);
+      StencilD sd;
+      int rb = remap_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz), xmin, ymin,
+                         zmin, xfac, yfac, zfac, sd);
+      if (rb & 2) bad |= DVM_EW_REMAP; else scatter_d(f, sd, kr);
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_fast(g, A, vc0 - ux, vc1 - uy, vc2 - uz, 1.0, s);
-      if (rb & 2) bad |= DVM_EW_REMAP; else scatter(f, s, kr2);
+      rb = remap_dfl(g, A, dfl_sub(vc0, ux), dfl_sub(vc1, uy), dfl_sub(vc2, uz), xmin, ymin, zmin,
+                     xfac, yfac, zfac, sd);
+      if (rb & 2) bad |= DVM_EW_REMAP; else scatter_d(f, sd, kr);
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
   }
@@ -1306,7 +1416,9 @@ __global__ void __launch_bounds__(256) k_wall_spec(WallArgs a) {
   const int rb = xwall ? remap(g, g.x, g.y, g.z, -g.x[i], g.y[j], g.z[k], 1.0, s)
                        : remap(g, g.x, g.y, g.z, g.x[i], -g.y[j], g.z[k], 1.0, s);
   if (rb & 2) { atomicOr(a.err, DVM_EW_REMAP); return; }
-  scatter(gh, s, dens);
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    if (s.node[q] >= 0) atomicAdd(gh + s.node[q], dens * s.mass[q]);
 }
 
 cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s) {
@@ -1534,15 +1646,17 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 // G_p = sum_k f z'^p (p = 0..3, z' = z - w0), then the raw moments up to third order
 // about the previous step's velocity (u0, v0, w0) follow from the columns with x' = x - u0,
 // y' = y - v0, and the central moments by shifting to the new velocity; being taken about
-// a velocity already close to u, the shift cancels nothing significant. Four FP64 ops per
-// node (five with the speed) instead of the reference's ~45.
+// a velocity already close to u, the shift cancels nothing significant. The sums run on
+// the FP32 pipe in hi + lo pairs (dfloat.cuh): each f and |xi| enters by an exact integer
+// split, each product and sum carries its rounding error, so a thread's partial sums keep
+// about 47 bits; only the per-thread totals go back to FP64 for the block reduction.
 constexpr int kMomThreads = 256;
-constexpr int kMomAcc = 20;
+constexpr int kMomAcc = 14;
 
 __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
   __shared__ double s_red[kMomAcc * 32];
-  __shared__ double s_ax[3 * kMaxAxis];
-  __shared__ double s_z[4 * kMaxAxis];
+  __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
+  __shared__ dfl s_z[3 * kMaxAxis];   // z', z'^2, z'^3
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
@@ -1551,52 +1665,67 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
   const double u0 = isfinite(P[DVM_P_U]) ? P[DVM_P_U] : 0.0;
   const double v0 = isfinite(P[DVM_P_V]) ? P[DVM_P_V] : 0.0;
   const double w0 = isfinite(P[DVM_P_W]) ? P[DVM_P_W] : 0.0;
-  for (int t = threadIdx.x; t < NX; t += blockDim.x) s_ax[t] = g.x[t] - u0;
-  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) s_ax[kMaxAxis + t] = g.y[t] - v0;
+  for (int t = threadIdx.x; t < NX; t += blockDim.x) {
+    const double xx = g.x[t] - u0;
+    s_ax[t] = dfl_from_double(xx);
+    s_ax[kMaxAxis + t] = dfl_from_double(xx * xx);
+  }
+  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) {
+    const double yy = g.y[t] - v0;
+    s_ax[2 * kMaxAxis + t] = dfl_from_double(yy);
+    s_ax[3 * kMaxAxis + t] = dfl_from_double(yy * yy);
+  }
   for (int t = threadIdx.x; t < NZ; t += blockDim.x) {
     const double zz = g.z[t] - w0;
-    s_z[t] = zz;
-    s_z[kMaxAxis + t] = zz * zz;
-    s_z[2 * kMaxAxis + t] = zz * zz * zz;
+    s_z[t] = dfl_from_double(zz);
+    s_z[kMaxAxis + t] = dfl_from_double(zz * zz);
+    s_z[2 * kMaxAxis + t] = dfl_from_double(zz * zz * zz);
   }
   __syncthreads();
   // accumulators: 0 n | 1-3 M_x M_y M_z | 4-9 M_xx M_yy M_zz M_xy M_xz M_yz |
   // 10-12 T3_x T3_y T3_z (sum f c'_i |c'|^2) | 13 speed
-  double acc[kMomAcc];
+  dacc sacc[kMomAcc];
 #pragma unroll
-  for (int q = 0; q < kMomAcc; ++q) acc[q] = 0.0;
+  for (int q = 0; q < kMomAcc; ++q) dacc_zero(sacc[q]);
   const double* speed = g.speed;
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
-    double G0 = 0.0, G1 = 0.0, G2 = 0.0, G3 = 0.0, S = 0.0;
+    dacc G0, G1, G2, G3, S;
+    dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
     for (int k = 0; k < NZ; ++k) {
       const int l = col + NXY * k;
-      const double fv = f[l];
-      G0 += fv;
-      G1 += fv * s_z[k];
-      G2 += fv * s_z[kMaxAxis + k];
-      G3 += fv * s_z[2 * kMaxAxis + k];
-      S += fv * speed[l];
+      const dfl fv = dfl_from_double(f[l]);
+      dacc_add(G0, fv);
+      dacc_fma(G1, fv, s_z[k]);
+      dacc_fma(G2, fv, s_z[kMaxAxis + k]);
+      dacc_fma(G3, fv, s_z[2 * kMaxAxis + k]);
+      dacc_fma(S, fv, dfl_from_double(__ldg(speed + l)));
     }
     const int j = col / NX, i = col - j * NX;
-    const double X = s_ax[i], Y = s_ax[kMaxAxis + j];
-    const double X2 = X * X, Y2 = Y * Y, XG0 = X * G0, YG0 = Y * G0;
-    acc[0] += G0;
-    acc[1] += XG0;
-    acc[2] += YG0;
-    acc[3] += G1;
-    acc[4] += X * XG0;
-    acc[5] += Y * YG0;
-    acc[6] += G2;
-    acc[7] += X * YG0;
-    acc[8] += X * G1;
-    acc[9] += Y * G1;
-    const double R2 = (X2 + Y2) * G0 + G2;   // sum_k f |c'|^2 over the column
-    const double R2z = (X2 + Y2) * G1 + G3;  // sum_k f z' |c'|^2
-    acc[10] += X * R2;
-    acc[11] += Y * R2;
-    acc[12] += R2z;
-    acc[13] += S;
+    const dfl X = s_ax[i], X2 = s_ax[kMaxAxis + i];
+    const dfl Y = s_ax[2 * kMaxAxis + j], Y2 = s_ax[3 * kMaxAxis + j];
+    const dfl g0 = dfl_norm(G0.hi, G0.lo), g1 = dfl_norm(G1.hi, G1.lo);
+    const dfl g2 = dfl_norm(G2.hi, G2.lo), g3 = dfl_norm(G3.hi, G3.lo);
+    dacc_add(sacc[0], g0);
+    dacc_fma(sacc[1], g0, X);
+    dacc_fma(sacc[2], g0, Y);
+    dacc_add(sacc[3], g1);
+    dacc_fma(sacc[4], g0, X2);
+    dacc_fma(sacc[5], g0, Y2);
+    dacc_add(sacc[6], g2);
+    dacc_fma(sacc[7], g0, dfl_mul(X, Y));
+    dacc_fma(sacc[8], g1, X);
+    dacc_fma(sacc[9], g1, Y);
+    const dfl XY2 = dfl_add(X2, Y2);
+    const dfl R2 = dfl_add(dfl_mul(XY2, g0), g2);   // sum_k f |c'|^2 over the column
+    const dfl R2z = dfl_add(dfl_mul(XY2, g1), g3);  // sum_k f z' |c'|^2
+    dacc_fma(sacc[10], R2, X);
+    dacc_fma(sacc[11], R2, Y);
+    dacc_add(sacc[12], R2z);
+    dacc_add(sacc[13], dfl_norm(S.hi, S.lo));
   }
+  double acc[kMomAcc];
+#pragma unroll
+  for (int q = 0; q < kMomAcc; ++q) acc[q] = dacc_to_double(sacc[q]);
   block_sum<kMomAcc>(acc, s_red);
   if (threadIdx.x == 0) {
     // the previous moments, for the residual (only this thread writes P)

@@ -316,6 +316,13 @@ def run_forms(pkg, args, fp64_value):
         "speedup_vs_fp64": res[pkg.DVM_PREC_FP32][0] / res[pkg.DVM_PREC_FP64][0],
         "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
         "steps_compared": args.steps + args.warmup}
+    out["cavity"] = run_cavity(pkg, args)
+    return out
+
+
+def run_cavity(pkg, args):
+    """Configuration 3 in the precision form and in FP64 from the same start and seed."""
+    import dataclasses
     cfg, g, f0 = cavity_config(pkg)
     res = {}
     kern = {}
@@ -327,7 +334,7 @@ def run_forms(pkg, args, fp64_value):
         res[prec] = (rate, ms, s.properties(), s.collision_count())
         s.close()
     cells = cfg.nx_space * cfg.ny_space
-    out["cavity"] = {
+    return {
         "workload": "2-D microcavity 64x64 cells, 24^3 on [-5,5], hard sphere, Kn=0.1, "
                     "diffuse walls T=1, lid u=0.3, samples from the reference formula "
                     "(ColnRMS 0.001), dt=0.0025",
@@ -342,7 +349,6 @@ def run_forms(pkg, args, fp64_value):
                  "ms_per_launch": kern[pkg.DVM_PREC_FP64]},
         "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
         "steps_compared": args.steps + args.warmup}
-    return out
 
 
 BATCH_GRIDS = (16, 24, 32, 40)
@@ -676,6 +682,14 @@ def run_gpu(args):
     return 0
 
 
+def run_case(args):
+    """One form alone (for profiling and quick checks): prints its JSON object."""
+    pkg = importlib.import_module("2d_dvm_microflows_gb300")
+    fn = {"cavity": run_cavity, "batch": run_batch, "served": run_serving}[args.case]
+    print(json.dumps({"case": args.case, "result": fn(pkg, args)}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -687,11 +701,15 @@ def main():
                     help="skip the precision-form and cavity measurements")
     ap.add_argument("--cells", type=int, default=None,
                     help="smaller case of the same workload (profiling only)")
+    ap.add_argument("--case", default=None, choices=["cavity", "batch", "served"],
+                    help="run one form alone and print its result (profiling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
     return run_gpu(args)
 
 

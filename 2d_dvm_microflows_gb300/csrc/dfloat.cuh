@@ -41,8 +41,10 @@ __device__ __forceinline__ dfl dfl_from_double(double x) {
     r.lo = 0.f;
     return r;
   }
-  if (ef >= 255) {           // |x| >= 2^128 or inf / NaN: carry to FP32 inf / NaN
-    r.hi = static_cast<float>(x);
+  if (ef >= 255) {           // |x| >= 2^128 or inf / NaN: FP32 inf / NaN (bit operations
+                             // only, so that no FP64 conversion is issued on the hot path)
+    const bool nan = (e == 2047) && (((bh & 0xfffffu) | bl) != 0u);
+    r.hi = __int_as_float(static_cast<int>(sign | 0x7f800000u | (nan ? 0x400000u : 0u)));
     r.lo = 0.f;
     return r;
   }
@@ -61,14 +63,27 @@ __device__ __forceinline__ dfl dfl_from_double(double x) {
   return r;
 }
 
-// Exact float -> double by integer operations; the rare FP32 subnormals (the lo part of
-// values below about 2^-102) take the hardware conversion.
+// Exact float -> double by integer operations (no FP64 conversion is issued): normal
+// floats by rebiasing the exponent, FP32 subnormals (the lo part of values below about
+// 2^-102) by normalising their mantissa, and inf / NaN carried over.
 __device__ __forceinline__ double dbl_from_float(float v) {
   const uint32_t u = static_cast<uint32_t>(__float_as_int(v));
   const uint32_t ex = (u >> 23) & 0xffu;
-  if (ex == 0u) return (u & 0x7fffffu) ? static_cast<double>(v) : 0.0;
-  const uint32_t hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-  const uint32_t lo = u << 29;
+  const uint32_t m = u & 0x7fffffu;
+  const uint32_t sign = u & 0x80000000u;
+  uint32_t hi, lo;
+  if (ex == 0u) {
+    if (m == 0u) return __hiloint2double(static_cast<int>(sign), 0);
+    const int p = 31 - __clz(static_cast<int>(m));            // top bit, 0..22
+    const unsigned long long mm =
+        (static_cast<unsigned long long>(m) << (52 - p)) & ((1ull << 52) - 1);
+    hi = sign | (static_cast<uint32_t>(p + 874) << 20) | static_cast<uint32_t>(mm >> 32);
+    lo = static_cast<uint32_t>(mm);
+  } else {
+    hi = sign | ((ex == 255u ? 2047u : ex + 896u) << 20) | (m >> 3) |
+         ((ex == 255u && m != 0u) ? 0x80000u : 0u);  // NaN stays NaN
+    lo = m << 29;
+  }
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
 }
 
@@ -105,6 +120,20 @@ __device__ __forceinline__ dfl dfl_add(dfl a, dfl b) {
 __device__ __forceinline__ dfl dfl_neg(dfl a) { return dfl_make(-a.hi, -a.lo); }
 
 __device__ __forceinline__ dfl dfl_sub(dfl a, dfl b) { return dfl_add(a, dfl_neg(b)); }
+
+// FP32 reciprocal and reciprocal square root estimates (MUFU, about 1 ulp); the callers
+// correct them with an exactly formed remainder.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 // Product with the FMA error term (the lo*lo term, below 2^-48 relative, is dropped).
 __device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
@@ -145,6 +174,46 @@ __device__ __forceinline__ void dacc_fma(dacc& s, dfl x, dfl c) {
 
 __device__ __forceinline__ double dacc_to_double(const dacc& s) {
   return dbl_from_float(s.hi) + dbl_from_float(s.lo);
+}
+
+// Block-wide sums of NV pairs without FP64 shuffles or adds: warp butterflies on the
+// (hi, lo) floats with pair additions, then warp 0 over the warp totals. Thread 0 gets
+// the totals as doubles in out; s_red must hold NV * 32 float2.
+template <int NV>
+__device__ __forceinline__ void block_sum_dfl(dacc (&v)[NV], float2* s_red, double (&out)[NV]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  dfl x[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    x[q] = dfl_norm(v[q].hi, v[q].lo);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dfl y;
+      y.hi = __shfl_xor_sync(0xffffffffu, x[q].hi, o);
+      y.lo = __shfl_xor_sync(0xffffffffu, x[q].lo, o);
+      x[q] = dfl_add(x[q], y);
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s_red[q * 32 + warp] = make_float2(x[q].hi, x[q].lo);
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const float2 t = lane < nw ? s_red[q * 32 + lane] : make_float2(0.f, 0.f);
+      dfl y = dfl_make(t.x, t.y);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        dfl z;
+        z.hi = __shfl_xor_sync(0xffffffffu, y.hi, o);
+        z.lo = __shfl_xor_sync(0xffffffffu, y.lo, o);
+        y = dfl_add(y, z);
+      }
+      out[q] = dfl_to_double(y);
+    }
+  }
 }
 
 }  // namespace dvm

@@ -35,15 +35,16 @@ struct dvm_ctx {
   double* d_props = nullptr;
   double* d_eq_pre = nullptr;
   double* d_eq_cache = nullptr;
-  double* d_cum_eq = nullptr;
-  double* d_cum_dev = nullptr;
-  double* d_kin = nullptr;
+  long long* d_cum_eq = nullptr;   // fixed-point CDFs
+  long long* d_cum_dev = nullptr;
+  float* d_kin = nullptr;
   int2* d_ref_eq = nullptr;
   int2* d_ref_dev = nullptr;
   CellPlan* d_plan = nullptr;
   long long* d_chunk_off = nullptr;
   long long* d_total_samples = nullptr;
   double* d_ghost = nullptr;
+  float2* d_cfl = nullptr;      // 2-D upwind |CFL| per axis node as hi + lo pairs
   uint32_t* d_err = nullptr;
   double* d_flush = nullptr;
   size_t flush_n = 0;
@@ -187,7 +188,7 @@ void release(dvm_ctx* c) {
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
                   c->d_axis_tab, c->d_gtab, c->d_trig, c->d_df, c->d_axis_tab_f,
-                  c->d_gtab_f, c->d_trig_f, c->d_residual};
+                  c->d_gtab_f, c->d_trig_f, c->d_residual, c->d_cfl};
   for (void* b : bufs)
     if (b) {
       if (c->async_alloc) cudaFreeAsync(b, c->stream);
@@ -311,7 +312,9 @@ int build_collision_tables(dvm_ctx* c) {
     h2d(c, c->d_gtab, gt.data(), gt.size() * sizeof(double2));
     c->tabs.gtab = c->d_gtab;
     c->tabs.gtab_n = ns;
-    c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
+    // staged in shared memory only while the collide CTA stays small enough for three
+    // CTAs per SM; larger tables are read through L1
+    c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 32 * 1024) ? 1 : 0;
   }
   if (c->p.precision == DVM_PREC_FP32) {
     // FP32 copies of the same tables for k_collide_f32
@@ -529,6 +532,20 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
       release(c);
       return st;
     }
+    // |dt/dx x_i|, |dt/dy y_j| split into float pairs for the convection kernel
+    std::vector<float2> cfl(g.nx + g.ny);
+    for (int i = 0; i < g.nx + g.ny; ++i) {
+      const double v = (i < g.nx) ? std::fabs(params->dt / params->dx * c->hx[i])
+                                  : std::fabs(params->dt / params->dy * c->hy[i - g.nx]);
+      const float h = static_cast<float>(v);
+      cfl[i] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+    }
+    if ((st = dalloc(c, &c->d_cfl, cfl.size()))) {
+      release(c);
+      return st;
+    }
+    h2d(c, c->d_cfl, cfl.data(), cfl.size() * sizeof(float2));
+    cudaStreamSynchronize(c->stream);
   }
   if (params->coll_method != DVM_COLL_NONE) {
     if ((st = build_collision_tables(c))) {
@@ -709,6 +726,7 @@ int dvm_compute_convection(dvm_ctx* c) {
       a.bc_left = c->p.bc[DVM_WALL_LEFT]; a.bc_right = c->p.bc[DVM_WALL_RIGHT];
       for (int s = 0; s < 4; ++s) a.base[s] = c->wall_base[s];
       a.xf = c->p.dt / c->p.dx; a.yf = c->p.dt / c->p.dy;
+      a.cfl = c->d_cfl;
       a.f = c->d_f; a.ghost = c->d_ghost; a.fconv = c->d_fconv;
       st = launch(c, DVM_K_CONVECT, [&] { return launch_convect2d(a, c->ncells, c->stream); });
     }
@@ -962,7 +980,8 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
              + sizeof(uint32_t) + nv * d                    // error word, speeds
              + sizeof(unsigned long long);                  // residual
   if (p->coll_method != DVM_COLL_NONE) {
-    b += 4 * C * (nv + 1) * d + C * 4 * d;                  // eq_pre, cum_eq, cum_dev, kin, cache
+    b += 3 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float) + C * 4 * d;  // eq_pre, cum_eq,
+                                                            // cum_dev, kin, cache
     b += 2 * C * kNRef * sizeof(int2) + C * sizeof(CellPlan) +
          (3 * C + 1) * sizeof(long long) + sizeof(long long);
     const size_t nmax = std::max(vg->nx, std::max(vg->ny, vg->nz));
@@ -978,7 +997,7 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
     size_t n = 2 * static_cast<size_t>(p->nx_space);
     if (p->bc[DVM_WALL_LEFT] == DVM_BC2D_WALL) n += p->ny_space;
     if (p->bc[DVM_WALL_RIGHT] == DVM_BC2D_WALL) n += p->ny_space;
-    b += n * nv * d;
+    b += n * nv * d + static_cast<size_t>(vg->nx + vg->ny) * sizeof(float2);
   }
   return b;
 }

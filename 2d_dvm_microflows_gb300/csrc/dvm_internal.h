@@ -48,11 +48,11 @@ struct CdfArgs {
   int ncells;
   const double* f;          // [C][nv]
   const double* props;      // [C][DVM_NPROP]
-  double* eq_pre;           // [C][nv+1] cached equilibrium prefix sums
+  double* eq_pre;           // [C][nv+1] cached equilibrium, one value per node
   double* eq_cache;         // [C][4]  dens, u, v, temp of the cached equilibrium
-  double* cum_eq;           // [C][nv+1]
-  double* cum_dev;          // [C][nv+1] (FMC: cumulative |f|)
-  double* kin;              // [C][nv+1] (VR: f - f_eq; FMC: f)
+  long long* cum_eq;        // [C][nv+1] cumulative f_eq, fixed point (see k_cdf)
+  long long* cum_dev;       // [C][nv+1] cumulative |f - f_eq| (FMC: |f|), fixed point
+  float* kin;               // [C][nv+1] (VR: f - f_eq; FMC: f), read for its sign
   int2* ref_eq;             // [C][1000]
   int2* ref_dev;            // [C][1000]
   CellPlan* plan;           // [C]
@@ -116,9 +116,9 @@ struct CollideArgs {
   uint32_t step;
   const uint32_t* step_dev;  // if set, the Philox step is read here (graph replays)
   double* f;
-  const double* cum_eq;
-  const double* cum_dev;
-  const double* kin;
+  const long long* cum_eq;
+  const long long* cum_dev;
+  const float* kin;
   const int2* ref_eq;
   const int2* ref_dev;
   const CellPlan* plan;
@@ -146,6 +146,7 @@ struct Convect2DArgs {
   int bc_left, bc_right;
   int base[4];
   double xf, yf;            // dt/dx, dt/dy
+  const float2* cfl;        // |dt/dx x_i| (nx) then |dt/dy y_j| (ny) as hi + lo pairs
   const double* f;
   const double* ghost;
   double* fconv;

@@ -23,8 +23,16 @@ namespace dvm {
 // ----------------------------------------------------------------------------------------
 // k_cdf: one CTA per cell.
 // VR: collisions/variance_reduction.f90:234-496. FMC: collisions/full_mc.f90:110-180.
+//
+// The cumulative sums are kept in 64-bit fixed point: every term (f_eq, |f - f_eq| or |f|,
+// all nonnegative) is truncated to a multiple of 2^-k, with 2^k chosen per cell so that
+// 16 n 2^k <= 2^62 (n the cell density), and summed in integers. The sums are exact and
+// independent of the order of summation, so the parallel scan gives the sequential sum
+// bit for bit; the quantum 2^-k is below 1e-17 n, finer than the FP64 rounding of the
+// reference's running sum. The partner search (k_collide) then compares integers only.
 constexpr int kCdfThreads = 512;
 constexpr int kCdfPer = 8;
+constexpr int kCdfCoarseMax = 2048;  // entries of the shared-memory coarse index per table
 
 __device__ long long num_coll_pairs(const CollParams& cp, double beta3_min, double densA,
                                     double densB, double temp) {
@@ -39,12 +47,70 @@ __device__ long long num_coll_pairs(const CollParams& cp, double beta3_min, doub
   return llround(val);
 }
 
+// x 2^k truncated to an integer, for x >= 0, from the bits of x (no FP64 op). Terms that
+// would not fit below 2^62 are clamped and reported.
+__device__ __forceinline__ long long to_fixed(double x, int k, uint32_t& bad) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x)) &
+                               0x7fffffffffffffffull;
+  const int e = static_cast<int>(b >> 52);
+  if (e == 0) return 0;  // zero or FP64 subnormal
+  if (e == 2047) { bad |= DVM_EW_NONFINITE; return 1ll << 58; }
+  const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  const int sh = e - 1075 + k;
+  if (sh >= 0) {
+    if (sh > 9) { bad |= DVM_EW_NONFINITE; return 1ll << 58; }
+    return static_cast<long long>(mant << sh);
+  }
+  if (sh <= -64) return 0;
+  return static_cast<long long>(mant >> (-sh));
+}
+
+// Sign of v as +-1.0f (the collision kernels read only the sign bit of kin).
+__device__ __forceinline__ float sign_float(double v) {
+  const uint32_t hi = static_cast<uint32_t>(__double_as_longlong(v) >> 32);
+  return __int_as_float(static_cast<int>((hi & 0x80000000u) | 0x3f800000u));
+}
+
+// Block-wide exclusive scan of two int64 per thread; tot gets the block totals.
+__device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long long& tot_a,
+                                                long long& tot_b, long long* s_scan) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long ta = __shfl_up_sync(0xffffffffu, ia, o);
+    const long long tb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) { ia += ta; ib += tb; }
+  }
+  if (lane == 31) { s_scan[warp] = ia; s_scan[32 + warp] = ib; }
+  __syncthreads();
+  if (warp == 0) {
+    long long wa = lane < nw ? s_scan[lane] : 0, wb = lane < nw ? s_scan[32 + lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long ta = __shfl_up_sync(0xffffffffu, wa, o);
+      const long long tb = __shfl_up_sync(0xffffffffu, wb, o);
+      if (lane >= o) { wa += ta; wb += tb; }
+    }
+    s_scan[64 + lane] = wa;
+    s_scan[96 + lane] = wb;
+  }
+  __syncthreads();
+  const long long wpa = warp > 0 ? s_scan[64 + warp - 1] : 0;
+  const long long wpb = warp > 0 ? s_scan[96 + warp - 1] : 0;
+  tot_a = s_scan[64 + nw - 1];
+  tot_b = s_scan[96 + nw - 1];
+  a = wpa + ia - a;  // exclusive
+  b = wpb + ib - b;
+}
+
 __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
-  __shared__ double s_scan[64];
+  __shared__ long long s_scan[2][128];
   __shared__ double s_par[6];
-  __shared__ int s_new;
+  __shared__ int s_new, s_k;
   __shared__ int s_right[2][kNRef];
   __shared__ double s_fac[3 * kMaxAxis];
+  __shared__ long long s_coarse[2][kCdfCoarseMax + 1];
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
   const int nv = g.nv;
@@ -52,14 +118,24 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   const double* f = a.f + static_cast<size_t>(cell) * nv;
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
   double* eq = a.eq_pre + cs;  // cached equilibrium, one value per node
-  double* ce = a.cum_eq + cs;
-  double* cd = a.cum_dev + cs;
-  double* kin = a.kin + cs;
+  long long* ce = a.cum_eq + cs;
+  long long* cd = a.cum_dev + cs;
+  float* kin = a.kin + cs;
   const bool vr = (a.cp.method == DVM_COLL_VR);
   const int NX = g.nx, NXY = g.nx * g.ny;
+  // coarse index: every cstep-th cumulative value, cstep a power of two
+  int cstep = 8;
+  while ((nv + 1) / cstep > kCdfCoarseMax) cstep <<= 1;
+  const int ncoarse = nv / cstep;  // entries 0..ncoarse
 
-  if (vr) {
-    if (threadIdx.x == 0) {
+  if (threadIdx.x == 0) {
+    // fixed-point scale from the cell density: 16 n 2^k <= 2^62
+    const double n0 = P[DVM_P_DENS];
+    int E = 1;
+    if (n0 > 0.0 && isfinite(n0)) E = ilogb(n0) + 1;  // n0 < 2^E
+    s_k = 58 - E;
+    s_new = 0;
+    if (vr) {
       const double dens = P[DVM_P_DENS], u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
       double temp = P[DVM_P_SPECIES_TEMP];
       if (temp < kDoubleTol) temp = P[DVM_P_TEMP];
@@ -73,59 +149,65 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
       s_new = nw;
       s_par[0] = mc; s_par[1] = u; s_par[2] = v; s_par[3] = w; s_par[4] = temp;
     }
-    __syncthreads();
-    if (s_new) {
-      // the Maxwellian times the node volume factorises over the axes:
-      // mc exp(-m|c-u|^2/T) bx by bz = [mc e_x bx] [e_y by] [e_z bz]
-      const double mc = s_par[0], temp = s_par[4], m = a.cp.mass;
-      const int nsum = g.nx + g.ny + g.nz;
-      for (int t = threadIdx.x; t < nsum; t += blockDim.x) {
-        double val = 0.0;
-        if (temp > 0.0) {
-          if (t < g.nx) {
-            const double c = g.x[t] - s_par[1];
-            val = mc * exp(-(c * c) * m / temp) * g.bx[t];
-          } else if (t < g.nx + g.ny) {
-            const double c = g.y[t - g.nx] - s_par[2];
-            val = exp(-(c * c) * m / temp) * g.by[t - g.nx];
-          } else {
-            const double c = g.z[t - g.nx - g.ny] - s_par[3];
-            val = exp(-(c * c) * m / temp) * g.bz[t - g.nx - g.ny];
-          }
-        }
-        s_fac[t < g.nx ? t : (t < g.nx + g.ny ? kMaxAxis + t - g.nx
-                                                : 2 * kMaxAxis + t - g.nx - g.ny)] = val;
-      }
-      __syncthreads();
-      for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-        const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
-        eq[l] = s_fac[i] * s_fac[kMaxAxis + j] * s_fac[2 * kMaxAxis + k];
-      }
-      __syncthreads();
-    }
   }
-  // deviation and CDFs: each thread scans kCdfPer consecutive nodes in sequence, the
-  // thread totals are scanned across the block (cumul_df of variance_reduction.f90:454-456,
-  // full_mc.f90:151-152)
-  double carry_e = 0.0, carry_d = 0.0;
+  __syncthreads();
+  const bool recompute = vr && s_new;
+  if (recompute) {
+    // the Maxwellian times the node volume factorises over the axes:
+    // mc exp(-m|c-u|^2/T) bx by bz = [mc e_x bx] [e_y by] [e_z bz]
+    const double mc = s_par[0], temp = s_par[4], m = a.cp.mass;
+    const int nsum = g.nx + g.ny + g.nz;
+    for (int t = threadIdx.x; t < nsum; t += blockDim.x) {
+      double val = 0.0;
+      if (temp > 0.0) {
+        if (t < g.nx) {
+          const double c = g.x[t] - s_par[1];
+          val = mc * exp(-(c * c) * m / temp) * g.bx[t];
+        } else if (t < g.nx + g.ny) {
+          const double c = g.y[t - g.nx] - s_par[2];
+          val = exp(-(c * c) * m / temp) * g.by[t - g.nx];
+        } else {
+          const double c = g.z[t - g.nx - g.ny] - s_par[3];
+          val = exp(-(c * c) * m / temp) * g.bz[t - g.nx - g.ny];
+        }
+      }
+      s_fac[t < g.nx ? t : (t < g.nx + g.ny ? kMaxAxis + t - g.nx
+                                              : 2 * kMaxAxis + t - g.nx - g.ny)] = val;
+    }
+    __syncthreads();
+  }
+  const int k = s_k;
+  uint32_t bad = 0;
+  // deviation and CDFs: each thread takes kCdfPer consecutive nodes of a chunk, scans them
+  // in sequence, and the thread sums are scanned across the block (cumul_df of
+  // variance_reduction.f90:454-456, full_mc.f90:151-152)
+  long long carry_e = 0, carry_d = 0;
   for (int base = 0; base < nv; base += kCdfThreads * kCdfPer) {
     const int l0 = base + threadIdx.x * kCdfPer;
-    double pe[kCdfPer], ad[kCdfPer];
+    long long pe[kCdfPer], ad[kCdfPer];
 #pragma unroll
     for (int q = 0; q < kCdfPer; ++q) {
       const int l = l0 + q;
-      pe[q] = 0.0;
-      ad[q] = 0.0;
+      pe[q] = 0;
+      ad[q] = 0;
       if (l < nv) {
         if (vr) {
-          pe[q] = eq[l];
-          const double pn = f[l] - pe[q];
-          kin[l + 1] = pn;
-          ad[q] = fabs(pn);
+          double ev;
+          if (recompute) {
+            const int kk = l / NXY, j = (l - kk * NXY) / NX, i = l - kk * NXY - j * NX;
+            ev = s_fac[i] * s_fac[kMaxAxis + j] * s_fac[2 * kMaxAxis + kk];
+            eq[l] = ev;
+          } else {
+            ev = eq[l];
+          }
+          const double pn = f[l] - ev;
+          kin[l + 1] = sign_float(pn);
+          pe[q] = to_fixed(ev, k, bad);
+          ad[q] = to_fixed(pn, k, bad);  // |pn| (the sign bit is dropped)
         } else {
           const double fv = f[l];
-          kin[l + 1] = fv;
-          ad[q] = fabs(fv);
+          kin[l + 1] = sign_float(fv);
+          ad[q] = to_fixed(fv, k, bad);
         }
       }
     }
@@ -134,41 +216,61 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
       pe[q] += pe[q - 1];
       ad[q] += ad[q - 1];
     }
-    double ie = pe[kCdfPer - 1], id = ad[kCdfPer - 1], te, td;
-    block_scan2(ie, id, te, td, s_scan);
-    const double oe = carry_e + (ie - pe[kCdfPer - 1]);
-    const double od = carry_d + (id - ad[kCdfPer - 1]);
+    long long oe = pe[kCdfPer - 1], od = ad[kCdfPer - 1], te, td;
+    block_scan2_i64(oe, od, te, td, &s_scan[0][0]);
+    oe += carry_e;
+    od += carry_d;
 #pragma unroll
     for (int q = 0; q < kCdfPer; ++q) {
-      const int l = l0 + q;
-      if (l < nv) {
-        if (vr) ce[l + 1] = oe + pe[q];
-        cd[l + 1] = od + ad[q];
+      const int p = l0 + q + 1;  // position in the cumulative arrays
+      if (p <= nv) {
+        const long long ve = oe + pe[q], vd = od + ad[q];
+        if (vr) ce[p] = ve;
+        cd[p] = vd;
+        if ((p & (cstep - 1)) == 0) {
+          s_coarse[0][p / cstep] = ve;
+          s_coarse[1][p / cstep] = vd;
+        }
       }
     }
     carry_e += te;
     carry_d += td;
+    __syncthreads();  // s_scan is reused by the next chunk
   }
-  if (threadIdx.x == 0) { ce[0] = 0.0; cd[0] = 0.0; kin[0] = 0.0; }
+  if (threadIdx.x == 0) {
+    ce[0] = 0; cd[0] = 0; kin[0] = 0.f;
+    s_coarse[0][0] = 0;
+    s_coarse[1][0] = 0;
+    if (carry_e < 0 || carry_d < 0) bad |= DVM_EW_NONFINITE;  // the scale did not hold
+  }
   __syncthreads();
 
   // Bucket tables, variance_reduction.f90:471-493: right(r) is the first l >= 1 with
-  // cum(l) >= r*max (the reference's running pointer reaches the same l because both the
-  // CDF and the targets are nondecreasing); left(r) = right(r-1) - 1; right(1000) = n.
-  // CDF values and targets are nonnegative, so their bit patterns compare as integers.
+  // cum(l) >= target(r), target(r) = floor(r T / 1000) with T = cum(n) (the reference's
+  // r * 0.001 * cum(n), here exact); left(r) = right(r-1) - 1; right(1000) = n. The coarse
+  // index narrows each lookup to cstep entries.
   const int ntab = vr ? 2 : 1;
   for (int t = 0; t < ntab; ++t) {
-    const double* cum = (vr && t == 0) ? ce : cd;
-    const long long* ck = reinterpret_cast<const long long*>(cum);
-    const double mx = 0.001 * cum[nv];
+    const int ti = (vr && t == 0) ? 0 : 1;
+    const long long* cum = (ti == 0) ? ce : cd;
+    const long long T = (ti == 0) ? carry_e : carry_d;
+    const long long Tq = T / 1000, Tr = T % 1000;
     for (int r = threadIdx.x + 1; r <= kNRef; r += kCdfThreads) {
-      const long long target = __double_as_longlong(static_cast<double>(r) * mx);
-      int lo = 1, hi = nv + 1;
+      const long long target = Tq * r + (Tr * r) / 1000;
+      int lo = 0, hi = ncoarse + 1;  // first coarse entry >= target
       while (lo < hi) {
-        const int mid = lo + (hi - lo) / 2;
-        if (target > ck[mid]) lo = mid + 1; else hi = mid;
+        const int mid = (lo + hi) >> 1;
+        if (target > s_coarse[ti][mid]) lo = mid + 1; else hi = mid;
       }
-      s_right[t][r - 1] = lo;
+      int plo = (lo == 0) ? 1 : (lo - 1) * cstep + 1;
+      int phi = (lo > ncoarse) ? nv : lo * cstep;
+      if (plo < 1) plo = 1;
+      phi = phi > nv ? nv : phi;
+      while (plo < phi) {  // first p in [plo, phi] with cum(p) >= target
+        const int mid = (plo + phi) >> 1;
+        if (target > cum[mid]) plo = mid + 1; else phi = mid;
+      }
+      s_right[t][r - 1] = plo;
     }
   }
   __syncthreads();
@@ -181,14 +283,17 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
       ref[r - 1] = e;
     }
   }
+  if (bad) atomicOr(a.err, bad);
 
   // Sample plan of this cell-step.
   if (threadIdx.x == 0) {
     CellPlan pl;
     const CollParams& cp = a.cp;
+    const double qk = ldexp(1.0, -k);
     if (vr) {
       const double dens = P[DVM_P_DENS], temp = P[DVM_P_SPECIES_TEMP];
-      const double eq_dens = ce[nv], neq_dens = cd[nv];
+      const double eq_dens = static_cast<double>(carry_e) * qk;
+      const double neq_dens = static_cast<double>(carry_d) * qk;
       const double fc = cp.dt * 0.5 / cp.Kn;  // n = m: factor_coeff = dt*0.5/Kn
       const double r = 0.5 * neq_dens / dens;
       const double dA[3] = {1.0, r, r}, dB[3] = {r, 1.0, r};
@@ -223,7 +328,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
                            : 0.0;
     } else {
       const double dens = P[DVM_P_DENS], temp = P[DVM_P_TEMP];
-      const double neg = 0.5 * (dens - cd[nv]);
+      const double neg = 0.5 * (dens - static_cast<double>(carry_d) * qk);
       const double absd = dens - 2.0 * neg;
       long long num;
       if (a.pairs.active) num = a.pairs.count[0];
@@ -302,39 +407,45 @@ cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
 // k_collide: persistent; a chunk is kCollideChunk consecutive samples of one
 // (cell, sub-integral). One thread per sample.
 //
-// GB300 runs FP64 at 1/64 of its FP32 rate, so this kernel keeps FP64 only where the
-// reference's FP64 rounding decides a discrete outcome (the partner search) and moves
-// the rest off the FP64 pipe: order-preserving integer keys for every search compare,
-// tables of node differences / reciprocals / remap denominator terms, a table of g and
-// g^(2-2 omega) on cubic uniform grids, the exact 1/2 mass ratios of like-species pairs,
-// and hi + lo float pairs for the post-collision velocities, the remap weights and the
-// contributions. Each of these changes a value by at most about 2^-46 relative; the
-// parity bar (1e-12 of max|f| against the restatement) checks the sum.
+// GB300 runs FP64 at 1/64 of its FP32 rate, so this kernel moves its arithmetic off the
+// FP64 pipe: the partner search compares exact fixed-point integers (the CDFs of k_cdf and
+// the target floor(R T) formed from the 53-bit integer behind R), the remap uses tables of
+// node differences / reciprocals / denominator terms, a table of g and g^(2-2 omega) on
+// cubic uniform grids, the exact 1/2 mass ratios of like-species pairs, and hi + lo float
+// pairs for the post-collision velocities, the remap weights and the contributions. Each
+// of these changes a value by at most about 2^-46 relative; the parity bar (1e-12 of
+// max|f| against the restatement) checks the sum.
 
-// Integer key with the order of the doubles (-0.0 folded onto +0.0).
-__device__ __forceinline__ long long okey(double d) {
-  long long b = __double_as_longlong(d);
-  if (b == static_cast<long long>(0x8000000000000000ULL)) b = 0;
-  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+// R 2^53 truncated, from the bits of R in [0, 1): the 53-bit integer behind a Philox
+// uniform, exactly.
+__device__ __forceinline__ unsigned long long u53_bits(double R) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(R));
+  const int e = static_cast<int>((b >> 52) & 0x7ff);
+  if (e == 0 || e > 1022 || 1022 - e >= 64) return 0;
+  return ((b & ((1ull << 52) - 1)) | (1ull << 52)) >> (1022 - e);
 }
 
-// referenced_search with integer compares (the CDF and the target are nonnegative).
-__device__ __forceinline__ int referenced_search_keys(const double* __restrict__ cum,
-                                                      const int2* __restrict__ ref, int n,
-                                                      double R, uint32_t& bad) {
-  if (R < kDoubleTol) return 0;
-  int i = static_cast<int>(ceil(R * 1000.0));
+// referenced_search (utils/sort_and_search.f90:40-86) on the fixed-point CDF: bucket
+// ceil(1000 R), then bisection for cum(idx) < R cum(n) <= cum(idx+1), with the target
+// floor(R T) and the bucket index formed exactly in integers. The buckets of k_cdf are
+// built with the same exact targets, so the answer always lies inside its bucket.
+__device__ __forceinline__ int referenced_search_fixed(const long long* __restrict__ cum,
+                                                       const int2* __restrict__ ref, int n,
+                                                       double R, uint32_t& bad) {
+  if (__double_as_longlong(R) < __double_as_longlong(kDoubleTol)) return 0;  // R < tol
+  const unsigned long long m = u53_bits(R);
+  int i = static_cast<int>((1000ull * m + ((1ull << 53) - 1)) >> 53);
   i = i < 1 ? 1 : (i > kNRef ? kNRef : i);
   const int2 lr = __ldg(ref + i - 1);
   int left = lr.x, right = lr.y;
   int idx = left + (right - left) / 2;
   if (left == right) return idx < n ? idx : n - 1;
-  const long long* ck = reinterpret_cast<const long long*>(cum);
-  const long long adj = okey(R * __ldg(cum + n));
+  const unsigned long long T = static_cast<unsigned long long>(__ldg(cum + n));
+  const long long adj = static_cast<long long>((__umul64hi(m, T) << 11) | ((m * T) >> 53));
   for (int it = 0; it < kMaxSearchIters; ++it) {
     if (idx < 0 || idx >= n) break;
-    const long long c0 = okey(__longlong_as_double(__ldg(ck + idx)));
-    if (adj > c0 && adj <= okey(__longlong_as_double(__ldg(ck + idx + 1)))) return idx;
+    const long long c0 = __ldg(cum + idx);
+    if (adj > c0 && adj <= __ldg(cum + idx + 1)) return idx;
     if (adj > c0) left = idx; else right = idx;
     idx = left + (right - left) / 2;
   }
@@ -342,7 +453,7 @@ __device__ __forceinline__ int referenced_search_keys(const double* __restrict__
   int lo = 0, hi = n;
   while (hi - lo > 1) {
     const int mid = lo + (hi - lo) / 2;
-    if (adj > okey(__ldg(cum + mid))) lo = mid; else hi = mid;
+    if (adj > __ldg(cum + mid)) lo = mid; else hi = mid;
   }
   return lo;
 }
@@ -389,9 +500,9 @@ __device__ __forceinline__ dfl dfl_scale(dfl a, float s) {  // s a power of two
 }
 
 // Division with one correction step (Karp-Markstein style): q1 = a/b in FP32, the
-// remainder a - q1 b formed exactly by FMA, divided again.
+// remainder a - q1 b formed exactly by FMA, divided again (about 2^-45 relative).
 __device__ __forceinline__ dfl dfl_div(dfl a, dfl b) {
-  const float rb = __frcp_rn(b.hi);
+  const float rb = rcp_approx(b.hi);
   const float q1 = __fmul_rn(a.hi, rb);
   const float p = __fmul_rn(q1, b.hi);
   const float e = __fmaf_rn(q1, b.hi, -p);
@@ -400,13 +511,15 @@ __device__ __forceinline__ dfl dfl_div(dfl a, dfl b) {
   return dfl_norm(q1, q2);
 }
 
+// Square root from the reciprocal square root estimate y: s = a y, then s + (a - s^2) y / 2.
 __device__ __forceinline__ dfl dfl_sqrt(dfl a) {
   if (!(a.hi > 0.f)) return dfl_make(0.f, 0.f);
-  const float s = __fsqrt_rn(a.hi);
+  const float y = rsqrt_approx(a.hi);
+  const float s = __fmul_rn(a.hi, y);
   const float p = __fmul_rn(s, s);
   const float e = __fmaf_rn(s, s, -p);
   const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
-  return dfl_norm(s, __fmul_rn(r, __fdiv_rn(0.5f, s)));
+  return dfl_norm(s, __fmul_rn(r, 0.5f * y));
 }
 
 // Nearest node, as nearest() but on pair keys.
@@ -560,7 +673,7 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   return L;
 }
 
-__global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
+__global__ void __launch_bounds__(kCollideChunk, 3) k_collide(CollideArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
   const CollideSmem L = collide_smem_layout(g, a.t);
@@ -658,10 +771,10 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
     } else {
       if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
       const bool aeq = vr && q == 0, beq = vr && q == 1;
-      lA = referenced_search_keys((aeq ? a.cum_eq : a.cum_dev) + cs,
+      lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
                                   (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                   nv, rA, bad);
-      lB = referenced_search_keys((beq ? a.cum_eq : a.cum_dev) + cs,
+      lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
                                   (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                   nv, rB, bad);
     }
@@ -684,7 +797,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide(CollideArgs a) {
       g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
     }
     // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old
-    const double* kc = a.kin + cs;
+    const float* kc = a.kin + cs;
     const bool negA = (vr && q == 0) ? false : signbit(__ldg(kc + lA + 1));
     const bool negB = (vr && q == 1) ? false : signbit(__ldg(kc + lB + 1));
     // vr_depletion_routine elastic part (variance_reduction.f90:1157-1166): kin_depl(1) =
@@ -1044,10 +1157,10 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, Co
     } else {
       if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
       const bool aeq = vr && q == 0, beq = vr && q == 1;
-      lA = referenced_search_keys((aeq ? a.cum_eq : a.cum_dev) + cs,
+      lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
                                   (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                   nv, rA, bad);
-      lB = referenced_search_keys((beq ? a.cum_eq : a.cum_dev) + cs,
+      lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
                                   (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                   nv, rB, bad);
     }
@@ -1069,7 +1182,7 @@ __global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, Co
       if (gg < 1e-13f) continue;
       g_sigma = (vhs == 1.f) ? gg : powf(gg, vhs);
     }
-    const double* kc = a.kin + cs;
+    const float* kc = a.kin + cs;
     const float sA = (vr && q == 0) ? 1.f : (signbit(__ldg(kc + lA + 1)) ? -1.f : 1.f);
     const float sB = (vr && q == 1) ? 1.f : (signbit(__ldg(kc + lB + 1)) ? -1.f : 1.f);
     const float kin = sA * sB * factor * g_sigma;
@@ -1177,13 +1290,21 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
 // M_kl = sum w phi_k phi_l, r_k = sum df phi_k, has zero mass, momentum and energy; it is
 // the smallest such change in the w-weighted norm and vanishes where df does. The sums
 // are taken column by column: per (i, j), sum_k of df z^p (p < 3) and of w z^p (p < 5).
+//
+// r must be FP64-accurate (it is the non-conservation being removed) and is summed in
+// hi + lo float pairs; M only sets the shape of the correction, whose size is that of r,
+// so FP32 sums suffice for it (a relative error e in M leaves e |r| unconserved, some
+// 1e-16 of the cell's moments). The correction w * poly is formed in FP32 for the same
+// reason, and f + df - w * poly is formed in FP64 from the exact doubles of the two floats.
 constexpr int kProjThreads = 256;
 
 __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
-  __shared__ double s_red[20 * 32];
-  __shared__ double s_lam[5];
-  __shared__ double s_ax[2 * kMaxAxis];
-  __shared__ double s_z[4 * kMaxAxis];
+  __shared__ float2 s_red[20 * 32];
+  __shared__ float s_lam[5];
+  __shared__ dfl s_axd[2 * kMaxAxis];  // x', y' as pairs
+  __shared__ dfl s_zd[2 * kMaxAxis];   // z', z'^2 as pairs
+  __shared__ float s_axf[2 * kMaxAxis];
+  __shared__ float s_zf[4 * kMaxAxis];  // z'^p, p = 1..4
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
@@ -1191,64 +1312,80 @@ __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
   double* f = a.f + static_cast<size_t>(cell) * nv;
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
   const double u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
-  for (int t = threadIdx.x; t < NX; t += blockDim.x) s_ax[t] = g.x[t] - u;
-  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) s_ax[kMaxAxis + t] = g.y[t] - v;
+  for (int t = threadIdx.x; t < NX; t += blockDim.x) {
+    const double x = g.x[t] - u;
+    s_axd[t] = dfl_from_double(x);
+    s_axf[t] = static_cast<float>(x);
+  }
+  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) {
+    const double y = g.y[t] - v;
+    s_axd[kMaxAxis + t] = dfl_from_double(y);
+    s_axf[kMaxAxis + t] = static_cast<float>(y);
+  }
   for (int t = threadIdx.x; t < NZ; t += blockDim.x) {
     const double z = g.z[t] - w;
-    s_z[t] = z;
-    s_z[kMaxAxis + t] = z * z;
-    s_z[2 * kMaxAxis + t] = z * z * z;
-    s_z[3 * kMaxAxis + t] = (z * z) * (z * z);
+    s_zd[t] = dfl_from_double(z);
+    s_zd[kMaxAxis + t] = dfl_from_double(z * z);
+    const float zf = static_cast<float>(z);
+    s_zf[t] = zf;
+    s_zf[kMaxAxis + t] = zf * zf;
+    s_zf[2 * kMaxAxis + t] = zf * zf * zf;
+    s_zf[3 * kMaxAxis + t] = (zf * zf) * (zf * zf);
   }
   __syncthreads();
-  // 0-4: r; 5-19: M (row-major upper triangle)
-  double acc[20];
+  // 0-4: r (pairs); 5-19: M (row-major upper triangle, FP32 per thread)
+  dacc acc[20];
 #pragma unroll
-  for (int q = 0; q < 20; ++q) acc[q] = 0.0;
+  for (int q = 0; q < 20; ++q) dacc_zero(acc[q]);
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
-    double D0 = 0.0, D1 = 0.0, D2 = 0.0, W0 = 0.0, W1 = 0.0, W2 = 0.0, W3 = 0.0, W4 = 0.0;
+    dacc D0, D1, D2;
+    dacc_zero(D0); dacc_zero(D1); dacc_zero(D2);
+    float W0 = 0.f, W1 = 0.f, W2 = 0.f, W3 = 0.f, W4 = 0.f;
+#pragma unroll 4
     for (int k = 0; k < NZ; ++k) {
-      const float dfl = df[col + NXY * k];
-      if (dfl == 0.f) continue;
-      const double d = static_cast<double>(dfl), wt = fabs(d);
-      const double z = s_z[k], z2 = s_z[kMaxAxis + k];
-      D0 += d; D1 += d * z; D2 += d * z2;
-      W0 += wt; W1 += wt * z; W2 += wt * z2;
-      W3 += wt * s_z[2 * kMaxAxis + k]; W4 += wt * s_z[3 * kMaxAxis + k];
+      const float d = df[col + NXY * k];
+      if (d == 0.f) continue;
+      const dfl dd = dfl_make(d, 0.f);
+      dacc_add(D0, dd);
+      dacc_fma(D1, dd, s_zd[k]);
+      dacc_fma(D2, dd, s_zd[kMaxAxis + k]);
+      const float wt = fabsf(d);
+      W0 += wt;
+      W1 = fmaf(wt, s_zf[k], W1);
+      W2 = fmaf(wt, s_zf[kMaxAxis + k], W2);
+      W3 = fmaf(wt, s_zf[2 * kMaxAxis + k], W3);
+      W4 = fmaf(wt, s_zf[3 * kMaxAxis + k], W4);
     }
     const int j = col / NX, i = col - j * NX;
-    const double X = s_ax[i], Y = s_ax[kMaxAxis + j];
-    const double R = X * X + Y * Y;
-    const double E0 = R * W0 + W2;  // sum w |c|^2
-    acc[0] += D0;
-    acc[1] += X * D0;
-    acc[2] += Y * D0;
-    acc[3] += D1;
-    acc[4] += R * D0 + D2;
-    acc[5] += W0;                    // M00
-    acc[6] += X * W0;                // M01
-    acc[7] += Y * W0;                // M02
-    acc[8] += W1;                    // M03
-    acc[9] += E0;                    // M04
-    acc[10] += X * X * W0;           // M11
-    acc[11] += X * Y * W0;           // M12
-    acc[12] += X * W1;               // M13
-    acc[13] += X * E0;               // M14
-    acc[14] += Y * Y * W0;           // M22
-    acc[15] += Y * W1;               // M23
-    acc[16] += Y * E0;               // M24
-    acc[17] += W2;                   // M33
-    acc[18] += R * W1 + W3;          // M34
-    acc[19] += R * R * W0 + 2.0 * R * W2 + W4;  // M44
+    const dfl X = s_axd[i], Y = s_axd[kMaxAxis + j];
+    const dfl R = dfl_add(dfl_mul(X, X), dfl_mul(Y, Y));
+    const dfl d0 = dfl_norm(D0.hi, D0.lo), d1 = dfl_norm(D1.hi, D1.lo);
+    const dfl d2 = dfl_norm(D2.hi, D2.lo);
+    dacc_add(acc[0], d0);
+    dacc_fma(acc[1], d0, X);
+    dacc_fma(acc[2], d0, Y);
+    dacc_add(acc[3], d1);
+    dacc_add(acc[4], dfl_add(dfl_mul(R, d0), d2));
+    const float Xf = s_axf[i], Yf = s_axf[kMaxAxis + j];
+    const float Rf = Xf * Xf + Yf * Yf;
+    const float E0 = fmaf(Rf, W0, W2);  // sum w |c|^2
+    const float m[15] = {W0, Xf * W0, Yf * W0, W1, E0,                     // M00..M04
+                         Xf * Xf * W0, Xf * Yf * W0, Xf * W1, Xf * E0,     // M11..M14
+                         Yf * Yf * W0, Yf * W1, Yf * E0,                   // M22..M24
+                         W2, fmaf(Rf, W1, W3),                             // M33, M34
+                         fmaf(Rf * Rf, W0, fmaf(2.f * Rf, W2, W4))};       // M44
+#pragma unroll
+    for (int q = 0; q < 15; ++q) acc[5 + q].hi += m[q];
   }
-  block_sum<20>(acc, s_red);
+  double tot[20];
+  block_sum_dfl<20>(acc, s_red, tot);
   if (threadIdx.x == 0) {
     // Cholesky of M; no correction if M is not positive definite (e.g. no collisions
     // landed in this cell)
     double M[5][5], L[5][5] = {{0}}, y[5], lam[5];
     int m = 5;
     for (int r = 0; r < 5; ++r)
-      for (int c = r; c < 5; ++c) { M[r][c] = acc[m]; M[c][r] = acc[m]; ++m; }
+      for (int c = r; c < 5; ++c) { M[r][c] = tot[m]; M[c][r] = tot[m]; ++m; }
     bool ok = true;
     for (int r = 0; r < 5 && ok; ++r) {
       for (int c = 0; c <= r; ++c) {
@@ -1264,7 +1401,7 @@ __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
     }
     if (ok) {
       for (int r = 0; r < 5; ++r) {
-        double sum = acc[r];
+        double sum = tot[r];
         for (int k = 0; k < r; ++k) sum -= L[r][k] * y[k];
         y[r] = sum / L[r][r];
       }
@@ -1276,21 +1413,22 @@ __global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
     } else {
       for (int r = 0; r < 5; ++r) lam[r] = 0.0;
     }
-    for (int r = 0; r < 5; ++r) s_lam[r] = lam[r];
+    for (int r = 0; r < 5; ++r) s_lam[r] = static_cast<float>(lam[r]);
   }
   __syncthreads();
-  const double l0 = s_lam[0], l1 = s_lam[1], l2 = s_lam[2], l3 = s_lam[3], l4 = s_lam[4];
+  const float l0 = s_lam[0], l1 = s_lam[1], l2 = s_lam[2], l3 = s_lam[3], l4 = s_lam[4];
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
     const int j = col / NX, i = col - j * NX;
-    const double X = s_ax[i], Y = s_ax[kMaxAxis + j];
-    const double base = l0 + l1 * X + l2 * Y + l4 * (X * X + Y * Y);
+    const float X = s_axf[i], Y = s_axf[kMaxAxis + j];
+    const float base = fmaf(l4, X * X + Y * Y, fmaf(l2, Y, fmaf(l1, X, l0)));
+#pragma unroll 4
     for (int k = 0; k < NZ; ++k) {
       const int l = col + NXY * k;
-      const float dfl = df[l];
-      if (dfl == 0.f) continue;
-      const double d = static_cast<double>(dfl);
-      const double poly = base + l3 * s_z[k] + l4 * s_z[kMaxAxis + k];
-      f[l] += d - fabs(d) * poly;
+      const float d = df[l];
+      if (d == 0.f) continue;
+      const float poly = fmaf(l4, s_zf[kMaxAxis + k], fmaf(l3, s_zf[k], base));
+      const float corr = fabsf(d) * poly;
+      f[l] = (f[l] + dbl_from_float(d)) - dbl_from_float(corr);
       df[l] = 0.f;
     }
   }
@@ -1450,69 +1588,80 @@ __device__ __forceinline__ int axis_class(int i, int neg, int pos, int zero, int
   return kClsNone;
 }
 
-__global__ void __launch_bounds__(256) k_convect2d(Convect2DArgs a) {
-  // |dt/dx * xi_x| and |dt/dy * xi_y| per axis node
-  __shared__ double s_cx[kMaxAxis], s_cy[kMaxAxis];
+// The update f0 + ax (upx - f0) + ay (upy - f0) runs on the FP32 pipe in hi + lo pairs
+// (about 2^-46 relative per step) with one FP64 add to form the output. A thread owns one
+// (i, j) column of the cell's slab and walks it along k, so the upwind choice, the CFL
+// factors and the perimeter classification are worked out once per column.
+constexpr int kConvThreads = 128;
+
+__global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
   const GridInfo& g = a.g;
-  for (int t = threadIdx.x; t < g.nx; t += blockDim.x) s_cx[t] = fabs(a.xf * g.x[t]);
-  for (int t = threadIdx.x; t < g.ny; t += blockDim.x) s_cy[t] = fabs(a.yf * g.y[t]);
-  __syncthreads();
-  const int nv = g.nv;
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= nv) return;
+  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= NXY) return;
   const int cell = blockIdx.y;
   const int cx = cell % a.nxs, cy = cell / a.nxs;
-  const int NX = g.nx, NXY = g.nx * g.ny;
-  const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
-  (void)k;
-  const size_t off = static_cast<size_t>(cell) * nv + l;
-  const double f0 = a.f[off];
-  const double xv = g.x[i], yv = g.y[j];
-  const double ax = s_cx[i], ay = s_cy[j];
+  const int j = col / NX, i = col - j * NX;
+  const double* f0p = a.f + static_cast<size_t>(cell) * nv + col;
+  double* out = a.fconv + static_cast<size_t>(cell) * nv + col;
+  const size_t row = static_cast<size_t>(a.nxs) * nv;
   const bool perim = (cx == 0 || cy == 0 || cx == a.nxs - 1 || cy == a.nys - 1);
-  double out;
+  // upwind sources along x and y: a pointer to the column in the neighbour cell or a
+  // wall ghost, or none
+  const double* px = nullptr;
+  const double* py = nullptr;
+  bool hx = true, hy = true, zero = false;
   if (!perim) {
-    const double px = (xv < 0.0) ? a.f[off + nv] : a.f[off - nv];
-    const size_t row = static_cast<size_t>(a.nxs) * nv;
-    const double py = (yv < 0.0) ? a.f[off + row] : a.f[off - row];
-    // f0 + ax (px - f0) + ay (py - f0)
-    out = fma(ay, py - f0, fma(ax, px - f0, f0));
+    px = (g.x[i] < 0.0) ? f0p + nv : f0p - nv;
+    py = (g.y[j] < 0.0) ? f0p + row : f0p - row;
   } else {
     const int ci = axis_class(i, g.i_neg, g.i_pos, g.i_zero, g.i_zero_flag);
     const int cj = axis_class(j, g.j_neg, g.j_pos, g.j_zero, g.j_zero_flag);
     if (ci == kClsNone || cj == kClsNone) {
-      out = 0.0;
+      zero = true;
     } else {
-      double gx = 0.0, gy = 0.0;
       if (ci == kClsNeg) {  // upwind is the right neighbour / right wall ghost
-        if (cx < a.nxs - 1) gx = a.f[off + nv];
-        else if (a.bc_right == DVM_BC2D_WALL) gx = a.ghost[static_cast<size_t>(a.base[1] + cy) * nv + l];
-        else if (a.bc_right == DVM_BC2D_COUETTE) gx = a.f[static_cast<size_t>(a.nxs) * cy * nv + l];
+        if (cx < a.nxs - 1) px = f0p + nv;
+        else if (a.bc_right == DVM_BC2D_WALL) px = a.ghost + static_cast<size_t>(a.base[1] + cy) * nv + col;
+        else if (a.bc_right == DVM_BC2D_COUETTE) px = a.f + static_cast<size_t>(a.nxs) * cy * nv + col;
       } else if (ci == kClsPos) {  // left neighbour / left wall ghost
-        if (cx > 0) gx = a.f[off - nv];
-        else if (a.bc_left == DVM_BC2D_WALL) gx = a.ghost[static_cast<size_t>(a.base[0] + cy) * nv + l];
-        else if (a.bc_left == DVM_BC2D_COUETTE) gx = f0;
+        if (cx > 0) px = f0p - nv;
+        else if (a.bc_left == DVM_BC2D_WALL) px = a.ghost + static_cast<size_t>(a.base[0] + cy) * nv + col;
+        else if (a.bc_left == DVM_BC2D_COUETTE) px = f0p;
       }
       if (cj == kClsNeg) {  // top neighbour / top wall ghost
-        if (cy < a.nys - 1) gy = a.f[off + static_cast<size_t>(a.nxs) * nv];
-        else gy = a.ghost[static_cast<size_t>(a.base[3] + cx) * nv + l];
+        if (cy < a.nys - 1) py = f0p + row;
+        else py = a.ghost + static_cast<size_t>(a.base[3] + cx) * nv + col;
       } else if (cj == kClsPos) {  // bottom neighbour / bottom wall ghost
-        if (cy > 0) gy = a.f[off - static_cast<size_t>(a.nxs) * nv];
-        else gy = a.ghost[static_cast<size_t>(a.base[2] + cx) * nv + l];
+        if (cy > 0) py = f0p - row;
+        else py = a.ghost + static_cast<size_t>(a.base[2] + cx) * nv + col;
       }
-      const bool hx = (ci != kClsZero), hy = (cj != kClsZero);
-      if (hx && hy) out = fma(ay, gy - f0, fma(ax, gx - f0, f0));
-      else if (hy) out = fma(ay, gy - f0, f0);
-      else if (hx) out = fma(ax, gx - f0, f0);
-      else out = f0;
+      hx = (ci != kClsZero);
+      hy = (cj != kClsZero);
     }
   }
-  a.fconv[off] = out;
+  if (zero) {
+    for (int k = 0; k < NZ; ++k) out[static_cast<size_t>(NXY) * k] = 0.0;
+    return;
+  }
+  const float2 cxf = __ldg(a.cfl + i), cyf = __ldg(a.cfl + NX + j);
+  const dfl AX = dfl_make(cxf.x, cxf.y), AY = dfl_make(cyf.x, cyf.y);
+#pragma unroll 4
+  for (int k = 0; k < NZ; ++k) {
+    const size_t o = static_cast<size_t>(NXY) * k;
+    const dfl F0 = dfl_from_double(f0p[o]);
+    dfl acc = F0;
+    // a missing source (closed wall without ghost) contributes a zero value, as in the
+    // reference's zero-initialised neighbour
+    if (hx) acc = dfl_add(acc, dfl_mul(AX, dfl_sub(px ? dfl_from_double(px[o]) : dfl_make(0.f, 0.f), F0)));
+    if (hy) acc = dfl_add(acc, dfl_mul(AY, dfl_sub(py ? dfl_from_double(py[o]) : dfl_make(0.f, 0.f), F0)));
+    out[o] = dfl_to_double(acc);
+  }
 }
 
 cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s) {
-  dim3 grid((a.g.nv + 255) / 256, ncells);
-  k_convect2d<<<grid, 256, 0, s>>>(a);
+  dim3 grid((a.g.nx * a.g.ny + kConvThreads - 1) / kConvThreads, ncells);
+  k_convect2d<<<grid, kConvThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1654,7 +1803,7 @@ constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
 
 __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
-  __shared__ double s_red[kMomAcc * 32];
+  __shared__ float2 s_red[kMomAcc * 32];
   __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
   __shared__ dfl s_z[3 * kMaxAxis];   // z', z'^2, z'^3
   const GridInfo& g = a.g;
@@ -1691,6 +1840,7 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
     dacc G0, G1, G2, G3, S;
     dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
+#pragma unroll 4
     for (int k = 0; k < NZ; ++k) {
       const int l = col + NXY * k;
       const dfl fv = dfl_from_double(f[l]);
@@ -1724,9 +1874,7 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
     dacc_add(sacc[13], dfl_norm(S.hi, S.lo));
   }
   double acc[kMomAcc];
-#pragma unroll
-  for (int q = 0; q < kMomAcc; ++q) acc[q] = dacc_to_double(sacc[q]);
-  block_sum<kMomAcc>(acc, s_red);
+  block_sum_dfl<kMomAcc>(sacc, s_red, acc);
   if (threadIdx.x == 0) {
     // the previous moments, for the residual (only this thread writes P)
     const double n_old = P[DVM_P_DENS], t_old = P[DVM_P_TEMP];

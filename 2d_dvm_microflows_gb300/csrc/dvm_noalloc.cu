@@ -58,7 +58,7 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   L.eq_cache = o; o = align256(o + sizeof(double) * C * 4);
   L.cum_eq = o; o = align256(o + sizeof(double) * C * nv1);
   L.cum_dev = o; o = align256(o + sizeof(double) * C * nv1);
-  L.kin = o; o = align256(o + sizeof(double) * C * nv1);
+  L.kin = o; o = align256(o + sizeof(float) * C * nv1);
   L.ref_eq = o; o = align256(o + sizeof(int2) * C * kNRef);
   L.ref_dev = o; o = align256(o + sizeof(int2) * C * kNRef);
   L.plan = o; o = align256(o + sizeof(CellPlan) * C);
@@ -265,9 +265,9 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   ca.g = g; ca.cp = cp; ca.ncells = ncells; ca.f = f; ca.props = props;
   ca.eq_pre = reinterpret_cast<double*>(base + L.eq_pre);
   ca.eq_cache = d_eq_cache;
-  ca.cum_eq = reinterpret_cast<double*>(base + L.cum_eq);
-  ca.cum_dev = reinterpret_cast<double*>(base + L.cum_dev);
-  ca.kin = reinterpret_cast<double*>(base + L.kin);
+  ca.cum_eq = reinterpret_cast<long long*>(base + L.cum_eq);
+  ca.cum_dev = reinterpret_cast<long long*>(base + L.cum_dev);
+  ca.kin = reinterpret_cast<float*>(base + L.kin);
   ca.ref_eq = reinterpret_cast<int2*>(base + L.ref_eq);
   ca.ref_dev = reinterpret_cast<int2*>(base + L.ref_dev);
   ca.plan = reinterpret_cast<CellPlan*>(base + L.plan);

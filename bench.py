@@ -320,6 +320,26 @@ def run_forms(pkg, args, fp64_value):
     return out
 
 
+def one_step_error(pkg, cfg, g, f0, steps_before=3):
+    """The precision form's own error: from one FP64 state, one FP64 step and one FP32 step
+    with the same Philox words (hence the same partners), compared per moment field."""
+    import dataclasses
+    s = pkg.DVMSolver(dataclasses.replace(cfg, precision=pkg.DVM_PREC_FP64), g)
+    s.initialize_dist_func(f0)
+    s.solve(steps_before)
+    state = s.phi()
+    s.close()
+    out = []
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec), g)
+        s.initialize_dist_func(state)
+        s.ntime = steps_before
+        s.solve(1)
+        out.append(s.properties())
+        s.close()
+    return moment_error(out[1], out[0])
+
+
 def run_cavity(pkg, args):
     """Configuration 3 in the precision form and in FP64 from the same start and seed."""
     import dataclasses
@@ -334,7 +354,9 @@ def run_cavity(pkg, args):
         res[prec] = (rate, ms, s.properties(), s.collision_count())
         s.close()
     cells = cfg.nx_space * cfg.ny_space
+    one_step = one_step_error(pkg, cfg, g, f0)
     return {
+        "one_step_moment_err_fp32_vs_fp64": one_step,
         "workload": "2-D microcavity 64x64 cells, 24^3 on [-5,5], hard sphere, Kn=0.1, "
                     "diffuse walls T=1, lid u=0.3, samples from the reference formula "
                     "(ColnRMS 0.001), dt=0.0025",
@@ -406,6 +428,18 @@ def run_batch(pkg, args):
         b.close()
     out["moment_err_fp32_vs_fp64"] = moment_error(props["fp32_batched"], props["fp64_batched"])
     out["steps_compared"] = 2 * args.steps + args.warmup
+    one = []
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        b = pkg.DVMBatch(dataclasses.replace(cfg, precision=prec), grids, gid, samples)
+        for i, f in enumerate(f0):
+            b.upload_f(i, f)
+        b.step(1)
+        one.append(b.properties())
+        b.close()
+    out["one_step_moment_err_fp32_vs_fp64"] = moment_error(one[1], one[0])
+    out["note"] = ("moment_err_fp32_vs_fp64 compares two Monte Carlo realisations after "
+                   "steps_compared steps (they decorrelate); one_step_* isolates the FP32 "
+                   "rounding: one step of each form from the same state and Philox words")
     # plain FP64: one context per instance, stepped one after another
     solvers = []
     for i, f in enumerate(f0):
@@ -538,7 +572,7 @@ def run_serving(pkg, args):
                            "peak_bytes": stats["peak_bytes"], "budget_bytes": SERVE_BUDGET,
                            "statuses": sorted(set(i["status"] for i, _ in served))}}
     # plain FP64: one solve at a time, per-step residual check
-    finish, lat_p, colls_p, cells_p, err = 0.0, [], 0, 0, []
+    finish, lat_p, colls_p, cells_p, err, plain_props = 0.0, [], 0, 0, [], []
     first = reqs[0][0]
     for (t, cfg, g, f0, _), (info, props32) in zip(reqs, served):
         ts = time.perf_counter()
@@ -552,12 +586,22 @@ def run_serving(pkg, args):
             if s.residual() <= SERVE_TOL:
                 break
         props64 = s.properties()
+        plain_props.append(props64)
         s.close()
         service = time.perf_counter() - ts
         finish = max(finish, t) + service
         lat_p.append((finish - t) * 1e3)
         cells_p += cfg.nx_space * cfg.ny_space * steps
         err.append(moment_error(props32, props64))
+    # the yardstick for the served-vs-plain difference: plain FP64 against itself with
+    # other seeds (two independent realisations of each request)
+    spread = []
+    for (t, cfg, g, f0, _), (info, _) in zip(reqs, served):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, seed=cfg.seed + 7919), g)
+        s.initialize_dist_func(f0)
+        s.solve(info["steps"])
+        spread.append(moment_error(s.properties(), plain_props[len(spread)]))
+        s.close()
     span = finish - min(first, 0.0)
     out["plain_fp64"] = {"p50_ms": _pct(lat_p, 50), "p99_ms": _pct(lat_p, 99),
                          "collisions_per_s": colls_p / span, "cell_updates_per_s": cells_p / span,
@@ -566,6 +610,12 @@ def run_serving(pkg, args):
     out["moment_err_served_fp32_vs_plain_fp64"] = {
         "max": max(e["max"] for e in err),
         "per_field": {k: max(e["per_field"][k] for e in err) for k in fields}}
+    out["moment_err_plain_fp64_seed_to_seed"] = {
+        "max": max(e["max"] for e in spread),
+        "per_field": {k: max(e["per_field"][k] for e in spread) for k in fields}}
+    out["note"] = ("served FP32 and plain FP64 runs of a request are two Monte Carlo "
+                   "realisations; their difference is compared with the FP64 seed-to-seed "
+                   "difference of the same requests")
     out["speedup_collisions"] = (out["served_fp32"]["collisions_per_s"] /
                                  out["plain_fp64"]["collisions_per_s"])
     out["speedup_cell_updates"] = (out["served_fp32"]["cell_updates_per_s"] /

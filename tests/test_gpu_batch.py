@@ -57,27 +57,55 @@ def test_batch_matches_grouped_contexts(gpulib, pkg, prec):
             assert np.abs(pb[i, :17] - ps[c, :17]).max() <= ptol * max(1.0, np.abs(ps[c]).max())
 
 
-def test_batch_fp32_moments_within_bar(gpulib, pkg):
+def _batch_props(pkg, grids, gid, samples, f0, prec, seed, steps):
+    b = pkg.DVMBatch(_cfg(pkg, prec, seed=seed), grids, gid, samples)
+    for i, f in enumerate(f0):
+        b.upload_f(i, f)
+    b.step(steps)
+    p = b.properties()
+    b.close()
+    return p
+
+
+def _scale(p64):
+    n, T = p64[:, 0:1], p64[:, 4:5]
+    return np.concatenate([n, np.sqrt(T).repeat(3, 1), T.repeat(2, 1), np.sqrt(T),
+                           0.5 * n * T, (n * T ** 1.5).repeat(3, 1), (0.5 * n * T).repeat(6, 1)],
+                          axis=1)
+
+
+def test_batch_fp32_one_step_error(gpulib, pkg):
+    """The precision form's own error: one FP32 step and one FP64 step from the same state
+    and the same Philox words (so the same partners) differ only by FP32 rounding."""
     ph = pkg.physics
     grids = [ph.VelocityGrid.uniform(n, -5.0, 5.0) for n in (16, 24)]
     samples = [int(1e5 * (n / 24.0) ** 3) for n in (16, 24)]
     gid, f0 = _instances(ph, grids, 12, 2)
-    out = []
+    p64 = _batch_props(pkg, grids, gid, samples, f0, pkg.DVM_PREC_FP64, 11, 1)
+    p32 = _batch_props(pkg, grids, gid, samples, f0, pkg.DVM_PREC_FP32, 11, 1)
+    err = (np.abs(p32[:, :17] - p64[:, :17]) / _scale(p64)).max(0)
+    assert err.max() <= 1e-6, dict(zip(pkg.PROP_NAMES, err))
+    assert np.abs(p32[:, 0] - p64[:, 0]).max() <= 1e-12  # mass conserved by both
+
+
+def test_batch_fp32_ensemble_within_bar(gpulib, pkg):
+    """Over ten steps the FP32 and FP64 Monte Carlo realisations decorrelate, so the forms
+    are compared as ensembles over seeds: the mean moments agree within three standard
+    errors and within the 1e-3 bar."""
+    ph = pkg.physics
+    grids = [ph.VelocityGrid.uniform(n, -5.0, 5.0) for n in (16, 24)]
+    samples = [int(1e5 * (n / 24.0) ** 3) for n in (16, 24)]
+    gid, f0 = _instances(ph, grids, 12, 2)
+    runs = {}
     for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
-        b = pkg.DVMBatch(_cfg(pkg, prec, seed=11), grids, gid, samples)
-        for i, f in enumerate(f0):
-            b.upload_f(i, f)
-        b.step(10)
-        out.append(b.properties())
-    p64, p32 = out
-    n, T = p64[:, 0:1], p64[:, 4:5]
-    scale = np.concatenate([n, np.sqrt(T).repeat(3, 1), T.repeat(2, 1), np.sqrt(T),
-                            0.5 * n * T, (n * T ** 1.5).repeat(3, 1), (0.5 * n * T).repeat(6, 1)],
-                           axis=1)
-    err = (np.abs(p32[:, :17] - p64[:, :17]) / scale).max(0)
-    assert err.max() <= 1e-3, dict(zip(pkg.PROP_NAMES, err))
-    # mass conserved per instance by both forms
-    assert np.abs(p32[:, 0] - p64[:, 0]).max() <= 1e-12
+        runs[prec] = np.stack([_batch_props(pkg, grids, gid, samples, f0, prec, 100 + k, 10)
+                               for k in range(6)])
+    a, b = runs[pkg.DVM_PREC_FP32], runs[pkg.DVM_PREC_FP64]
+    sc = _scale(b.mean(0))
+    diff = np.abs(a.mean(0)[:, :17] - b.mean(0)[:, :17]) / sc
+    se = np.sqrt(a.var(0, ddof=1) / len(a) + b.var(0, ddof=1) / len(b))[:, :17] / sc
+    assert (diff <= 3.0 * se + 1e-12).mean() >= 0.95, (diff.max(), se.max())
+    assert diff.max() <= 1e-3, diff.max()
 
 
 def test_batch_rejects_bad_instances(gpulib, pkg):

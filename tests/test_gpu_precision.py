@@ -105,3 +105,21 @@ def test_fp32_pairlist_close_to_restatement(gpulib, pkg, oracle):
     cpu.compute_collision_integral(0, pkg.PairList(subs))
     d32, d64 = gpu.phi()[0] - f0, cpu.phi()[0] - f0
     assert np.abs(d32 - d64).max() <= 1e-4 * np.abs(d64).max()
+
+
+def test_cavity_fp32_one_step_error(gpulib, pkg):
+    """The precision form's own error on the cavity: one step of each form from the same
+    state with the same Philox words differs only by FP32 rounding (far below the bar)."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(12, -5.0, 5.0)
+    nxs = nys = 6
+    f0 = np.stack([ph.maxwellian(g, 1.0, 0.1 * (c % 3), 0.0, 0.0, 1.0 + 0.05 * (c % 5))
+                   for c in range(nxs * nys)])
+    walls = ((1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0), (1, 0.3, 0, 0, 1.0))
+    kw = dict(geometry=pkg.DVM_GEOM_2D, nx_space=nxs, ny_space=nys, dx=0.5, dy=0.5,
+              deltat=0.03, Kn=0.1, iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+              samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=20000, walls=walls, seed=5)
+    (p64, _, _), (p32, _, e32) = _pair(pkg, g, f0, 1, **kw)
+    err = moment_errors(p32, p64)
+    assert err.max() <= 1e-6, dict(zip(pkg.PROP_NAMES, err))
+    assert e32 == 0

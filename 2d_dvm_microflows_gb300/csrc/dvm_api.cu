@@ -740,7 +740,10 @@ int dvm_compute_convection(dvm_ctx* c) {
     std::memcpy(a.wall[1], c->p.wall[DVM_WALL_RIGHT], sizeof(a.wall[1]));
     a.f = c->d_f; a.fconv = c->d_fconv; a.err = c->d_err;
     st = launch(c, DVM_K_CONVECT, [&] { return launch_convect1d(a, c->stream); });
-    if (!st) st = launch(c, DVM_K_BC1D, [&] { return launch_bc1d(a, c->stream); });
+    const bool nodes = (a.bc[0] != DVM_BC1D_DIFFUSE) || (a.bc[1] != DVM_BC1D_DIFFUSE);
+    const bool diffuse = (a.bc[0] == DVM_BC1D_DIFFUSE) || (a.bc[1] == DVM_BC1D_DIFFUSE);
+    if (!st && nodes) st = launch(c, DVM_K_BC1D, [&] { return launch_bc1d_nodes(a, c->stream); });
+    if (!st && diffuse) st = launch(c, DVM_K_BC1D, [&] { return launch_bc1d(a, c->stream); });
   }
   if (!st) std::swap(c->d_f, c->d_fconv);  // perform_dist_func_update (phi <- phi_conv)
   return st;

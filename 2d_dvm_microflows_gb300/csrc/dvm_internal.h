@@ -189,7 +189,8 @@ cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_wall_specular(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s);
 cudaError_t launch_convect1d(const Convect1DArgs& a, cudaStream_t s);
-cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s);
+cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s);         // diffuse ends
+cudaError_t launch_bc1d_nodes(const Convect1DArgs& a, cudaStream_t s);   // the other ends
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s);
 cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s);
 int collide_blocks_per_sm(size_t smem);

@@ -479,11 +479,6 @@ struct SmemAxesD {
   int n[3];
 };
 
-struct StencilD {
-  int node[7];
-  dfl mass[7];
-};
-
 // Order-preserving key of a normalised pair (|lo| at most half an ulp of hi).
 __device__ __forceinline__ long long dkey(dfl a) {
   const uint32_t h = static_cast<uint32_t>(okeyf(a.hi));
@@ -562,10 +557,13 @@ __device__ __forceinline__ void axis_terms(const SmemAxesD& A, int ax, int o, in
   }
 }
 
-// compute_remapping_quantities (collisions/remapping.f90:92-394), f_off = 1, in pairs.
-__device__ __forceinline__ int remap_dfl(const GridInfo& g, const SmemAxesD& A, dfl u, dfl v,
-                                         dfl w, float xmin, float ymin, float zmin, float xfac,
-                                         float yfac, float zfac, StencilD& s) {
+// compute_remapping_quantities (collisions/remapping.f90:92-394), f_off = 1, in pairs,
+// with the replenishment scatter of the contribution w8 (apply_phi_replenishment,
+// replenishing_collisions.f90:356-434) into f.
+__device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAxesD& A, dfl u,
+                                                 dfl v, dfl w, float xmin, float ymin,
+                                                 float zmin, float xfac, float yfac, float zfac,
+                                                 double* f, dfl w8) {
   int corner = 0, bad = 0;
   int o_i = nearest_d(A, 0, u, xmin, xfac, corner, bad);
   int o_j = nearest_d(A, 1, v, ymin, yfac, corner, bad);
@@ -613,30 +611,42 @@ __device__ __forceinline__ int remap_dfl(const GridInfo& g, const SmemAxesD& A, 
     if (fz) den = dfl_add(den, t_z);
     f_e = dfl_div(num, den);
   }
-  const dfl f_ex = fx ? f_e : zero, f_ey = fy ? f_e : zero, f_ez = fz ? f_e : zero;
-  const dfl f_ix = dfl_mul(dfl_sub(a, dfl_mul(f_ex, ext_x)), inv_x);
-  const dfl f_iy = dfl_mul(dfl_sub(b, dfl_mul(f_ey, ext_y)), inv_y);
-  const dfl f_iz = dfl_mul(dfl_sub(c, dfl_mul(f_ez, ext_z)), inv_z);
-  const dfl sum = dfl_add(dfl_add(dfl_add(f_ix, f_iy), dfl_add(f_iz, f_ex)), dfl_add(f_ey, f_ez));
-  const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
+  if (bad & 2) return bad;
+  // weights and their contributions w * mass, scattered as they are formed (the centre
+  // node takes 1 - the others, as in the reference)
   const int NX = g.nx, NXY = g.nx * g.ny;
   const int base = o_i + NX * o_j + NXY * o_k;
-  s.node[0] = base;
-  s.node[1] = base + sa;
-  s.node[2] = base + NX * sb;
-  s.node[3] = base + NXY * sc;
-  s.node[4] = fx ? base - sa : -1;
-  s.node[5] = fy ? base - NX * sb : -1;
-  s.node[6] = fz ? base - NXY * sc : -1;
-  s.mass[0] = f_o; s.mass[1] = f_ix; s.mass[2] = f_iy; s.mass[3] = f_iz;
-  s.mass[4] = f_ex; s.mass[5] = f_ey; s.mass[6] = f_ez;
+  dfl sum = zero;
+  if (fx) {
+    atomicAdd(f + base - sa, dfl_to_double(dfl_mul(w8, f_e)));
+    sum = f_e;
+  }
+  if (fy) {
+    atomicAdd(f + base - NX * sb, dfl_to_double(dfl_mul(w8, f_e)));
+    sum = dfl_add(sum, f_e);
+  }
+  if (fz) {
+    atomicAdd(f + base - NXY * sc, dfl_to_double(dfl_mul(w8, f_e)));
+    sum = dfl_add(sum, f_e);
+  }
+  {
+    const dfl f_ix = dfl_mul(dfl_sub(a, fx ? dfl_mul(f_e, ext_x) : zero), inv_x);
+    atomicAdd(f + base + sa, dfl_to_double(dfl_mul(w8, f_ix)));
+    sum = dfl_add(sum, f_ix);
+  }
+  {
+    const dfl f_iy = dfl_mul(dfl_sub(b, fy ? dfl_mul(f_e, ext_y) : zero), inv_y);
+    atomicAdd(f + base + NX * sb, dfl_to_double(dfl_mul(w8, f_iy)));
+    sum = dfl_add(sum, f_iy);
+  }
+  {
+    const dfl f_iz = dfl_mul(dfl_sub(c, fz ? dfl_mul(f_e, ext_z) : zero), inv_z);
+    atomicAdd(f + base + NXY * sc, dfl_to_double(dfl_mul(w8, f_iz)));
+    sum = dfl_add(sum, f_iz);
+  }
+  const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
+  atomicAdd(f + base, dfl_to_double(dfl_mul(w8, f_o)));
   return bad;
-}
-
-__device__ __forceinline__ void scatter_d(double* f, const StencilD& s, dfl w) {
-#pragma unroll
-  for (int q = 0; q < 7; ++q)
-    if (s.node[q] >= 0) atomicAdd(f + s.node[q], dfl_to_double(dfl_mul(w, s.mass[q])));
 }
 
 // t = R - k/kTrigN (k = the top 10 bits of R) as a pair, and k, from the bits of R in [0, 1).
@@ -673,7 +683,7 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   return L;
 }
 
-__global__ void __launch_bounds__(kCollideChunk, 3) k_collide(CollideArgs a) {
+__global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
   const CollideSmem L = collide_smem_layout(g, a.t);
@@ -885,14 +895,13 @@ __global__ void __launch_bounds__(kCollideChunk, 3) k_collide(CollideArgs a) {
         uy = dfl_mul(hs, sphi);
         uz = dfl_mul(hg, ct);
       }
-      StencilD sd;
-      int rb = remap_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz), xmin, ymin,
-                         zmin, xfac, yfac, zfac, sd);
-      if (rb & 2) bad |= DVM_EW_REMAP; else scatter_d(f, sd, kr);
+      int rb = remap_scatter_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
+                                 xmin, ymin, zmin, xfac, yfac, zfac, f, kr);
+      if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_dfl(g, A, dfl_sub(vc0, ux), dfl_sub(vc1, uy), dfl_sub(vc2, uz), xmin, ymin, zmin,
-                     xfac, yfac, zfac, sd);
-      if (rb & 2) bad |= DVM_EW_REMAP; else scatter_d(f, sd, kr);
+      rb = remap_scatter_dfl(g, A, dfl_sub(vc0, ux), dfl_sub(vc1, uy), dfl_sub(vc2, uz), xmin,
+                             ymin, zmin, xfac, yfac, zfac, f, kr);
+      if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
   }
@@ -1086,7 +1095,7 @@ __host__ __device__ inline CollideSmemF collide_f32_smem_layout(const GridInfo& 
   return L;
 }
 
-__global__ void __launch_bounds__(kCollideChunk) k_collide_f32(CollideArgs a, CollTablesF tf,
+__global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a, CollTablesF tf,
                                                                 float* __restrict__ dfs) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
@@ -1690,7 +1699,44 @@ cudaError_t launch_convect1d(const Convect1DArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// End conditions (grid_ref conditions/boundary_conditions.f90:319-1000); one CTA per end.
+// End conditions (grid_ref conditions/boundary_conditions.f90:319-1000). The node-local
+// ones (specular, inflow Maxwellian, zero gradient) run one thread per node over both
+// ends (blockIdx.y = end); the diffuse wall, which needs the incoming and outgoing flux
+// sums of its end first, runs one CTA per end.
+__global__ void __launch_bounds__(256) k_bc1d_nodes(Convect1DArgs a) {
+  const GridInfo& g = a.g;
+  const int e = blockIdx.y;  // 0 left, 1 right
+  const int bc = a.bc[e];
+  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nv) return;
+  const int nx = (e == 0) ? 0 : a.nxs - 1;
+  const double* f = a.f + static_cast<size_t>(nx) * nv;
+  double* fc = a.fconv + static_cast<size_t>(nx) * nv;
+  const double* W = a.wall[e];
+  if (bc == DVM_BC1D_SPECULAR) {  // apply_specular_wall :446-564
+    const double xv = g.x[l % NX];
+    const double fac = a.factor * xv;
+    if (e == 0 && xv < 0.0) fc[l] = f[l] - fac * (f[l + nv] - f[l]);
+    if (e == 1 && xv > 0.0) fc[l] = f[l] - fac * (f[l] - f[l - nv]);
+  } else if (bc == DVM_BC1D_INOUT) {  // apply_fixed_in_out_flow :783-913
+    const double dens = W[DVM_WP_DENS], T = W[DVM_WP_TEMP], u = W[DVM_WP_U];
+    const double mc = dens * maxwell_coeff(a.mass, T, a.pi);
+    const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
+    const double b3 = g.bx[i] * g.by[j] * g.bz[k];
+    fc[l] = maxwellian(g.x[i], g.y[j], g.z[k], mc, a.mass, u, 0.0, 0.0, T) * b3;
+  } else if (bc == DVM_BC1D_ZEROGRAD) {  // apply_zero_gradient_flow :915-962
+    const double* src = a.fconv + static_cast<size_t>(e == 0 ? 1 : a.nxs - 2) * nv;
+    fc[l] = src[l];
+  }
+}
+
+cudaError_t launch_bc1d_nodes(const Convect1DArgs& a, cudaStream_t s) {
+  dim3 grid((a.g.nv + 255) / 256, 2);
+  k_bc1d_nodes<<<grid, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 constexpr int kBc1dThreads = 1024;
 
 __global__ void __launch_bounds__(kBc1dThreads) k_bc1d(Convect1DArgs a) {
@@ -1703,25 +1749,7 @@ __global__ void __launch_bounds__(kBc1dThreads) k_bc1d(Convect1DArgs a) {
   const double* f = a.f + static_cast<size_t>(nx) * nv;
   double* fc = a.fconv + static_cast<size_t>(nx) * nv;
   const double* W = a.wall[e];
-  if (bc == DVM_BC1D_SPECULAR) {  // apply_specular_wall :446-564
-    for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-      const double xv = g.x[l % NX];
-      const double fac = a.factor * xv;
-      if (e == 0 && xv < 0.0) fc[l] = f[l] - fac * (f[l + nv] - f[l]);
-      if (e == 1 && xv > 0.0) fc[l] = f[l] - fac * (f[l] - f[l - nv]);
-    }
-  } else if (bc == DVM_BC1D_INOUT) {  // apply_fixed_in_out_flow :783-913
-    const double dens = W[DVM_WP_DENS], T = W[DVM_WP_TEMP], u = W[DVM_WP_U];
-    const double mc = dens * maxwell_coeff(a.mass, T, a.pi);
-    for (int l = threadIdx.x; l < nv; l += blockDim.x) {
-      const int k = l / NXY, j = (l - k * NXY) / NX, i = l - k * NXY - j * NX;
-      const double b3 = g.bx[i] * g.by[j] * g.bz[k];
-      fc[l] = maxwellian(g.x[i], g.y[j], g.z[k], mc, a.mass, u, 0.0, 0.0, T) * b3;
-    }
-  } else if (bc == DVM_BC1D_ZEROGRAD) {  // apply_zero_gradient_flow :915-962
-    const double* src = a.fconv + static_cast<size_t>(e == 0 ? 1 : a.nxs - 2) * nv;
-    for (int l = threadIdx.x; l < nv; l += blockDim.x) fc[l] = src[l];
-  } else if (bc == DVM_BC1D_DIFFUSE) {  // apply_diffuse_reflection :566-781
+  if (bc == DVM_BC1D_DIFFUSE) {  // apply_diffuse_reflection :566-781
     const double T = W[DVM_WP_TEMP], u = W[DVM_WP_U], v = W[DVM_WP_V], w = W[DVM_WP_W];
     const double* f2 = a.f + static_cast<size_t>(e == 0 ? 1 : a.nxs - 2) * nv;
     const double mc = maxwell_coeff(a.mass, T, a.pi);

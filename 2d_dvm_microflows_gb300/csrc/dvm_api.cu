@@ -29,7 +29,7 @@ struct dvm_ctx {
   std::vector<double> hx, hy, hz, hbx, hby, hbz;
   // device buffers
   double* d_axes = nullptr;   // x, y, z, bx, by, bz
-  double* d_speed = nullptr;  // |xi| per node
+  float2* d_speed = nullptr;  // |xi| per node as a hi + lo float pair
   double* d_f = nullptr;
   double* d_fconv = nullptr;
   double* d_props = nullptr;
@@ -508,7 +508,12 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
       release(c);
       return st;
     }
-    h2d(c, c->d_speed, sp.data(), nv * sizeof(double));
+    std::vector<float2> sp2(nv);
+    for (size_t l = 0; l < nv; ++l) {
+      const float h = static_cast<float>(sp[l]);
+      sp2[l] = make_float2(h, static_cast<float>(sp[l] - static_cast<double>(h)));
+    }
+    h2d(c, c->d_speed, sp2.data(), nv * sizeof(float2));
     g.speed = c->d_speed;
     cudaStreamSynchronize(c->stream);
   }
@@ -669,7 +674,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
   if (!st) {
     CdfArgs ca{};
     ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
-    ca.f = c->d_f; ca.props = c->d_props; ca.eq_pre = c->d_eq_pre; ca.eq_cache = c->d_eq_cache;
+    ca.f = c->d_f; ca.props = c->d_props; ca.eq_pre = reinterpret_cast<long long*>(c->d_eq_pre); ca.eq_cache = c->d_eq_cache;
     ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
     ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan;
     ca.pairs = pd; ca.err = c->d_err;
@@ -980,7 +985,7 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
   const size_t d = sizeof(double);
   size_t b = 2 * (vg->nx + vg->ny + vg->nz) * d            // axes
              + 2 * C * nv * d + C * DVM_NPROP * d           // f, f_conv, properties
-             + sizeof(uint32_t) + nv * d                    // error word, speeds
+             + sizeof(uint32_t) + nv * sizeof(float2)       // error word, speeds
              + sizeof(unsigned long long);                  // residual
   if (p->coll_method != DVM_COLL_NONE) {
     b += 3 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float) + C * 4 * d;  // eq_pre, cum_eq,

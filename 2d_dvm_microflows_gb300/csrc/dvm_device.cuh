@@ -34,7 +34,7 @@ struct GridInfo {
   const double* bx;
   const double* by;
   const double* bz;
-  const double* speed;  // |xi| per node (moments); may be null where unused
+  const float2* speed;  // |xi| per node as a hi + lo pair (moments); may be null where unused
 };
 
 // ----------------------------------------------------------------------------------------

@@ -48,7 +48,7 @@ struct CdfArgs {
   int ncells;
   const double* f;          // [C][nv]
   const double* props;      // [C][DVM_NPROP]
-  double* eq_pre;           // [C][nv+1] cached equilibrium, one value per node
+  long long* eq_pre;        // [C][nv+1] cached equilibrium, fixed point, one value per node
   double* eq_cache;         // [C][4]  dens, u, v, temp of the cached equilibrium
   long long* cum_eq;        // [C][nv+1] cumulative f_eq, fixed point (see k_cdf)
   long long* cum_dev;       // [C][nv+1] cumulative |f - f_eq| (FMC: |f|), fixed point

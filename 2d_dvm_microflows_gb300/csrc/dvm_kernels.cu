@@ -30,9 +30,11 @@ namespace dvm {
 // independent of the order of summation, so the parallel scan gives the sequential sum
 // bit for bit; the quantum 2^-k is below 1e-17 n, finer than the FP64 rounding of the
 // reference's running sum. The partner search (k_collide) then compares integers only.
-constexpr int kCdfThreads = 512;
+constexpr int kCdfThreads = 256;
 constexpr int kCdfPer = 8;
-constexpr int kCdfCoarseMax = 2048;  // entries of the shared-memory coarse index per table
+constexpr int kCdfChunk = kCdfThreads * kCdfPer;  // nodes per scan chunk
+constexpr int kCdfPitch = kCdfPer + 1;            // padded per-thread row in shared memory
+constexpr int kCdfCoarseMax = 1024;  // entries of the shared-memory coarse index per table
 
 __device__ long long num_coll_pairs(const CollParams& cp, double beta3_min, double densA,
                                     double densB, double temp) {
@@ -63,6 +65,31 @@ __device__ __forceinline__ long long to_fixed(double x, int k, uint32_t& bad) {
   }
   if (sh <= -64) return 0;
   return static_cast<long long>(mant >> (-sh));
+}
+
+// x 2^k truncated towards zero, signed, for a double x (bit operations only).
+__device__ __forceinline__ long long to_fixed_s(double x, int k, uint32_t& bad) {
+  const unsigned long long sb = static_cast<unsigned long long>(__double_as_longlong(x));
+  const long long v = to_fixed(x, k, bad);  // |x| 2^k
+  return (sb >> 63) ? -v : v;
+}
+
+// v 2^k truncated towards zero, signed, for a float v (bit operations only).
+__device__ __forceinline__ long long to_fixed_f(float v, int k, uint32_t& bad) {
+  const uint32_t b = static_cast<uint32_t>(__float_as_int(v));
+  const int e = static_cast<int>((b >> 23) & 0xffu);
+  if (e == 0) return 0;  // zero or FP32 subnormal (below 1.2e-38)
+  if (e == 255) { bad |= DVM_EW_NONFINITE; return 0; }
+  const unsigned long long m = (b & 0x7fffffu) | 0x800000u;
+  const int sh = e - 150 + k;
+  unsigned long long r;
+  if (sh >= 0) {
+    if (sh > 38) { bad |= DVM_EW_NONFINITE; return 0; }
+    r = m << sh;
+  } else {
+    r = (sh <= -64) ? 0ull : (m >> (-sh));
+  }
+  return (b >> 31) ? -static_cast<long long>(r) : static_cast<long long>(r);
 }
 
 // Sign of v as +-1.0f (the collision kernels read only the sign bit of kin).
@@ -105,11 +132,17 @@ __device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long
 }
 
 __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
+  // chunk staging: node m of a chunk sits at (m / kCdfPer) * kCdfPitch + m % kCdfPer, so
+  // global memory is read and written in coalesced rows while each thread scans
+  // kCdfPer consecutive nodes
+  extern __shared__ long long s_stage[];  // 2 * kCdfThreads * kCdfPitch
+  long long* s_e = s_stage;
+  long long* s_d = s_stage + kCdfThreads * kCdfPitch;
   __shared__ long long s_scan[2][128];
   __shared__ double s_par[6];
-  __shared__ int s_new, s_k;
+  __shared__ int s_new, s_k, s_ke;
   __shared__ int s_right[2][kNRef];
-  __shared__ double s_fac[3 * kMaxAxis];
+  __shared__ dfl s_fac[3 * kMaxAxis];
   __shared__ long long s_coarse[2][kCdfCoarseMax + 1];
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
@@ -117,7 +150,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
   const double* f = a.f + static_cast<size_t>(cell) * nv;
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
-  double* eq = a.eq_pre + cs;  // cached equilibrium, one value per node
+  long long* eq = a.eq_pre + cs;  // cached equilibrium, fixed point, one value per node
   long long* ce = a.cum_eq + cs;
   long long* cd = a.cum_dev + cs;
   float* kin = a.kin + cs;
@@ -129,11 +162,13 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   const int ncoarse = nv / cstep;  // entries 0..ncoarse
 
   if (threadIdx.x == 0) {
-    // fixed-point scale from the cell density: 16 n 2^k <= 2^62
-    const double n0 = P[DVM_P_DENS];
-    int E = 1;
-    if (n0 > 0.0 && isfinite(n0)) E = ilogb(n0) + 1;  // n0 < 2^E
-    s_k = 58 - E;
+    // fixed-point scale from a density: 16 n 2^k <= 2^62
+    auto scale = [](double n0) {
+      int E = 1;
+      if (n0 > 0.0 && isfinite(n0)) E = ilogb(n0) + 1;  // n0 < 2^E
+      return 58 - E;
+    };
+    s_k = scale(P[DVM_P_DENS]);
     s_new = 0;
     if (vr) {
       const double dens = P[DVM_P_DENS], u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
@@ -147,6 +182,9 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
                       fabs(v - cache[2]) > tol * v || fabs(temp - cache[3]) > tol * temp);
       if (nw) { cache[0] = dens; cache[1] = u; cache[2] = v; cache[3] = temp; }
       s_new = nw;
+      // the equilibrium CDF keeps the scale of the density it was built for, so a cached
+      // one stays valid (with its bucket table) until the cache is renewed
+      s_ke = scale(cache[0]);
       s_par[0] = mc; s_par[1] = u; s_par[2] = v; s_par[3] = w; s_par[4] = temp;
     }
   }
@@ -171,50 +209,83 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
           val = exp(-(c * c) * m / temp) * g.bz[t - g.nx - g.ny];
         }
       }
+      const dfl v = dfl_from_double(val);
       s_fac[t < g.nx ? t : (t < g.nx + g.ny ? kMaxAxis + t - g.nx
-                                              : 2 * kMaxAxis + t - g.nx - g.ny)] = val;
+                                              : 2 * kMaxAxis + t - g.nx - g.ny)] =
+          dfl_norm(v.hi, v.lo);
     }
     __syncthreads();
   }
-  const int k = s_k;
+  const int k = s_k, ke = s_ke;
   uint32_t bad = 0;
   // deviation and CDFs: each thread takes kCdfPer consecutive nodes of a chunk, scans them
   // in sequence, and the thread sums are scanned across the block (cumul_df of
   // variance_reduction.f90:454-456, full_mc.f90:151-152)
+  // The node terms are formed without FP64 instructions: f enters the fixed point from
+  // its bits, f_eq = e_x e_y e_z is a pair product converted once (and cached in fixed
+  // point), and f - f_eq and its magnitude are integer operations. For VR every term
+  // uses the scale of the cached equilibrium's density (the cache is renewed whenever
+  // the density moves by more than cdf_tolerance, well inside the scale's 16x margin).
+  const int kc = vr ? ke : k;
+  // (i, j, k) steps of a row of kCdfThreads nodes
+  const int NY = g.ny;
+  const int st_i = kCdfThreads % NX, st_j = (kCdfThreads / NX) % NY, st_k = kCdfThreads / NXY;
   long long carry_e = 0, carry_d = 0;
-  for (int base = 0; base < nv; base += kCdfThreads * kCdfPer) {
-    const int l0 = base + threadIdx.x * kCdfPer;
-    long long pe[kCdfPer], ad[kCdfPer];
-#pragma unroll
-    for (int q = 0; q < kCdfPer; ++q) {
-      const int l = l0 + q;
-      pe[q] = 0;
-      ad[q] = 0;
-      if (l < nv) {
-        if (vr) {
-          double ev;
-          if (recompute) {
-            const int kk = l / NXY, j = (l - kk * NXY) / NX, i = l - kk * NXY - j * NX;
-            ev = s_fac[i] * s_fac[kMaxAxis + j] * s_fac[2 * kMaxAxis + kk];
-            eq[l] = ev;
-          } else {
-            ev = eq[l];
-          }
-          const double pn = f[l] - ev;
-          kin[l + 1] = sign_float(pn);
-          pe[q] = to_fixed(ev, k, bad);
-          ad[q] = to_fixed(pn, k, bad);  // |pn| (the sign bit is dropped)
-        } else {
+  for (int base = 0; base < nv; base += kCdfChunk) {
+    // 1. node terms in coalesced rows: f and f_eq to fixed point, kin, the cached f_eq
+    {
+      int ii = 0, jj = 0, kk = 0;
+      if (recompute) {
+        const int l0 = base + threadIdx.x;
+        kk = l0 / NXY;
+        jj = (l0 - kk * NXY) / NX;
+        ii = l0 - kk * NXY - jj * NX;
+      }
+#pragma unroll 4
+      for (int r = 0; r < kCdfPer; ++r) {
+        const int m = threadIdx.x + r * kCdfThreads;
+        const int l = base + m;
+        long long te = 0, td = 0;
+        if (l < nv) {
           const double fv = f[l];
-          kin[l + 1] = sign_float(fv);
-          ad[q] = to_fixed(fv, k, bad);
+          const long long F = to_fixed_s(fv, kc, bad);
+          if (vr) {
+            long long E;
+            if (recompute) {
+              const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
+                                     s_fac[2 * kMaxAxis + kk]);
+              E = to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
+              eq[l] = E;
+              te = E;
+            } else {
+              E = eq[l];
+            }
+            const long long d = F - E;
+            kin[l + 1] = d < 0 ? -1.f : 1.f;
+            td = d < 0 ? -d : d;
+          } else {
+            kin[l + 1] = sign_float(fv);
+            td = F < 0 ? -F : F;
+          }
+        }
+        const int pos = (m / kCdfPer) * kCdfPitch + (m % kCdfPer);
+        s_e[pos] = te;
+        s_d[pos] = td;
+        if (recompute) {
+          ii += st_i; if (ii >= NX) { ii -= NX; ++jj; }
+          jj += st_j; if (jj >= NY) { jj -= NY; ++kk; }
+          kk += st_k;
         }
       }
     }
+    __syncthreads();
+    // 2. each thread scans its kCdfPer consecutive nodes, the block scans the thread sums
+    long long pe[kCdfPer], ad[kCdfPer];
+    const int row = threadIdx.x * kCdfPitch;
 #pragma unroll
-    for (int q = 1; q < kCdfPer; ++q) {
-      pe[q] += pe[q - 1];
-      ad[q] += ad[q - 1];
+    for (int q = 0; q < kCdfPer; ++q) {
+      pe[q] = s_e[row + q] + (q ? pe[q - 1] : 0);
+      ad[q] = s_d[row + q] + (q ? ad[q - 1] : 0);
     }
     long long oe = pe[kCdfPer - 1], od = ad[kCdfPer - 1], te, td;
     block_scan2_i64(oe, od, te, td, &s_scan[0][0]);
@@ -222,10 +293,19 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
     od += carry_d;
 #pragma unroll
     for (int q = 0; q < kCdfPer; ++q) {
-      const int p = l0 + q + 1;  // position in the cumulative arrays
+      s_e[row + q] = oe + pe[q];
+      s_d[row + q] = od + ad[q];
+    }
+    __syncthreads();
+    // 3. coalesced stores of the cumulative sums (position p = node + 1) and the coarse index
+#pragma unroll 4
+    for (int r = 0; r < kCdfPer; ++r) {
+      const int m = threadIdx.x + r * kCdfThreads;
+      const int p = base + m + 1;
       if (p <= nv) {
-        const long long ve = oe + pe[q], vd = od + ad[q];
-        if (vr) ce[p] = ve;
+        const int pos = (m / kCdfPer) * kCdfPitch + (m % kCdfPer);
+        const long long ve = s_e[pos], vd = s_d[pos];
+        if (recompute) ce[p] = ve;
         cd[p] = vd;
         if ((p & (cstep - 1)) == 0) {
           s_coarse[0][p / cstep] = ve;
@@ -235,10 +315,11 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
     }
     carry_e += te;
     carry_d += td;
-    __syncthreads();  // s_scan is reused by the next chunk
+    __syncthreads();  // s_e, s_d and s_scan are reused by the next chunk
   }
   if (threadIdx.x == 0) {
-    ce[0] = 0; cd[0] = 0; kin[0] = 0.f;
+    if (recompute) ce[0] = 0;
+    cd[0] = 0; kin[0] = 0.f;
     s_coarse[0][0] = 0;
     s_coarse[1][0] = 0;
     if (carry_e < 0 || carry_d < 0) bad |= DVM_EW_NONFINITE;  // the scale did not hold
@@ -251,6 +332,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   // index narrows each lookup to cstep entries.
   const int ntab = vr ? 2 : 1;
   for (int t = 0; t < ntab; ++t) {
+    if (vr && t == 0 && !recompute) continue;  // cached equilibrium: table unchanged
     const int ti = (vr && t == 0) ? 0 : 1;
     const long long* cum = (ti == 0) ? ce : cd;
     const long long T = (ti == 0) ? carry_e : carry_d;
@@ -275,6 +357,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   }
   __syncthreads();
   for (int t = 0; t < ntab; ++t) {
+    if (vr && t == 0 && !recompute) continue;
     int2* ref = ((vr && t == 0) ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef;
     for (int r = threadIdx.x + 1; r <= kNRef; r += kCdfThreads) {
       int2 e;
@@ -292,8 +375,9 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
     const double qk = ldexp(1.0, -k);
     if (vr) {
       const double dens = P[DVM_P_DENS], temp = P[DVM_P_SPECIES_TEMP];
-      const double eq_dens = static_cast<double>(carry_e) * qk;
-      const double neq_dens = static_cast<double>(carry_d) * qk;
+      const long long te = recompute ? carry_e : ce[nv];
+      const double eq_dens = static_cast<double>(te) * ldexp(1.0, -ke);
+      const double neq_dens = static_cast<double>(carry_d) * ldexp(1.0, -ke);
       const double fc = cp.dt * 0.5 / cp.Kn;  // n = m: factor_coeff = dt*0.5/Kn
       const double r = 0.5 * neq_dens / dens;
       const double dA[3] = {1.0, r, r}, dB[3] = {r, 1.0, r};
@@ -345,7 +429,10 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
 }
 
 cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
-  k_cdf<<<a.ncells, kCdfThreads, 0, s>>>(a);
+  constexpr int smem = 2 * kCdfThreads * kCdfPitch * static_cast<int>(sizeof(long long));
+  const cudaError_t e = cudaFuncSetAttribute(k_cdf, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_cdf<<<a.ncells, kCdfThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1307,7 +1394,7 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
 // reason, and f + df - w * poly is formed in FP64 from the exact doubles of the two floats.
 constexpr int kProjThreads = 256;
 
-__global__ void __launch_bounds__(kProjThreads) k_project(ProjectArgs a) {
+__global__ void __launch_bounds__(kProjThreads, 3) k_project(ProjectArgs a) {
   __shared__ float2 s_red[20 * 32];
   __shared__ float s_lam[5];
   __shared__ dfl s_axd[2 * kMaxAxis];  // x', y' as pairs
@@ -1830,7 +1917,7 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
 
-__global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
+__global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
   __shared__ float2 s_red[kMomAcc * 32];
   __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
   __shared__ dfl s_z[3 * kMaxAxis];   // z', z'^2, z'^3
@@ -1864,7 +1951,7 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
   dacc sacc[kMomAcc];
 #pragma unroll
   for (int q = 0; q < kMomAcc; ++q) dacc_zero(sacc[q]);
-  const double* speed = g.speed;
+  const float2* speed = g.speed;
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
     dacc G0, G1, G2, G3, S;
     dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
@@ -1876,7 +1963,8 @@ __global__ void __launch_bounds__(kMomThreads) k_moments(MomentArgs a) {
       dacc_fma(G1, fv, s_z[k]);
       dacc_fma(G2, fv, s_z[kMaxAxis + k]);
       dacc_fma(G3, fv, s_z[2 * kMaxAxis + k]);
-      dacc_fma(S, fv, dfl_from_double(__ldg(speed + l)));
+      const float2 sp = __ldg(speed + l);
+      dacc_fma(S, fv, dfl_make(sp.x, sp.y));
     }
     const int j = col / NX, i = col - j * NX;
     const dfl X = s_ax[i], X2 = s_ax[kMaxAxis + i];

@@ -263,7 +263,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
 
   CdfArgs ca{};
   ca.g = g; ca.cp = cp; ca.ncells = ncells; ca.f = f; ca.props = props;
-  ca.eq_pre = reinterpret_cast<double*>(base + L.eq_pre);
+  ca.eq_pre = reinterpret_cast<long long*>(base + L.eq_pre);
   ca.eq_cache = d_eq_cache;
   ca.cum_eq = reinterpret_cast<long long*>(base + L.cum_eq);
   ca.cum_dev = reinterpret_cast<long long*>(base + L.cum_dev);

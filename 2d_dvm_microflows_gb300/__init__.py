@@ -237,6 +237,24 @@ class DVMSolver:
     def synchronize(self):
         _check(self.lib.dvm_synchronize(self.ctx), "dvm_synchronize")
 
+    def checkpoint(self):
+        """The context's state as bytes (restart.f90's ntime + phi, plus the cached
+        equilibrium the next step may reuse)."""
+        n = C.c_uint64()
+        _check(self.lib.dvm_checkpoint_size(self.ctx, C.byref(n)), "dvm_checkpoint_size")
+        buf = C.create_string_buffer(n.value)
+        _check(self.lib.dvm_checkpoint_save(self.ctx, C.c_uint64(self.ntime), buf, n.value),
+               "dvm_checkpoint_save")
+        return buf.raw
+
+    def restore(self, data):
+        """Loads a checkpoint of a context of the same shape; the run continues from it."""
+        buf = C.create_string_buffer(bytes(data), len(data))
+        nt = C.c_uint64()
+        _check(self.lib.dvm_checkpoint_load(self.ctx, buf, len(data), C.byref(nt)),
+               "dvm_checkpoint_load")
+        self.ntime = nt.value
+
     def residual(self):
         """Largest relative change of the moments in the last step (dvm_get_residual)."""
         v = C.c_double()
@@ -409,3 +427,36 @@ class DVMServer:
         _check(self.lib.dvm_server_stats(self.sv, C.byref(n), C.byref(a), C.byref(b)),
                "dvm_server_stats")
         return {"completed": n.value, "peak_active": a.value, "peak_bytes": b.value}
+
+
+# Tecplot output of the moments, in the layout of write_properties
+# (input_output/visualization.f90:620-660, 1591-1660): a title, a variables line, and per
+# output time a zone of rows "time x y <properties>", cells ordered x outer, y inner.
+TECPLOT_FIELDS = (("Density", DVM_P_DENS), ("X-Velocity", DVM_P_U), ("Y-Velocity", DVM_P_V),
+                  ("Z-Velocity", DVM_P_W), ("Temperature", DVM_P_TEMP),
+                  ("Avg Speed", DVM_P_AVG_SPEED), ("Pressure", DVM_P_PRESSURE),
+                  ("Heat Flux X", DVM_P_QX), ("Heat Flux Y", DVM_P_QY),
+                  ("Heat Flux Z", DVM_P_QZ))
+TECPLOT_STRESS = (("xx", DVM_P_TXX), ("yy", DVM_P_TYY), ("zz", DVM_P_TZZ), ("xy", DVM_P_TXY),
+                  ("xz", DVM_P_TXZ), ("yz", DVM_P_TYZ))
+
+
+def write_properties_header(path):
+    names = ['"Time"', '"x-Location"', '"y-Location"'] + ['"%s"' % n for n, _ in TECPLOT_FIELDS]
+    names += ['"Tau %s"' % n for n, _ in TECPLOT_STRESS]
+    with open(path, "w") as fh:
+        fh.write('title = "Macroscopic Properties"\n')
+        fh.write("variables = " + ", ".join(names) + "\n")
+
+
+def append_properties(path, time, props, nx_space, ny_space, dx, dy):
+    """One output time: props[cells, DVM_NPROP] with cell = cx + nx_space * cy."""
+    props = np.asarray(props).reshape(nx_space * ny_space, DVM_NPROP)
+    cols = [q for _, q in TECPLOT_FIELDS] + [q for _, q in TECPLOT_STRESS]
+    with open(path, "a") as fh:
+        fh.write("zone i=%5d\n" % (nx_space * ny_space))
+        for cx in range(nx_space):
+            for cy in range(ny_space):
+                p = props[cx + nx_space * cy]
+                row = [time, (cx + 0.5) * dx, (cy + 0.5) * dy] + [p[q] for q in cols]
+                fh.write("".join("%24.15e" % v for v in row) + "\n")

@@ -31,6 +31,9 @@ DVM_WP_DENS, DVM_WP_U, DVM_WP_V, DVM_WP_W, DVM_WP_TEMP = 0, 1, 2, 3, 4
 PROP_NAMES = ["dens", "u", "v", "w", "temp", "species_temp", "avg_speed", "pressure",
               "qx", "qy", "qz", "txx", "tyy", "tzz", "txy", "txz", "tyz"]
 DVM_P = {n: i for i, n in enumerate(PROP_NAMES)}
+(DVM_P_DENS, DVM_P_U, DVM_P_V, DVM_P_W, DVM_P_TEMP, DVM_P_SPECIES_TEMP, DVM_P_AVG_SPEED,
+ DVM_P_PRESSURE, DVM_P_QX, DVM_P_QY, DVM_P_QZ, DVM_P_TXX, DVM_P_TYY, DVM_P_TZZ, DVM_P_TXY,
+ DVM_P_TXZ, DVM_P_TYZ) = range(17)
 DVM_NPROP = 20
 
 # kernel ids for instrumentation
@@ -100,6 +103,9 @@ ENTRY_POINTS = {
     "dvm_time_steps": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_double)]),
     "dvm_flush_l2": (C.c_int, [_P]),
     "dvm_get_residual": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "dvm_checkpoint_size": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "dvm_checkpoint_save": (C.c_int, [_P, C.c_uint64, C.c_void_p, C.c_uint64]),
+    "dvm_checkpoint_load": (C.c_int, [_P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "dvm_batch_create": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), C.c_int,
                                    C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_int64),
                                    C.POINTER(_P)]),

@@ -845,6 +845,103 @@ int dvm_get_residual(dvm_ctx* c, double* residual) {
   return st;
 }
 
+}  // extern "C"
+
+// ---- checkpoint / restart ------------------------------------------------------------
+// Layout: a header, then f [C][Nv], the properties [C][NPROP], and with collisions the
+// equilibrium cache [C][4], the cached equilibrium [C][Nv+1] with its CDF [C][Nv+1] and
+// bucket table [C][1000] (the state a cache hit of the next step reuses). Everything else
+// a step reads is rebuilt within the step.
+namespace {
+struct CkptHeader {
+  char magic[8];        // "DVMCKPT1"
+  uint64_t ntime;
+  int32_t ncells, nv, geometry, coll_method, precision, nprop;
+  uint64_t bytes;
+};
+
+struct CkptPart {
+  void* dev;
+  size_t bytes;
+};
+
+int ckpt_parts(dvm_ctx* c, CkptPart (&parts)[6]) {
+  const size_t C = c->ncells, nv = c->g.nv;
+  int n = 0;
+  parts[n++] = {c->d_f, C * nv * sizeof(double)};
+  parts[n++] = {c->d_props, C * DVM_NPROP * sizeof(double)};
+  if (c->p.coll_method != DVM_COLL_NONE) {
+    parts[n++] = {c->d_eq_cache, C * 4 * sizeof(double)};
+    parts[n++] = {c->d_eq_pre, C * (nv + 1) * sizeof(long long)};
+    parts[n++] = {c->d_cum_eq, C * (nv + 1) * sizeof(long long)};
+    parts[n++] = {c->d_ref_eq, C * kNRef * sizeof(int2)};
+  }
+  return n;
+}
+}  // namespace
+
+extern "C" {
+
+int dvm_checkpoint_size(dvm_ctx* c, uint64_t* bytes) {
+  if (!c || !bytes) return DVM_ERR_PARAM;
+  CkptPart parts[6];
+  const int n = ckpt_parts(c, parts);
+  uint64_t b = sizeof(CkptHeader);
+  for (int i = 0; i < n; ++i) b += parts[i].bytes;
+  *bytes = b;
+  return DVM_OK;
+}
+
+int dvm_checkpoint_save(dvm_ctx* c, uint64_t ntime, void* buf, uint64_t bytes) {
+  uint64_t need = 0;
+  if (!c || !buf || dvm_checkpoint_size(c, &need) || bytes < need) return DVM_ERR_PARAM;
+  CkptHeader h{};
+  std::memcpy(h.magic, "DVMCKPT1", 8);
+  h.ntime = ntime;
+  h.ncells = c->ncells; h.nv = c->g.nv; h.geometry = c->p.geometry;
+  h.coll_method = c->p.coll_method; h.precision = c->p.precision; h.nprop = DVM_NPROP;
+  h.bytes = need;
+  std::memcpy(buf, &h, sizeof(h));
+  CkptPart parts[6];
+  const int n = ckpt_parts(c, parts);
+  char* p = static_cast<char*>(buf) + sizeof(h);
+  int st = DVM_OK;
+  for (int i = 0; i < n && !st; ++i) {
+    st = cuda_status(cudaMemcpyAsync(p, parts[i].dev, parts[i].bytes, cudaMemcpyDeviceToHost,
+                                     c->stream));
+    p += parts[i].bytes;
+  }
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  return st;
+}
+
+int dvm_checkpoint_load(dvm_ctx* c, const void* buf, uint64_t bytes, uint64_t* ntime) {
+  uint64_t need = 0;
+  if (!c || !buf || dvm_checkpoint_size(c, &need) || bytes < need) return DVM_ERR_PARAM;
+  CkptHeader h;
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, "DVMCKPT1", 8) != 0 || h.bytes != need || h.ncells != c->ncells ||
+      h.nv != c->g.nv || h.geometry != c->p.geometry || h.coll_method != c->p.coll_method ||
+      h.nprop != DVM_NPROP)
+    return DVM_ERR_PARAM;
+  CkptPart parts[6];
+  const int n = ckpt_parts(c, parts);
+  const char* p = static_cast<const char*>(buf) + sizeof(h);
+  int st = DVM_OK;
+  for (int i = 0; i < n && !st; ++i) {
+    st = cuda_status(cudaMemcpyAsync(parts[i].dev, p, parts[i].bytes, cudaMemcpyHostToDevice,
+                                     c->stream));
+    p += parts[i].bytes;
+  }
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  if (!st && ntime) *ntime = h.ntime;
+  return st;
+}
+
+}  // extern "C"
+
+extern "C" {
+
 int dvm_flush_l2(dvm_ctx* c) {
   if (!c) return DVM_ERR_PARAM;
   if (!c->d_flush) {

@@ -283,14 +283,57 @@ class Host {
   }
 
   // solve (solver/dvm_solver.f90:231-369)
-  int solve(long long nsteps) {
+  // Tecplot output of the moments in the layout of write_properties
+  // (input_output/visualization.f90:620-660, 1591-1660).
+  const char* props_dat = nullptr;
+  long long props_every = 1;
+
+  void write_props_header() const {
+    FILE* fp = std::fopen(props_dat, "w");
+    if (!fp) return;
+    std::fprintf(fp, "title = \"Macroscopic Properties\"\n");
+    std::fprintf(fp, "variables = \"Time\", \"x-Location\", \"y-Location\", \"Density\", "
+                     "\"X-Velocity\", \"Y-Velocity\", \"Z-Velocity\", \"Temperature\", "
+                     "\"Avg Speed\", \"Pressure\", \"Heat Flux X\", \"Heat Flux Y\", "
+                     "\"Heat Flux Z\", \"Tau xx\", \"Tau yy\", \"Tau zz\", \"Tau xy\", "
+                     "\"Tau xz\", \"Tau yz\"\n");
+    std::fclose(fp);
+  }
+
+  int write_props(long long ntime) const {
+    std::vector<double> pr(static_cast<size_t>(ncells) * DVM_NPROP);
+    int st = dvm_get_properties(ctx, pr.data());
+    if (st) return st;
+    FILE* fp = std::fopen(props_dat, "a");
+    if (!fp) return DVM_ERR_PARAM;
+    static const int cols[] = {DVM_P_DENS, DVM_P_U, DVM_P_V, DVM_P_W, DVM_P_TEMP, DVM_P_AVG_SPEED,
+                               DVM_P_PRESSURE, DVM_P_QX, DVM_P_QY, DVM_P_QZ, DVM_P_TXX, DVM_P_TYY,
+                               DVM_P_TZZ, DVM_P_TXY, DVM_P_TXZ, DVM_P_TYZ};
+    std::fprintf(fp, "zone i=%5d\n", ncells);
+    const double time = static_cast<double>(ntime) * p.dt;
+    for (int cx = 0; cx < p.nx_space; ++cx)
+      for (int cy = 0; cy < p.ny_space; ++cy) {
+        const double* q = pr.data() + static_cast<size_t>(cx + p.nx_space * cy) * DVM_NPROP;
+        std::fprintf(fp, "%24.15e%24.15e%24.15e", time, (cx + 0.5) * p.dx, (cy + 0.5) * p.dy);
+        for (int c : cols) std::fprintf(fp, "%24.15e", q[c]);
+        std::fprintf(fp, "\n");
+      }
+    std::fclose(fp);
+    return DVM_OK;
+  }
+
+  int solve(long long nsteps, long long first = 0) {
     std::printf("%8s %12s %18s %18s %18s %12s\n", "ntime", "time", "dens", "x_vel", "temp", "colls");
-    for (long long ntime = 1; ntime <= nsteps; ++ntime) {
+    for (long long ntime = first + 1; ntime <= first + nsteps; ++ntime) {
       int st = dvm_compute_collision_integral(ctx, static_cast<uint64_t>(ntime - 1), nullptr);
       if (!st) st = dvm_compute_convection(ctx);
       if (!st) st = dvm_calculate_physical_properties(ctx);
       if (st) return st;
-      if (ntime % display_freq == 0 || ntime == nsteps) print_update(ntime);
+      if (ntime % display_freq == 0 || ntime == first + nsteps) print_update(ntime);
+      if (props_dat && (ntime % props_every == 0 || ntime == first + nsteps)) {
+        st = write_props(ntime);
+        if (st) return st;
+      }
     }
     uint32_t word = 0;
     dvm_get_error_word(ctx, &word);
@@ -302,6 +345,18 @@ class Host {
     ctx = nullptr;
   }
 };
+
+bool read_file(const char* path, std::vector<char>& v) {
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return false;
+  std::fseek(fp, 0, SEEK_END);
+  const long n = std::ftell(fp);
+  std::fseek(fp, 0, SEEK_SET);
+  v.resize(n > 0 ? static_cast<size_t>(n) : 0);
+  const size_t got = v.empty() ? 0 : std::fread(v.data(), 1, v.size(), fp);
+  std::fclose(fp);
+  return got == v.size();
+}
 
 bool write_doubles(const char* path, const std::vector<double>& v) {
   FILE* fp = std::fopen(path, "wb");
@@ -316,18 +371,27 @@ bool write_doubles(const char* path, const std::vector<double>& v) {
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: %s <input deck> [--check] [--steps N] [--dump-f FILE] "
-                         "[--dump-props FILE]\n", argv[0]);
+                         "[--dump-props FILE] [--props-dat FILE] [--props-every N] "
+                         "[--restart-in FILE] [--restart-out FILE]\n", argv[0]);
     return 1;
   }
   bool check = false;
   long long steps = -1;
   const char* dump_f = nullptr;
   const char* dump_props = nullptr;
+  const char* props_dat = nullptr;
+  const char* restart_in = nullptr;
+  const char* restart_out = nullptr;
+  long long props_every = 1;
   for (int a = 2; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--check")) check = true;
     else if (!std::strcmp(argv[a], "--steps") && a + 1 < argc) steps = std::atoll(argv[++a]);
     else if (!std::strcmp(argv[a], "--dump-f") && a + 1 < argc) dump_f = argv[++a];
     else if (!std::strcmp(argv[a], "--dump-props") && a + 1 < argc) dump_props = argv[++a];
+    else if (!std::strcmp(argv[a], "--props-dat") && a + 1 < argc) props_dat = argv[++a];
+    else if (!std::strcmp(argv[a], "--props-every") && a + 1 < argc) props_every = std::atoll(argv[++a]);
+    else if (!std::strcmp(argv[a], "--restart-in") && a + 1 < argc) restart_in = argv[++a];
+    else if (!std::strcmp(argv[a], "--restart-out") && a + 1 < argc) restart_out = argv[++a];
   }
   Deck deck;
   if (!deck.load(argv[1])) { std::fprintf(stderr, "Error: cannot read %s\n", argv[1]); return 1; }
@@ -349,7 +413,30 @@ int main(int argc, char** argv) {
     return 0;
   }
   int st = h.initialize_solver();
-  if (!st) st = h.solve(steps);
+  long long first = 0;
+  if (!st && restart_in) {  // continue a saved run (restart.f90: ntime and phi)
+    std::vector<char> buf;
+    uint64_t nt = 0;
+    if (!read_file(restart_in, buf)) st = DVM_ERR_PARAM;
+    if (!st) st = dvm_checkpoint_load(h.ctx, buf.data(), buf.size(), &nt);
+    first = static_cast<long long>(nt);
+  }
+  h.props_dat = props_dat;
+  h.props_every = props_every > 0 ? props_every : 1;
+  if (!st && props_dat) {
+    h.write_props_header();
+    st = h.write_props(first);
+  }
+  if (!st) st = h.solve(steps, first);
+  if (!st && restart_out) {
+    uint64_t n = 0;
+    st = dvm_checkpoint_size(h.ctx, &n);
+    std::vector<char> buf(n);
+    if (!st) st = dvm_checkpoint_save(h.ctx, static_cast<uint64_t>(first + steps), buf.data(), n);
+    FILE* fp = st ? nullptr : std::fopen(restart_out, "wb");
+    if (!st && (!fp || std::fwrite(buf.data(), 1, n, fp) != n)) st = DVM_ERR_PARAM;
+    if (fp) std::fclose(fp);
+  }
   if (!st && dump_f) {
     std::vector<double> out(h.f.size());
     st = dvm_download_f(h.ctx, out.data());

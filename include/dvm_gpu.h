@@ -194,6 +194,17 @@ int dvm_last_collision_count(dvm_ctx* ctx, int64_t* count);
  * No reference counterpart (the reference runs a fixed number of steps). */
 int dvm_get_residual(dvm_ctx* ctx, double* residual);
 
+/* ---- checkpoint / restart ------------------------------------------------------------ */
+/* Replaces the reference's restart files (input_output/restart.f90:93-250, ntime and phi):
+ * the checkpoint holds ntime, f, the properties and the cached equilibrium with its CDF
+ * and bucket table, so that a context restored from it continues the run exactly as the
+ * saved one would (the Philox stream is indexed by ntime). The buffer is host memory of
+ * dvm_checkpoint_size bytes; dvm_checkpoint_load checks that it belongs to a context of
+ * the same cells, grid size, geometry and collision method. */
+int dvm_checkpoint_size(dvm_ctx* ctx, uint64_t* bytes);
+int dvm_checkpoint_save(dvm_ctx* ctx, uint64_t ntime, void* buf, uint64_t bytes);
+int dvm_checkpoint_load(dvm_ctx* ctx, const void* buf, uint64_t bytes, uint64_t* ntime);
+
 /* ---- batched homogeneous instances --------------------------------------------------- */
 /* Many independent 0-D relaxations (the reference's homogeneous case, nx_space = ny_space =
  * 1, run for many initial states and grids at once). No reference counterpart. Instances on

@@ -84,3 +84,28 @@ def test_host_matches_python_host(gpulib, host, pkg, tmp_path, deck):
     s.solve(steps)
     f_py = s.phi().ravel()
     assert np.abs(f_host - f_py).max() <= 1e-12 * np.abs(f_py).max()
+
+
+@pytest.mark.gpu
+def test_host_restart_continues_the_run(gpulib, host, tmp_path):
+    """restart.f90's role: a run stopped after 1 step and restarted for 2 ends where the
+    straight 3-step run ends; the Tecplot file has one zone per output time."""
+    deck = os.path.join(DECKS, "shock1d.inp")
+    straight, part, resumed = tmp_path / "a.bin", tmp_path / "ck.bin", tmp_path / "b.bin"
+    dat = tmp_path / "props.dat"
+    r = subprocess.run([host, deck, "--steps", "3", "--dump-f", str(straight), "--props-dat",
+                        str(dat)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([host, deck, "--steps", "1", "--restart-out", str(part)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([host, deck, "--steps", "2", "--restart-in", str(part), "--dump-f",
+                        str(resumed)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    a = np.fromfile(str(straight), dtype=np.float64)
+    b = np.fromfile(str(resumed), dtype=np.float64)
+    assert np.abs(a - b).max() <= 1e-13 * np.abs(a).max()
+    lines = dat.read_text().splitlines()
+    assert lines[0].startswith("title") and lines[1].startswith("variables")
+    assert sum(1 for l in lines if l.startswith("zone")) == 4  # times 0, 1, 2, 3
+    assert len(lines) == 2 + 4 * 11

@@ -91,6 +91,20 @@ __device__ __forceinline__ double dfl_to_double(dfl a) {
   return dbl_from_float(a.hi) + dbl_from_float(a.lo);
 }
 
+// Exact float -> double for a normal float or zero (no subnormal, inf or NaN handling):
+// the short form for values known to lie well inside the float range.
+__device__ __forceinline__ double dbl_from_normal_float(float v) {
+  const uint32_t u = static_cast<uint32_t>(__float_as_int(v));
+  const uint32_t hi = (u & 0x80000000u) | (((u >> 23) & 0xffu) + 896u) << 20 | ((u & 0x7fffffu) >> 3);
+  const uint32_t lo = u << 29;
+  return (u & 0x7fffffffu) ? __hiloint2double(static_cast<int>(hi), static_cast<int>(lo)) : 0.0;
+}
+
+// Pair -> double for pairs of normal floats (hi in the normal range, lo normal or zero).
+__device__ __forceinline__ double dfl_to_double_normal(dfl a) {
+  return dbl_from_normal_float(a.hi) + dbl_from_normal_float(a.lo);
+}
+
 // Knuth's TwoSum: s + e = a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);

@@ -184,6 +184,7 @@ cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, float* df, int grid,
                                cudaStream_t s);
 cudaError_t launch_project(const ProjectArgs& a, cudaStream_t s);
+
 int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t);
 cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_wall_specular(const WallArgs& a, cudaStream_t s);

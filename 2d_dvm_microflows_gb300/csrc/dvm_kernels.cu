@@ -705,34 +705,34 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   const int base = o_i + NX * o_j + NXY * o_k;
   dfl sum = zero;
   if (fx) {
-    atomicAdd(f + base - sa, dfl_to_double(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - sa, dfl_to_double_normal(dfl_mul(w8, f_e)));
     sum = f_e;
   }
   if (fy) {
-    atomicAdd(f + base - NX * sb, dfl_to_double(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - NX * sb, dfl_to_double_normal(dfl_mul(w8, f_e)));
     sum = dfl_add(sum, f_e);
   }
   if (fz) {
-    atomicAdd(f + base - NXY * sc, dfl_to_double(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - NXY * sc, dfl_to_double_normal(dfl_mul(w8, f_e)));
     sum = dfl_add(sum, f_e);
   }
   {
     const dfl f_ix = dfl_mul(dfl_sub(a, fx ? dfl_mul(f_e, ext_x) : zero), inv_x);
-    atomicAdd(f + base + sa, dfl_to_double(dfl_mul(w8, f_ix)));
+    atomicAdd(f + base + sa, dfl_to_double_normal(dfl_mul(w8, f_ix)));
     sum = dfl_add(sum, f_ix);
   }
   {
     const dfl f_iy = dfl_mul(dfl_sub(b, fy ? dfl_mul(f_e, ext_y) : zero), inv_y);
-    atomicAdd(f + base + NX * sb, dfl_to_double(dfl_mul(w8, f_iy)));
+    atomicAdd(f + base + NX * sb, dfl_to_double_normal(dfl_mul(w8, f_iy)));
     sum = dfl_add(sum, f_iy);
   }
   {
     const dfl f_iz = dfl_mul(dfl_sub(c, fz ? dfl_mul(f_e, ext_z) : zero), inv_z);
-    atomicAdd(f + base + NXY * sc, dfl_to_double(dfl_mul(w8, f_iz)));
+    atomicAdd(f + base + NXY * sc, dfl_to_double_normal(dfl_mul(w8, f_iz)));
     sum = dfl_add(sum, f_iz);
   }
   const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
-  atomicAdd(f + base, dfl_to_double(dfl_mul(w8, f_o)));
+  atomicAdd(f + base, dfl_to_double_normal(dfl_mul(w8, f_o)));
   return bad;
 }
 
@@ -1007,6 +1007,7 @@ int collide_blocks_per_sm(size_t smem) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide, kCollideChunk, smem) !=
       cudaSuccess)
     n = 1;
+  cudaGetLastError();  // a refused query must not surface at the next launch
   return n > 0 ? n : 1;
 }
 
@@ -1182,9 +1183,19 @@ __host__ __device__ inline CollideSmemF collide_f32_smem_layout(const GridInfo& 
   return L;
 }
 
-__global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a, CollTablesF tf,
-                                                                float* __restrict__ dfs) {
-  extern __shared__ __align__(16) unsigned char s_raw[];
+// Shared-memory tables of the FP32 collide kernels.
+struct F32Ctx {
+  SmemAxesF A;
+  const float2* gtab;
+  const float2* strig;
+  float vhs, ralpha;
+  bool vss, vr;
+  int NR;
+  uint32_t step;
+};
+
+__device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const CollTablesF& tf,
+                                                  unsigned char* s_raw) {
   const GridInfo& g = a.g;
   const CollideSmemF L = collide_f32_smem_layout(g, a.t, tf.gtab_smem);
   float* sv = reinterpret_cast<float*>(s_raw + L.axes);
@@ -1209,26 +1220,152 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   if (tf.gtab_smem)
     for (int t = threadIdx.x; t < a.t.gtab_n; t += blockDim.x) sg[t] = tf.gtab[t];
   for (int t = threadIdx.x; t < kTrigN; t += blockDim.x) strig[t] = tf.trig[t];
-  __syncthreads();
-  SmemAxesF A;
-  A.v[0] = sv; A.v[1] = sv + g.nx; A.v[2] = sv + g.nx + g.ny;
-  A.mid[0] = sk; A.mid[1] = sk + g.nx; A.mid[2] = sk + g.nx + g.ny;
-  A.tab[0] = st; A.tab[1] = st + a.t.nmax; A.tab[2] = st + 2 * a.t.nmax;
-  A.n[0] = g.nx; A.n[1] = g.ny; A.n[2] = g.nz;
-  const float2* gtab = a.t.gtab ? (tf.gtab_smem ? sg : tf.gtab) : nullptr;
+  F32Ctx c;
+  c.A.v[0] = sv; c.A.v[1] = sv + g.nx; c.A.v[2] = sv + g.nx + g.ny;
+  c.A.mid[0] = sk; c.A.mid[1] = sk + g.nx; c.A.mid[2] = sk + g.nx + g.ny;
+  c.A.tab[0] = st; c.A.tab[1] = st + a.t.nmax; c.A.tab[2] = st + 2 * a.t.nmax;
+  c.A.n[0] = g.nx; c.A.n[1] = g.ny; c.A.n[2] = g.nz;
+  c.gtab = a.t.gtab ? (tf.gtab_smem ? sg : tf.gtab) : nullptr;
+  c.strig = strig;
+  c.vhs = static_cast<float>(2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega)));
+  c.ralpha = 1.f / static_cast<float>(0.5 * (a.cp.alpha + a.cp.alpha));
+  c.vss = fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol;
+  c.vr = (a.cp.method == DVM_COLL_VR);
+  c.NR = a.cp.num_repl;
+  c.step = a.step_dev ? *a.step_dev : a.step;
+  return c;
+}
 
+// One sample of sub-integral q of a cell in FP32, scattered into df (global or shared).
+__device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const CollTablesF& tf,
+                                                   const F32Ctx& c, int cell, int q, long long i,
+                                                   float factor, float* df, uint32_t& bad) {
+  const GridInfo& g = a.g;
+  const SmemAxesF& A = c.A;
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
+  const size_t cs = static_cast<size_t>(cell) * (nv + 1);
+  const bool vr = c.vr;
+  double rA = 0.0, rB = 0.0;
+  const bool rec = a.pairs.active;
+  if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, c.step, q, 0u, rA, rB);
+  int lA, lB;
+  if (rec && a.pairs.glA[q]) {
+    lA = a.pairs.glA[q][i];
+    lB = a.pairs.glB[q][i];
+  } else {
+    if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
+    const bool aeq = vr && q == 0, beq = vr && q == 1;
+    lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
+                                 (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
+                                 nv, rA, bad);
+    lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
+                                 (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
+                                 nv, rB, bad);
+  }
+  const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
+  const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
+  const float xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
+  const float xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
+  float gg, g_sigma;
+  if (c.gtab) {
+    const int di = iB - iA, dj = jB - jA, dk = kB - kA;
+    const int s2 = di * di + dj * dj + dk * dk;
+    if (s2 == 0) return;
+    const float2 e = c.gtab[s2];
+    gg = e.x;
+    g_sigma = e.y;
+  } else {
+    const float gx = xB - xA, gy = yB - yA, gz = zB - zA;
+    gg = sqrtf(gx * gx + gy * gy + gz * gz);
+    if (gg < 1e-13f) return;
+    g_sigma = (c.vhs == 1.f) ? gg : powf(gg, c.vhs);
+  }
+  const float* kc = a.kin + cs;
+  const float sA = (vr && q == 0) ? 1.f : (signbit(__ldg(kc + lA + 1)) ? -1.f : 1.f);
+  const float sB = (vr && q == 1) ? 1.f : (signbit(__ldg(kc + lB + 1)) ? -1.f : 1.f);
+  const float kin = sA * sB * factor * g_sigma;
+  atomicAdd(df + lA, -kin);
+  atomicAdd(df + lB, -kin);
+  const int NR = c.NR;
+  const float kr = kin / static_cast<float>(NR);
+  const float vc0 = 0.5f * (xA + xB), vc1 = 0.5f * (yA + yB), vc2 = 0.5f * (zA + zB);
+  const float hg = 0.5f * gg;
+  for (int r = 0; r < NR; ++r) {
+    float rphi, rcos;
+    if (rec) {
+      rphi = static_cast<float>(a.pairs.rphi[q][i * NR + r]);
+      rcos = static_cast<float>(a.pairs.rcos[q][i * NR + r]);
+    } else {
+      // the top 24 bits of the two uniforms the FP64 form draws from this counter
+      uint32_t o[4];
+      philox4x32_10(static_cast<uint32_t>(i), cell, c.step, (q & 3u) | ((1u + r) << 2),
+                    static_cast<uint32_t>(a.cp.seed), static_cast<uint32_t>(a.cp.seed >> 32), o);
+      rphi = static_cast<float>(o[1] >> 8) * 0x1.0p-24f;
+      rcos = static_cast<float>(o[3] >> 8) * 0x1.0p-24f;
+    }
+    float sphi, cphi;
+    {
+      const float rk = floorf(rphi * static_cast<float>(kTrigN));
+      const int k = min(max(static_cast<int>(rk), 0), kTrigN - 1);
+      const float th = tf.two_pi * (rphi - rk * (1.f / kTrigN));
+      const float t2 = th * th;
+      const float st = th * (1.f - t2 * (1.f / 6.f));
+      const float ct = 1.f - 0.5f * t2;
+      const float2 cs2 = c.strig[k];
+      cphi = cs2.x * ct - cs2.y * st;
+      sphi = cs2.y * ct + cs2.x * st;
+    }
+    float ux, uy, uz;
+    if (c.vss) {
+      const float ur = fabsf(xA - vc0) + fabsf(xB - vc0);
+      const float vr_ = fabsf(yA - vc1) + fabsf(yB - vc1);
+      const float wr = fabsf(zA - vc2) + fabsf(zB - vc2);
+      const float ct = 2.f * powf(rcos, c.ralpha) - 1.f;
+      const float stt = sqrtf(fmaxf(1.f - ct * ct, 0.f));
+      const float den = sqrtf(vr_ * vr_ + wr * wr);
+      float rx, ry, rz;
+      if (den > 1e-13f * gg) {
+        rx = ct * ur + stt * sphi * den;
+        ry = ct * vr_ + stt * (gg * wr * cphi - ur * vr_ * sphi) / den;
+        rz = ct * wr - stt * (gg * vr_ * cphi + ur * wr * sphi) / den;
+      } else {
+        rx = ct * ur; ry = stt * cphi * ur; rz = stt * sphi * ur;
+      }
+      ux = 0.5f * rx; uy = 0.5f * ry; uz = 0.5f * rz;
+    } else {
+      const float ct = 2.f * rcos - 1.f;
+      const float stt = sqrtf(fmaxf(1.f - ct * ct, 0.f));
+      ux = hg * stt * cphi;
+      uy = hg * stt * sphi;
+      uz = hg * ct;
+    }
+    StencilF sA_, sB_;
+    int rb = remap_f32(g, A, vc0 + ux, vc1 + uy, vc2 + uz, sA_);
+    if (rb & 2) bad |= DVM_EW_REMAP;
+    else {
+#pragma unroll
+      for (int m = 0; m < 7; ++m)
+        if (sA_.node[m] >= 0) atomicAdd(df + sA_.node[m], kr * sA_.mass[m]);
+    }
+    rb = remap_f32(g, A, vc0 - ux, vc1 - uy, vc2 - uz, sB_);
+    if (rb & 2) bad |= DVM_EW_REMAP;
+    else {
+#pragma unroll
+      for (int m = 0; m < 7; ++m)
+        if (sB_.node[m] >= 0) atomicAdd(df + sB_.node[m], kr * sB_.mass[m]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a, CollTablesF tf,
+                                                                float* __restrict__ dfs) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  const F32Ctx c = load_f32_tables(a, tf, s_raw);
+  __syncthreads();
+  const int nv = a.g.nv;
   const int nent = 3 * a.ncells;
   const long long total = a.chunk_off[nent];
-  const bool vr = (a.cp.method == DVM_COLL_VR);
-  const int NR = a.cp.num_repl;
-  const float vhs = static_cast<float>(2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega)));
-  const float alpha = static_cast<float>(0.5 * (a.cp.alpha + a.cp.alpha));
-  const float ralpha = 1.f / alpha;
-  const bool vss = fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol;
-  const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
-
   for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
     int lo = 0, hi = nent;
     while (hi - lo > 1) {
@@ -1239,119 +1376,8 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
     const CellPlan& pl = a.plan[cell];
     const long long i = (chunk - a.chunk_off[lo]) * kCollideChunk + threadIdx.x;
     if (i >= pl.num[q]) continue;
-    const float factor = static_cast<float>(pl.factor[q]);
-    const size_t cs = static_cast<size_t>(cell) * (nv + 1);
-    float* df = dfs + static_cast<size_t>(cell) * nv;
-
-    double rA = 0.0, rB = 0.0;
-    const bool rec = a.pairs.active;
-    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, rA, rB);
-    int lA, lB;
-    if (rec && a.pairs.glA[q]) {
-      lA = a.pairs.glA[q][i];
-      lB = a.pairs.glB[q][i];
-    } else {
-      if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
-      const bool aeq = vr && q == 0, beq = vr && q == 1;
-      lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
-                                  (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                  nv, rA, bad);
-      lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
-                                  (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                  nv, rB, bad);
-    }
-    const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
-    const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
-    const float xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
-    const float xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
-    float gg, g_sigma;
-    if (gtab) {
-      const int di = iB - iA, dj = jB - jA, dk = kB - kA;
-      const int s2 = di * di + dj * dj + dk * dk;
-      if (s2 == 0) continue;
-      const float2 e = gtab[s2];
-      gg = e.x;
-      g_sigma = e.y;
-    } else {
-      const float gx = xB - xA, gy = yB - yA, gz = zB - zA;
-      gg = sqrtf(gx * gx + gy * gy + gz * gz);
-      if (gg < 1e-13f) continue;
-      g_sigma = (vhs == 1.f) ? gg : powf(gg, vhs);
-    }
-    const float* kc = a.kin + cs;
-    const float sA = (vr && q == 0) ? 1.f : (signbit(__ldg(kc + lA + 1)) ? -1.f : 1.f);
-    const float sB = (vr && q == 1) ? 1.f : (signbit(__ldg(kc + lB + 1)) ? -1.f : 1.f);
-    const float kin = sA * sB * factor * g_sigma;
-    atomicAdd(df + lA, -kin);
-    atomicAdd(df + lB, -kin);
-    const float kr = kin / static_cast<float>(NR);
-    const float vc0 = 0.5f * (xA + xB), vc1 = 0.5f * (yA + yB), vc2 = 0.5f * (zA + zB);
-    const float hg = 0.5f * gg;
-    for (int r = 0; r < NR; ++r) {
-      float rphi, rcos;
-      if (rec) {
-        rphi = static_cast<float>(a.pairs.rphi[q][i * NR + r]);
-        rcos = static_cast<float>(a.pairs.rcos[q][i * NR + r]);
-      } else {
-        // the top 24 bits of the two uniforms the FP64 form draws from this counter
-        uint32_t o[4];
-        philox4x32_10(static_cast<uint32_t>(i), cell, step, (q & 3u) | ((1u + r) << 2),
-                      static_cast<uint32_t>(a.cp.seed), static_cast<uint32_t>(a.cp.seed >> 32), o);
-        rphi = static_cast<float>(o[1] >> 8) * 0x1.0p-24f;
-        rcos = static_cast<float>(o[3] >> 8) * 0x1.0p-24f;
-      }
-      float sphi, cphi;
-      {
-        const float rk = floorf(rphi * static_cast<float>(kTrigN));
-        const int k = min(max(static_cast<int>(rk), 0), kTrigN - 1);
-        const float th = tf.two_pi * (rphi - rk * (1.f / kTrigN));
-        const float t2 = th * th;
-        const float st = th * (1.f - t2 * (1.f / 6.f));
-        const float ct = 1.f - 0.5f * t2;
-        const float2 cs2 = strig[k];
-        cphi = cs2.x * ct - cs2.y * st;
-        sphi = cs2.y * ct + cs2.x * st;
-      }
-      float ux, uy, uz;
-      if (vss) {
-        const float ur = fabsf(xA - vc0) + fabsf(xB - vc0);
-        const float vr_ = fabsf(yA - vc1) + fabsf(yB - vc1);
-        const float wr = fabsf(zA - vc2) + fabsf(zB - vc2);
-        const float ct = 2.f * powf(rcos, ralpha) - 1.f;
-        const float stt = sqrtf(fmaxf(1.f - ct * ct, 0.f));
-        const float den = sqrtf(vr_ * vr_ + wr * wr);
-        float rx, ry, rz;
-        if (den > 1e-13f * gg) {
-          rx = ct * ur + stt * sphi * den;
-          ry = ct * vr_ + stt * (gg * wr * cphi - ur * vr_ * sphi) / den;
-          rz = ct * wr - stt * (gg * vr_ * cphi + ur * wr * sphi) / den;
-        } else {
-          rx = ct * ur; ry = stt * cphi * ur; rz = stt * sphi * ur;
-        }
-        ux = 0.5f * rx; uy = 0.5f * ry; uz = 0.5f * rz;
-      } else {
-        const float ct = 2.f * rcos - 1.f;
-        const float stt = sqrtf(fmaxf(1.f - ct * ct, 0.f));
-        ux = hg * stt * cphi;
-        uy = hg * stt * sphi;
-        uz = hg * ct;
-      }
-      StencilF sA_, sB_;
-      int rb = remap_f32(g, A, vc0 + ux, vc1 + uy, vc2 + uz, sA_);
-      if (rb & 2) bad |= DVM_EW_REMAP;
-      else {
-#pragma unroll
-        for (int m = 0; m < 7; ++m)
-          if (sA_.node[m] >= 0) atomicAdd(df + sA_.node[m], kr * sA_.mass[m]);
-      }
-      rb = remap_f32(g, A, vc0 - ux, vc1 - uy, vc2 - uz, sB_);
-      if (rb & 2) bad |= DVM_EW_REMAP;
-      else {
-#pragma unroll
-        for (int m = 0; m < 7; ++m)
-          if (sB_.node[m] >= 0) atomicAdd(df + sB_.node[m], kr * sB_.mass[m]);
-      }
-    }
+    collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
+                       dfs + static_cast<size_t>(cell) * nv, bad);
   }
   if (bad) atomicOr(a.err, bad);
 }
@@ -1366,6 +1392,7 @@ int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide_f32, kCollideChunk, smem) !=
       cudaSuccess)
     n = 1;
+  cudaGetLastError();
   return n > 0 ? n : 1;
 }
 
@@ -1394,19 +1421,17 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
 // reason, and f + df - w * poly is formed in FP64 from the exact doubles of the two floats.
 constexpr int kProjThreads = 256;
 
-__global__ void __launch_bounds__(kProjThreads, 3) k_project(ProjectArgs a) {
+// The projection of one cell, for the block: df (global or shared) is read, its projected
+// value added to f, and df zeroed when it is the global increment buffer.
+__device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool zero_df,
+                                             double* f, const double* P) {
   __shared__ float2 s_red[20 * 32];
   __shared__ float s_lam[5];
   __shared__ dfl s_axd[2 * kMaxAxis];  // x', y' as pairs
   __shared__ dfl s_zd[2 * kMaxAxis];   // z', z'^2 as pairs
   __shared__ float s_axf[2 * kMaxAxis];
   __shared__ float s_zf[4 * kMaxAxis];  // z'^p, p = 1..4
-  const GridInfo& g = a.g;
-  const int cell = blockIdx.x;
-  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
-  float* df = a.df + static_cast<size_t>(cell) * nv;
-  double* f = a.f + static_cast<size_t>(cell) * nv;
-  const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
+  const int NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
   const double u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
   for (int t = threadIdx.x; t < NX; t += blockDim.x) {
     const double x = g.x[t] - u;
@@ -1525,9 +1550,15 @@ __global__ void __launch_bounds__(kProjThreads, 3) k_project(ProjectArgs a) {
       const float poly = fmaf(l4, s_zf[kMaxAxis + k], fmaf(l3, s_zf[k], base));
       const float corr = fabsf(d) * poly;
       f[l] = (f[l] + dbl_from_float(d)) - dbl_from_float(corr);
-      df[l] = 0.f;
+      if (zero_df) df[l] = 0.f;
     }
   }
+}
+
+__global__ void __launch_bounds__(kProjThreads, 3) k_project(ProjectArgs a) {
+  const int cell = blockIdx.x;
+  const size_t off = static_cast<size_t>(cell) * a.g.nv;
+  project_cell(a.g, a.df + off, true, a.f + off, a.props + static_cast<size_t>(cell) * DVM_NPROP);
 }
 
 cudaError_t launch_project(const ProjectArgs& a, cudaStream_t s) {

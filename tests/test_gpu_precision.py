@@ -123,3 +123,18 @@ def test_cavity_fp32_one_step_error(gpulib, pkg):
     err = moment_errors(p32, p64)
     assert err.max() <= 1e-6, dict(zip(pkg.PROP_NAMES, err))
     assert e32 == 0
+
+
+@pytest.mark.parametrize("n", [16, 40])
+def test_fp32_one_step_error_grid_sizes(gpulib, pkg, n):
+    """One step of the FP32 form on a small and a large grid (tables in shared memory and
+    the g-table through L1): within FP32 rounding of the FP64 step, conservative."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(n, -5.0, 5.0)
+    f0 = ph.bimodal(g)
+    kw = dict(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FIXED,
+              samples_per_step=50000, deltat=0.02, seed=6)
+    (p64, _, _), (p32, _, e32) = _pair(pkg, g, f0, 1, **kw)
+    err = moment_errors(p32, p64)
+    assert err.max() <= 1e-6, dict(zip(pkg.PROP_NAMES, err))
+    assert abs(p32[0, 0] - p64[0, 0]) <= 1e-12 and e32 == 0

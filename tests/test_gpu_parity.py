@@ -321,3 +321,22 @@ def test_ensemble_moments_within_3se(gpulib, pkg, oracle):
     for q in (pkg.DVM_P["qx"], pkg.DVM_P["txx"], pkg.DVM_P["txy"], pkg.DVM_P["tyy"]):
         se = np.sqrt(a[:, q].var(ddof=1) / K + b[:, q].var(ddof=1) / K)
         assert abs(a[:, q].mean() - b[:, q].mean()) <= 3.0 * se + 1e-14, pkg.PROP_NAMES[q]
+
+
+@pytest.mark.parametrize("method", ["VR", "FMC"])
+def test_philox_steps_larger_grid(gpulib, pkg, oracle, method):
+    """A 20^3 grid (g-table through L1 rather than shared memory) with 4e4 samples per
+    step: the steps agree with the restatement within 1e-12."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(20, -6.0, 6.0)
+    f0 = ph.bimodal(g)
+    coll = pkg.DVM_COLL_VR if method == "VR" else pkg.DVM_COLL_FMC
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, iColl=coll, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                            samples_per_step=40000, omega=0.81, seed=17, deltat=0.02,
+                            cdf_tolerance=0.01)
+    for _ in range(2):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert gpu.collision_count() == cpu.collision_count()
+    assert gpu.error_word() == 0

@@ -7,7 +7,8 @@
 
 namespace dvm {
 
-constexpr int kCollideChunk = 256;  // samples per chunk = threads per collide CTA
+constexpr int kCollideChunk = 256;  // threads per collide CTA
+constexpr int kChunkSamples = 32;   // samples per chunk of one (cell, sub-integral): a warp
 
 // Samples and depletion factor of each sub-integral of one cell-step
 // (variance_reduction.f90:669-683, 822-835, 967-981; full_mc.f90:330-331).

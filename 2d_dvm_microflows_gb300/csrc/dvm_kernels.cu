@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(1024) k_plan(int ncells, const CellPlan* plan,
     const int e = base + threadIdx.x;
     long long num = 0;
     if (e < n) num = plan[e / 3].num[e % 3];
-    long long ch = (num + kCollideChunk - 1) / kCollideChunk;
+    long long ch = (num + kChunkSamples - 1) / kChunkSamples;
     long long v = ch;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -491,7 +491,7 @@ cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
 }
 
 // ----------------------------------------------------------------------------------------
-// k_collide: persistent; a chunk is kCollideChunk consecutive samples of one
+// k_collide: persistent; a chunk is kChunkSamples consecutive samples of one
 // (cell, sub-integral). One thread per sample.
 //
 // GB300 runs FP64 at 1/64 of its FP32 rate, so this kernel moves its arithmetic off the
@@ -843,7 +843,14 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
 
-  for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
+  // one warp per chunk; chunks are visited in a scattered order (a bijection of
+  // 0..total-1), so the warps in flight at any moment work on many cells and their FP64
+  // atomics spread over many f slabs instead of piling onto the busiest nodes of one cell
+  const int wpb = blockDim.x >> 5;
+  for (long long pos = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
+       pos < total; pos += static_cast<long long>(gridDim.x) * wpb) {
+    const long long chunk = static_cast<long long>(
+        (static_cast<unsigned long long>(pos) * 2147483647ull) % static_cast<unsigned long long>(total));
     int lo = 0, hi = nent;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -851,7 +858,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
     }
     const int cell = lo / 3, q = lo - 3 * (lo / 3);
     const CellPlan& pl = a.plan[cell];
-    const long long i = (chunk - a.chunk_off[lo]) * kCollideChunk + threadIdx.x;
+    const long long i = (chunk - a.chunk_off[lo]) * kChunkSamples + (threadIdx.x & 31);
     if (i >= pl.num[q]) continue;
     const double factor = pl.factor[q];
     const size_t cs = static_cast<size_t>(cell) * (nv + 1);
@@ -1366,7 +1373,11 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   const int nent = 3 * a.ncells;
   const long long total = a.chunk_off[nent];
   uint32_t bad = 0;
-  for (long long chunk = blockIdx.x; chunk < total; chunk += gridDim.x) {
+  const int wpb = blockDim.x >> 5;
+  for (long long pos = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
+       pos < total; pos += static_cast<long long>(gridDim.x) * wpb) {
+    const long long chunk = static_cast<long long>(
+        (static_cast<unsigned long long>(pos) * 2147483647ull) % static_cast<unsigned long long>(total));
     int lo = 0, hi = nent;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -1374,7 +1385,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
     }
     const int cell = lo / 3, q = lo - 3 * (lo / 3);
     const CellPlan& pl = a.plan[cell];
-    const long long i = (chunk - a.chunk_off[lo]) * kCollideChunk + threadIdx.x;
+    const long long i = (chunk - a.chunk_off[lo]) * kChunkSamples + (threadIdx.x & 31);
     if (i >= pl.num[q]) continue;
     collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
                        dfs + static_cast<size_t>(cell) * nv, bad);

@@ -325,8 +325,8 @@ def test_ensemble_moments_within_3se(gpulib, pkg, oracle):
 
 @pytest.mark.parametrize("method", ["VR", "FMC"])
 def test_philox_steps_larger_grid(gpulib, pkg, oracle, method):
-    """A 20^3 grid (g-table through L1 rather than shared memory) with 4e4 samples per
-    step: the steps agree with the restatement within 1e-12."""
+    """A 20^3 grid with 4e4 samples per step: the steps agree with the restatement
+    within 1e-12."""
     ph = pkg.physics
     g = ph.VelocityGrid.uniform(20, -6.0, 6.0)
     f0 = ph.bimodal(g)

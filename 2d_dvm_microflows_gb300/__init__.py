@@ -292,6 +292,13 @@ class DVMSolver:
     def flush_l2(self):
         _check(self.lib.dvm_flush_l2(self.ctx), "dvm_flush_l2")
 
+    def atomic_rate(self, window_bytes):
+        """Measured FP64 atomic adds per second over a window of device memory."""
+        v = C.c_double()
+        _check(self.lib.dvm_atomic_rate(self.ctx, C.c_uint64(int(window_bytes)), C.byref(v)),
+               "dvm_atomic_rate")
+        return v.value
+
 
 class DVMBatch:
     """Many independent 0-D relaxations stepped together (dvm_batch_*): instances on the same

@@ -952,6 +952,26 @@ int dvm_flush_l2(dvm_ctx* c) {
   return cuda_status(launch_flush(c->d_flush, c->flush_n, c->stream));
 }
 
+int dvm_atomic_rate(dvm_ctx* c, uint64_t window_bytes, double* per_s) {
+  if (!c || !per_s || window_bytes < sizeof(double)) return DVM_ERR_PARAM;
+  int st = dvm_flush_l2(c);  // allocates the scratch buffer
+  if (st) return st;
+  const size_t n = std::min(static_cast<size_t>(window_bytes / sizeof(double)), c->flush_n);
+  const int blocks = c->num_sms * 8, per_thread = 256;
+  cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+  st = cuda_status(launch_atomic_probe(c->d_flush, n, blocks, per_thread, c->stream));  // warm
+  if (!st) cudaEventRecord(e0, c->stream);
+  if (!st) st = cuda_status(launch_atomic_probe(c->d_flush, n, blocks, per_thread, c->stream));
+  if (!st) cudaEventRecord(e1, c->stream);
+  if (!st) st = cuda_status(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  if (!st) cudaEventElapsedTime(&ms, e0, e1);
+  c->ev_pool.push_back(e0);
+  c->ev_pool.push_back(e1);
+  *per_s = ms > 0.f ? static_cast<double>(blocks) * 256.0 * per_thread / (ms * 1e-3) : 0.0;
+  return st;
+}
+
 }  // extern "C"
 
 // ----------------------------------------------------------------------------------------

@@ -2126,6 +2126,22 @@ cudaError_t launch_step_end(uint32_t* counter, long long* acc, const long long* 
   return cudaGetLastError();
 }
 
+// FP64 atomic-add throughput probe: every thread adds to pseudo-random doubles of a
+// window of n (the scatter pattern of k_collide over an L2-resident slab of f).
+__global__ void __launch_bounds__(256) k_atomic_probe(double* buf, size_t n, int per_thread) {
+  uint32_t x = 0x9E3779B9u * (blockIdx.x * blockDim.x + threadIdx.x + 1u);
+  for (int r = 0; r < per_thread; ++r) {
+    x ^= x << 13; x ^= x >> 17; x ^= x << 5;
+    atomicAdd(buf + (x % n), 1e-300);
+  }
+}
+
+cudaError_t launch_atomic_probe(double* buf, size_t n, int blocks, int per_thread,
+                                cudaStream_t s) {
+  k_atomic_probe<<<blocks, 256, 0, s>>>(buf, n, per_thread);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s) {
   k_flush<<<1216, 256, 0, s>>>(buf, n);
   return cudaGetLastError();

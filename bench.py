@@ -42,6 +42,7 @@ OMEGA = 0.81
 SAMPLES = 200000
 SEED = 20261203
 BYTES_PER_SAMPLE = 8 * (2 + 2 * 16)  # 2 partner reads + 16 atomic read-modify-writes
+ATOMICS_PER_SAMPLE = 16              # 2 depletions + 2 x 7 replenishment nodes
 
 
 def workload_config(pkg, ncells=None):
@@ -698,6 +699,10 @@ def run_gpu(args):
         with open(tp) as fh:
             traffic = json.load(fh).get("bytes_per_launch")
     kernels = {k: {"ms_total": v[0], "launches": v[1]} for k, v in prof.items() if v[1]}
+    # the collide kernel's scatter is FP64 atomics into an L2-resident f: its second
+    # roofline is the measured atomic rate over a window the size of f
+    atom_peak = s.atomic_rate(NCELLS * nv * 8)
+    atom_achieved = samples_per_launch * ATOMICS_PER_SAMPLE / t_launch
     line = {
         "metric": "MC collisions/s", "value": value, "unit": "collisions/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
@@ -708,6 +713,11 @@ def run_gpu(args):
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_sample": BYTES_PER_SAMPLE},
+        "roofline_atomic": {"kernel": "collide", "achieved": atom_achieved, "peak": atom_peak,
+                            "unit": "FP64 atomic adds/s", "frac": atom_achieved / atom_peak,
+                            "atomics_per_sample": ATOMICS_PER_SAMPLE,
+                            "peak_source": "measured in this run (dvm_atomic_rate, pseudo-"
+                                           "random adds over a window the size of f)"},
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "collisions/s",
                 "h2d_bytes_per_step": NCELLS * nv * 8, "d2h_bytes_per_step": NCELLS * nv * 8},

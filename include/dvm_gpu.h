@@ -290,6 +290,10 @@ int dvm_launch_count(dvm_ctx* ctx, int64_t* launches);
 int dvm_time_steps(dvm_ctx* ctx, uint64_t first_step, int nsteps, double* ms);
 /* Writes a buffer of bytes > L2 on the context's stream (cold-cache timing). */
 int dvm_flush_l2(dvm_ctx* ctx);
+/* FP64 atomic-add throughput (adds per second) of pseudo-random addresses in a window of
+ * window_bytes of device memory: the roofline of a scatter whose target stays in L2.
+ * Instrumentation; no reference counterpart. */
+int dvm_atomic_rate(dvm_ctx* ctx, uint64_t window_bytes, double* per_s);
 
 /* ---- collisions without device allocation ------------------------------------------ */
 /* No counterpart in the reference. The collision integral of dvm_compute_collision_integral

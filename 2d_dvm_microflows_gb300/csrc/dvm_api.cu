@@ -378,6 +378,10 @@ CollParams coll_params(const dvm_ctx* c) {
   cp.cdf_tolerance = c->p.cdf_tolerance;
   cp.pi = c->pi;
   cp.seed = c->p.seed;
+  // compute_num_coll_pairs (collision_utilities.f90:106-140): beta3_min * m^(3/2), averaged
+  // over the (like-species) pair
+  const double b3a = c->g.beta3_min * std::pow(c->p.mass, 3.0 / 2.0);
+  cp.b3 = 0.5 * (b3a + b3a);
   return cp;
 }
 

@@ -38,6 +38,7 @@ struct CollParams {
   double mass, omega, alpha, sigma, dt, Kn, coln_rms, cdf_tolerance;
   double pi;
   uint64_t seed;
+  double b3;           // mass-weighted beta3_min of compute_num_coll_pairs (host-computed)
 };
 
 cudaError_t launch_step_end(uint32_t* counter, long long* acc, const long long* total,

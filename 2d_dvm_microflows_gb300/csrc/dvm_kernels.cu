@@ -36,15 +36,12 @@ constexpr int kCdfChunk = kCdfThreads * kCdfPer;  // nodes per scan chunk
 constexpr int kCdfPitch = kCdfPer + 1;            // padded per-thread row in shared memory
 constexpr int kCdfCoarseMax = 1024;  // entries of the shared-memory coarse index per table
 
-__device__ long long num_coll_pairs(const CollParams& cp, double beta3_min, double densA,
-                                    double densB, double temp) {
-  // compute_num_coll_pairs, collisions/collision_utilities.f90:106-140 (n = m)
+// compute_num_coll_pairs, collisions/collision_utilities.f90:106-140 (n = m); ct is
+// (0.5 (T + T))^(2/3), formed once per cell, and cp.b3 the pair's mass-weighted beta3_min.
+__device__ long long num_coll_pairs(const CollParams& cp, double ct, double densA,
+                                    double densB) {
   const double rms_sq = cp.coln_rms * cp.coln_rms;
-  const double b3a = beta3_min * pow(cp.mass, 3.0 / 2.0);
-  const double b3 = 0.5 * (b3a + b3a);
-  double ct = 0.5 * (temp + temp);
-  ct = pow(ct, 2.0 / 3.0);
-  const double val = (0.5 * cp.dt * ct * densA * densB) / (cp.Kn * rms_sq * b3);
+  const double val = (0.5 * cp.dt * ct * densA * densB) / (cp.Kn * rms_sq * cp.b3);
   if (!(val < 9.0e18)) return 0;
   return llround(val);
 }
@@ -403,8 +400,9 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
           used += nq;
         }
       } else {
+        const double ct = pow(0.5 * (temp + temp), 2.0 / 3.0);
         for (int q = 0; q < 3; ++q)
-          pl.num[q] = (dens > 0.0) ? num_coll_pairs(cp, g.beta3_min, dA[q], dB[q], temp) : 0;
+          pl.num[q] = (dens > 0.0) ? num_coll_pairs(cp, ct, dA[q], dB[q]) : 0;
       }
       for (int q = 0; q < 3; ++q)
         pl.factor[q] = (pl.num[q] > 0)
@@ -417,7 +415,8 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
       long long num;
       if (a.pairs.active) num = a.pairs.count[0];
       else if (cp.samples_mode == DVM_SAMPLES_FIXED) num = (dens > 0.0) ? cp.samples_per_step : 0;
-      else num = (dens > 0.0) ? num_coll_pairs(cp, g.beta3_min, absd / dens, absd / dens, temp) : 0;
+      else num = (dens > 0.0) ? num_coll_pairs(cp, pow(0.5 * (temp + temp), 2.0 / 3.0),
+                                               absd / dens, absd / dens) : 0;
       double factor = (num > 0) ? (cp.dt / cp.Kn) * cp.sigma * absd * absd / static_cast<double>(num)
                                 : 0.0;
       factor = 0.5 * factor;

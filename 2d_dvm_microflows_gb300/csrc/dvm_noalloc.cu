@@ -260,6 +260,10 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   cp.cdf_tolerance = p->cdf_tolerance;
   cp.pi = pi;
   cp.seed = p->seed;
+  {
+    const double b3a = g.beta3_min * std::pow(p->mass, 3.0 / 2.0);
+    cp.b3 = 0.5 * (b3a + b3a);
+  }
 
   CdfArgs ca{};
   ca.g = g; ca.cp = cp; ca.ncells = ncells; ca.f = f; ca.props = props;

@@ -477,7 +477,7 @@ SERVE_RATE = 50.0        # Poisson arrivals per second
 SERVE_MAX_STEPS = 40
 SERVE_TOL = 1e-6
 SERVE_BUDGET = 64 << 30  # admission budget, bytes of HBM
-SERVE_SLOTS = 16
+SERVE_SLOTS = 4   # concurrent requests: enough to overlap small kernels and host gaps
 
 
 def serving_workload(pkg, nreq=SERVE_REQUESTS, seed=SEED):

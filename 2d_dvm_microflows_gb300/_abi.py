@@ -12,7 +12,7 @@ DVM_OK, DVM_ERR_PARAM, DVM_ERR_OOM, DVM_ERR_CUDA, DVM_ERR_NUMERIC, DVM_ERR_TIMEO
     DVM_ERR_NODEVICE, DVM_ERR_TOO_LARGE = range(8)
 
 # device error word bits
-DVM_EW_SEARCH, DVM_EW_REMAP, DVM_EW_NONFINITE, DVM_EW_NEGDENS = 1, 2, 4, 8
+DVM_EW_SEARCH, DVM_EW_REMAP, DVM_EW_NONFINITE, DVM_EW_NEGDENS, DVM_EW_WAIT = 1, 2, 4, 8, 16
 
 # iColl / iConv / geometry
 DVM_COLL_NONE, DVM_COLL_FMC, DVM_COLL_VR = 0, 2, 3

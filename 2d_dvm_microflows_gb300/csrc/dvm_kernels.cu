@@ -132,9 +132,11 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   // chunk staging: node m of a chunk sits at (m / kCdfPer) * kCdfPitch + m % kCdfPer, so
   // global memory is read and written in coalesced rows while each thread scans
   // kCdfPer consecutive nodes
-  extern __shared__ long long s_stage[];  // 2 * kCdfThreads * kCdfPitch
+  extern __shared__ __align__(16) long long s_stage[];  // 2 * kCdfThreads * kCdfPitch, 2 f chunks
   long long* s_e = s_stage;
   long long* s_d = s_stage + kCdfThreads * kCdfPitch;
+  double* s_f = reinterpret_cast<double*>(s_stage + 2 * kCdfThreads * kCdfPitch);
+  __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ long long s_scan[2][128];
   __shared__ double s_par[6];
   __shared__ int s_new, s_k, s_ke;
@@ -224,11 +226,37 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   // uses the scale of the cached equilibrium's density (the cache is renewed whenever
   // the density moves by more than cdf_tolerance, well inside the scale's 16x margin).
   const int kc = vr ? ke : k;
+  // f arrives chunk by chunk in shared memory through bulk asynchronous copies, double
+  // buffered so that the copy of the next chunk overlaps the scan of this one (a cell's
+  // slab is contiguous; the copies need 16-byte alignment, i.e. an even node count)
+  const bool bulk = (nv % 2 == 0);
+  if (bulk && threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_proxy_async();
+    bulk_load(s_f, f, static_cast<uint32_t>(min(kCdfChunk, nv)) * 8u, &s_bar[0]);
+  }
+  __syncthreads();
+  uint32_t parity[2] = {0u, 0u};
+  int chunk_no = 0;
   // (i, j, k) steps of a row of kCdfThreads nodes
   const int NY = g.ny;
   const int st_i = kCdfThreads % NX, st_j = (kCdfThreads / NX) % NY, st_k = kCdfThreads / NXY;
   long long carry_e = 0, carry_d = 0;
-  for (int base = 0; base < nv; base += kCdfChunk) {
+  for (int base = 0; base < nv; base += kCdfChunk, ++chunk_no) {
+    const int buf = chunk_no & 1;
+    const double* fchunk = s_f + buf * kCdfChunk;
+    if (bulk) {
+      if (threadIdx.x == 0 && base + kCdfChunk < nv) {
+        // the other buffer was last read before the barrier that ended the previous chunk
+        fence_proxy_async();
+        bulk_load(s_f + (buf ^ 1) * kCdfChunk, f + base + kCdfChunk,
+                  static_cast<uint32_t>(min(kCdfChunk, nv - base - kCdfChunk)) * 8u,
+                  &s_bar[buf ^ 1]);
+      }
+      if (!mbar_wait(&s_bar[buf], parity[buf])) bad |= DVM_EW_WAIT;
+      parity[buf] ^= 1u;
+    }
     // 1. node terms in coalesced rows: f and f_eq to fixed point, kin, the cached f_eq
     {
       int ii = 0, jj = 0, kk = 0;
@@ -244,7 +272,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
         const int l = base + m;
         long long te = 0, td = 0;
         if (l < nv) {
-          const double fv = f[l];
+          const double fv = bulk ? fchunk[m] : f[l];
           const long long F = to_fixed_s(fv, kc, bad);
           if (vr) {
             long long E;
@@ -428,7 +456,8 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
 }
 
 cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
-  constexpr int smem = 2 * kCdfThreads * kCdfPitch * static_cast<int>(sizeof(long long));
+  constexpr int smem = 2 * kCdfThreads * kCdfPitch * static_cast<int>(sizeof(long long)) +
+                       2 * kCdfChunk * static_cast<int>(sizeof(double));
   const cudaError_t e = cudaFuncSetAttribute(k_cdf, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   k_cdf<<<a.ncells, kCdfThreads, smem, s>>>(a);

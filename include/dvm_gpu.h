@@ -48,7 +48,8 @@ enum {
   DVM_EW_SEARCH = 1,      /* CDF inversion left its bucket (reference would loop)    */
   DVM_EW_REMAP = 2,       /* remap found no exterior node (remapping.f90:348 stops)  */
   DVM_EW_NONFINITE = 4,   /* non-finite moment                                       */
-  DVM_EW_NEGDENS = 8      /* non-positive cell density                               */
+  DVM_EW_NEGDENS = 8,     /* non-positive cell density                               */
+  DVM_EW_WAIT = 16        /* a bounded device wait (bulk copy barrier) ran out       */
 };
 
 /* iColl (collisions/collision_integral.f90:35-38) */

@@ -1987,14 +1987,15 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
 
-__global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
+// The moments of one cell, for the block; src.begin(col) opens an (i, j) column and
+// src.value(k) returns the value of its node k as a pair.
+template <class Src>
+__device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, Src& src) {
   __shared__ float2 s_red[kMomAcc * 32];
   __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
   __shared__ dfl s_z[3 * kMaxAxis];   // z', z'^2, z'^3
   const GridInfo& g = a.g;
-  const int cell = blockIdx.x;
-  const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
-  const double* f = a.f + static_cast<size_t>(cell) * nv;
+  const int NX = g.nx, NXY = g.nx * g.ny, NZ = g.nz;
   double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
   const double u0 = isfinite(P[DVM_P_U]) ? P[DVM_P_U] : 0.0;
   const double v0 = isfinite(P[DVM_P_V]) ? P[DVM_P_V] : 0.0;
@@ -2025,10 +2026,11 @@ __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
   for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
     dacc G0, G1, G2, G3, S;
     dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
+    src.begin(col);
 #pragma unroll 4
     for (int k = 0; k < NZ; ++k) {
       const int l = col + NXY * k;
-      const dfl fv = dfl_from_double(f[l]);
+      const dfl fv = src.value(k);
       dacc_add(G0, fv);
       dacc_fma(G1, fv, s_z[k]);
       dacc_fma(G2, fv, s_z[kMaxAxis + k]);
@@ -2069,7 +2071,7 @@ __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
     const double n = acc[0];
     if (n == 0.0) {
       for (int q = 0; q < DVM_NPROP; ++q) P[q] = 0.0;
-      return;
+      return;  // (thread 0, after the block reduction)
     }
     const double m = a.mass;
     const double dx = acc[1] / n, dy = acc[2] / n, dz = acc[3] / n;
@@ -2129,8 +2131,32 @@ __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
   }
 }
 
+// Threads per moments CTA: the columns split into the fewest rounds of at most kMomThreads,
+// each round a whole number of warps (576 columns of a 24^3 grid: 3 rounds of 192, no
+// idle tail round).
+static int moment_threads(const GridInfo& g) {
+  const int cols = g.nx * g.ny;
+  const int rounds = (cols + kMomThreads - 1) / kMomThreads;
+  const int per = (cols + rounds - 1) / rounds;
+  return ((per + 31) / 32) * 32;
+}
+
+// Node values straight from f.
+struct MomSourceF {
+  const double* f;
+  int NXY, col;
+  __device__ void begin(int c) { col = c; }
+  __device__ dfl value(int k) const { return dfl_from_double(f[col + NXY * k]); }
+};
+
+__global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
+  const int cell = blockIdx.x;
+  MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
+  moments_of_cell(a, cell, src);
+}
+
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
-  k_moments<<<a.ncells, kMomThreads, 0, s>>>(a);
+  k_moments<<<a.ncells, moment_threads(a.g), 0, s>>>(a);
   return cudaGetLastError();
 }
 

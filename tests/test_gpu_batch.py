@@ -36,7 +36,11 @@ def test_batch_matches_grouped_contexts(gpulib, pkg, prec):
     batch = pkg.DVMBatch(_cfg(pkg, prec), grids, gid, samples)
     for i, f in enumerate(f0):
         batch.upload_f(i, f)
-    batch.step(3)
+    # FP32 atomics round in arrival order, so two runs differ at FP32 rounding after one step;
+    # from the second step on such differences can move a sample across a CDF boundary and
+    # the runs decorrelate, so the FP32 form is compared after one step
+    nsteps = 3 if prec == pkg.DVM_PREC_FP64 else 1
+    batch.step(nsteps)
     pb = batch.properties()
     for q, g in enumerate(grids):
         members = np.flatnonzero(gid == q)
@@ -46,7 +50,7 @@ def test_batch_matches_grouped_contexts(gpulib, pkg, prec):
         cfg.samples_per_step = samples[q]
         s = pkg.DVMSolver(cfg, g)
         s.initialize_dist_func(np.stack([f0[i] for i in members]))
-        s.solve(3)
+        s.solve(nsteps)
         ps, fs = s.properties(), s.phi()
         # FP64 scatters in FP64 atomics (order effects at round-off); the FP32 form's FP32
         # atomics round in arrival order, so two runs agree to FP32 rounding of the increment

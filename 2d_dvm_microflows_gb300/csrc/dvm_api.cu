@@ -33,7 +33,6 @@ struct dvm_ctx {
   double* d_f = nullptr;
   double* d_fconv = nullptr;
   double* d_props = nullptr;
-  double* d_eq_pre = nullptr;
   double* d_eq_cache = nullptr;
   long long* d_cum_eq = nullptr;   // fixed-point CDFs
   long long* d_cum_dev = nullptr;
@@ -184,7 +183,7 @@ void release(dvm_ctx* c) {
   if (!c) return;
   harvest(c);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
-  void* bufs[] = {c->d_axes, c->d_speed, c->d_f, c->d_fconv, c->d_props, c->d_eq_pre, c->d_eq_cache,
+  void* bufs[] = {c->d_axes, c->d_speed, c->d_f, c->d_fconv, c->d_props, c->d_eq_cache,
                   c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
                   c->d_axis_tab, c->d_gtab, c->d_trig, c->d_df, c->d_axis_tab_f,
@@ -477,7 +476,7 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
     return st;
   }
   if (params->coll_method != DVM_COLL_NONE) {
-    if ((st = dalloc(c, &c->d_eq_pre, C * (nv + 1))) || (st = dalloc(c, &c->d_eq_cache, C * 4)) ||
+    if ((st = dalloc(c, &c->d_eq_cache, C * kEqCache)) ||
         (st = dalloc(c, &c->d_cum_eq, C * (nv + 1))) || (st = dalloc(c, &c->d_cum_dev, C * (nv + 1))) ||
         (st = dalloc(c, &c->d_kin, C * (nv + 1))) || (st = dalloc(c, &c->d_ref_eq, C * kNRef)) ||
         (st = dalloc(c, &c->d_ref_dev, C * kNRef)) || (st = dalloc(c, &c->d_plan, C)) ||
@@ -524,10 +523,7 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
   cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream);
   cudaMemsetAsync(c->d_f, 0, C * nv * sizeof(double), c->stream);
   cudaMemsetAsync(c->d_props, 0, C * DVM_NPROP * sizeof(double), c->stream);
-  if (c->d_eq_pre) {
-    cudaMemsetAsync(c->d_eq_pre, 0, C * (nv + 1) * sizeof(double), c->stream);
-    cudaMemsetAsync(c->d_eq_cache, 0, C * 4 * sizeof(double), c->stream);
-  }
+  if (c->d_eq_cache) cudaMemsetAsync(c->d_eq_cache, 0, C * kEqCache * sizeof(double), c->stream);
   // 2-D wall ghost entries: left/right walls (if walls), bottom and top (always walls)
   if (params->geometry == DVM_GEOM_2D && params->conv_method == DVM_CONV_UPWIND1) {
     int n = 0;
@@ -678,7 +674,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
   if (!st) {
     CdfArgs ca{};
     ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
-    ca.f = c->d_f; ca.props = c->d_props; ca.eq_pre = reinterpret_cast<long long*>(c->d_eq_pre); ca.eq_cache = c->d_eq_cache;
+    ca.f = c->d_f; ca.props = c->d_props; ca.eq_cache = c->d_eq_cache;
     ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
     ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan;
     ca.pairs = pd; ca.err = c->d_err;
@@ -858,7 +854,7 @@ int dvm_get_residual(dvm_ctx* c, double* residual) {
 // a step reads is rebuilt within the step.
 namespace {
 struct CkptHeader {
-  char magic[8];        // "DVMCKPT1"
+  char magic[8];        // "DVMCKPT2"
   uint64_t ntime;
   int32_t ncells, nv, geometry, coll_method, precision, nprop;
   uint64_t bytes;
@@ -875,8 +871,7 @@ int ckpt_parts(dvm_ctx* c, CkptPart (&parts)[6]) {
   parts[n++] = {c->d_f, C * nv * sizeof(double)};
   parts[n++] = {c->d_props, C * DVM_NPROP * sizeof(double)};
   if (c->p.coll_method != DVM_COLL_NONE) {
-    parts[n++] = {c->d_eq_cache, C * 4 * sizeof(double)};
-    parts[n++] = {c->d_eq_pre, C * (nv + 1) * sizeof(long long)};
+    parts[n++] = {c->d_eq_cache, C * kEqCache * sizeof(double)};
     parts[n++] = {c->d_cum_eq, C * (nv + 1) * sizeof(long long)};
     parts[n++] = {c->d_ref_eq, C * kNRef * sizeof(int2)};
   }
@@ -900,7 +895,7 @@ int dvm_checkpoint_save(dvm_ctx* c, uint64_t ntime, void* buf, uint64_t bytes) {
   uint64_t need = 0;
   if (!c || !buf || dvm_checkpoint_size(c, &need) || bytes < need) return DVM_ERR_PARAM;
   CkptHeader h{};
-  std::memcpy(h.magic, "DVMCKPT1", 8);
+  std::memcpy(h.magic, "DVMCKPT2", 8);
   h.ntime = ntime;
   h.ncells = c->ncells; h.nv = c->g.nv; h.geometry = c->p.geometry;
   h.coll_method = c->p.coll_method; h.precision = c->p.precision; h.nprop = DVM_NPROP;
@@ -924,7 +919,7 @@ int dvm_checkpoint_load(dvm_ctx* c, const void* buf, uint64_t bytes, uint64_t* n
   if (!c || !buf || dvm_checkpoint_size(c, &need) || bytes < need) return DVM_ERR_PARAM;
   CkptHeader h;
   std::memcpy(&h, buf, sizeof(h));
-  if (std::memcmp(h.magic, "DVMCKPT1", 8) != 0 || h.bytes != need || h.ncells != c->ncells ||
+  if (std::memcmp(h.magic, "DVMCKPT2", 8) != 0 || h.bytes != need || h.ncells != c->ncells ||
       h.nv != c->g.nv || h.geometry != c->p.geometry || h.coll_method != c->p.coll_method ||
       h.nprop != DVM_NPROP)
     return DVM_ERR_PARAM;
@@ -1012,7 +1007,7 @@ int autotune(dvm_batch* b) {
     // 0-D contexts never use f_conv: it holds the saved f
     int st = cuda_status(cudaMemcpyAsync(c->d_fconv, c->d_f, bytes, cudaMemcpyDeviceToDevice,
                                          c->stream));
-    std::vector<double> cache(static_cast<size_t>(c->ncells) * 4);
+    std::vector<double> cache(static_cast<size_t>(c->ncells) * kEqCache);
     if (!st && c->d_eq_cache)
       st = cuda_status(cudaMemcpyAsync(cache.data(), c->d_eq_cache, cache.size() * sizeof(double),
                                        cudaMemcpyDeviceToHost, c->stream));
@@ -1109,8 +1104,8 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
              + sizeof(uint32_t) + nv * sizeof(float2)       // error word, speeds
              + sizeof(unsigned long long);                  // residual
   if (p->coll_method != DVM_COLL_NONE) {
-    b += 3 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float) + C * 4 * d;  // eq_pre, cum_eq,
-                                                            // cum_dev, kin, cache
+    b += 2 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float)  // cum_eq, cum_dev, kin,
+         + C * kEqCache * d;                                  // equilibrium cache
     b += 2 * C * kNRef * sizeof(int2) + C * sizeof(CellPlan) +
          (3 * C + 1) * sizeof(long long) + sizeof(long long);
     const size_t nmax = std::max(vg->nx, std::max(vg->ny, vg->nz));

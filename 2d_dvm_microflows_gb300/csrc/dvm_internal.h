@@ -44,14 +44,17 @@ struct CollParams {
 cudaError_t launch_step_end(uint32_t* counter, long long* acc, const long long* total,
                             cudaStream_t s);
 
+// Moments kept per cell for the equilibrium cache of k_cdf: dens, u, v, temp (the
+// renewal test) and w (the cached equilibrium was built with it).
+constexpr int kEqCache = 5;
+
 struct CdfArgs {
   GridInfo g;
   CollParams cp;
   int ncells;
   const double* f;          // [C][nv]
   const double* props;      // [C][DVM_NPROP]
-  long long* eq_pre;        // [C][nv+1] cached equilibrium, fixed point, one value per node
-  double* eq_cache;         // [C][4]  dens, u, v, temp of the cached equilibrium
+  double* eq_cache;         // [C][kEqCache] dens, u, v, temp, w of the cached equilibrium
   long long* cum_eq;        // [C][nv+1] cumulative f_eq, fixed point (see k_cdf)
   long long* cum_dev;       // [C][nv+1] cumulative |f - f_eq| (FMC: |f|), fixed point
   float* kin;               // [C][nv+1] (VR: f - f_eq; FMC: f), read for its sign

@@ -31,10 +31,10 @@ namespace dvm {
 // bit for bit; the quantum 2^-k is below 1e-17 n, finer than the FP64 rounding of the
 // reference's running sum. The partner search (k_collide) then compares integers only.
 constexpr int kCdfThreads = 256;
-constexpr int kCdfPer = 8;
+constexpr int kCdfPer = 4;
 constexpr int kCdfChunk = kCdfThreads * kCdfPer;  // nodes per scan chunk
 constexpr int kCdfPitch = kCdfPer + 1;            // padded per-thread row in shared memory
-constexpr int kCdfCoarseMax = 1024;  // entries of the shared-memory coarse index per table
+constexpr int kCdfCoarseMax = 512;   // entries of the shared-memory coarse index per table
 
 // compute_num_coll_pairs, collisions/collision_utilities.f90:106-140 (n = m); ct is
 // (0.5 (T + T))^(2/3), formed once per cell, and cp.b3 the pair's mass-weighted beta3_min.
@@ -136,11 +136,14 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   long long* s_e = s_stage;
   long long* s_d = s_stage + kCdfThreads * kCdfPitch;
   double* s_f = reinterpret_cast<double*>(s_stage + 2 * kCdfThreads * kCdfPitch);
+  // the bucket tables are built after the scan, in the staging rows it no longer needs
+  int (*s_right)[kNRef] = reinterpret_cast<int (*)[kNRef]>(s_stage);
+  static_assert(2 * kNRef * sizeof(int) <= 2 * kCdfThreads * kCdfPitch * sizeof(long long),
+                "bucket tables must fit in the staging rows");
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ long long s_scan[2][128];
   __shared__ double s_par[6];
   __shared__ int s_new, s_k, s_ke;
-  __shared__ int s_right[2][kNRef];
   __shared__ dfl s_fac[3 * kMaxAxis];
   __shared__ long long s_coarse[2][kCdfCoarseMax + 1];
   const GridInfo& g = a.g;
@@ -149,7 +152,6 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
   const double* f = a.f + static_cast<size_t>(cell) * nv;
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
-  long long* eq = a.eq_pre + cs;  // cached equilibrium, fixed point, one value per node
   long long* ce = a.cum_eq + cs;
   long long* cd = a.cum_dev + cs;
   float* kin = a.kin + cs;
@@ -173,23 +175,27 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
       const double dens = P[DVM_P_DENS], u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
       double temp = P[DVM_P_SPECIES_TEMP];
       if (temp < kDoubleTol) temp = P[DVM_P_TEMP];
-      const double mc = (dens > 0.0) ? dens * maxwell_coeff(a.cp.mass, temp, a.cp.pi) : 0.0;
-      double* cache = a.eq_cache + static_cast<size_t>(cell) * 4;
+      double* cache = a.eq_cache + static_cast<size_t>(cell) * kEqCache;
       const double tol = a.cp.cdf_tolerance;
-      // new_eq_flag, variance_reduction.f90:316-322 (w is neither tested nor stored)
+      // new_eq_flag, variance_reduction.f90:316-322 (w is not tested; it is kept with the
+      // cache because the cached equilibrium was built with it)
       const int nw = (fabs(dens - cache[0]) > tol * dens || fabs(u - cache[1]) > tol * u ||
                       fabs(v - cache[2]) > tol * v || fabs(temp - cache[3]) > tol * temp);
-      if (nw) { cache[0] = dens; cache[1] = u; cache[2] = v; cache[3] = temp; }
+      if (nw) { cache[0] = dens; cache[1] = u; cache[2] = v; cache[3] = temp; cache[4] = w; }
       s_new = nw;
       // the equilibrium CDF keeps the scale of the density it was built for, so a cached
       // one stays valid (with its bucket table) until the cache is renewed
       s_ke = scale(cache[0]);
-      s_par[0] = mc; s_par[1] = u; s_par[2] = v; s_par[3] = w; s_par[4] = temp;
+      // the equilibrium of the cache's moments: on a renewal the current ones; otherwise
+      // the node values are formed again, bit for bit those of the renewal step
+      const double cd = cache[0], ct = cache[3];
+      s_par[0] = (cd > 0.0) ? cd * maxwell_coeff(a.cp.mass, ct, a.cp.pi) : 0.0;
+      s_par[1] = cache[1]; s_par[2] = cache[2]; s_par[3] = cache[4]; s_par[4] = ct;
     }
   }
   __syncthreads();
   const bool recompute = vr && s_new;
-  if (recompute) {
+  if (vr) {
     // the Maxwellian times the node volume factorises over the axes:
     // mc exp(-m|c-u|^2/T) bx by bz = [mc e_x bx] [e_y by] [e_z bz]
     const double mc = s_par[0], temp = s_par[4], m = a.cp.mass;
@@ -221,8 +227,8 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   // in sequence, and the thread sums are scanned across the block (cumul_df of
   // variance_reduction.f90:454-456, full_mc.f90:151-152)
   // The node terms are formed without FP64 instructions: f enters the fixed point from
-  // its bits, f_eq = e_x e_y e_z is a pair product converted once (and cached in fixed
-  // point), and f - f_eq and its magnitude are integer operations. For VR every term
+  // its bits, f_eq = e_x e_y e_z is a pair product converted to fixed point, and f - f_eq
+  // and its magnitude are integer operations. For VR every term
   // uses the scale of the cached equilibrium's density (the cache is renewed whenever
   // the density moves by more than cdf_tolerance, well inside the scale's 16x margin).
   const int kc = vr ? ke : k;
@@ -260,7 +266,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
     // 1. node terms in coalesced rows: f and f_eq to fixed point, kin, the cached f_eq
     {
       int ii = 0, jj = 0, kk = 0;
-      if (recompute) {
+      if (vr) {
         const int l0 = base + threadIdx.x;
         kk = l0 / NXY;
         jj = (l0 - kk * NXY) / NX;
@@ -275,16 +281,10 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
           const double fv = bulk ? fchunk[m] : f[l];
           const long long F = to_fixed_s(fv, kc, bad);
           if (vr) {
-            long long E;
-            if (recompute) {
-              const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
-                                     s_fac[2 * kMaxAxis + kk]);
-              E = to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
-              eq[l] = E;
-              te = E;
-            } else {
-              E = eq[l];
-            }
+            const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
+                                   s_fac[2 * kMaxAxis + kk]);
+            const long long E = to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
+            if (recompute) te = E;
             const long long d = F - E;
             kin[l + 1] = d < 0 ? -1.f : 1.f;
             td = d < 0 ? -d : d;
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
         const int pos = (m / kCdfPer) * kCdfPitch + (m % kCdfPer);
         s_e[pos] = te;
         s_d[pos] = td;
-        if (recompute) {
+        if (vr) {
           ii += st_i; if (ii >= NX) { ii -= NX; ++jj; }
           jj += st_j; if (jj >= NY) { jj -= NY; ++kk; }
           kk += st_k;

@@ -40,7 +40,7 @@ size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
 // Offsets of every buffer inside the scratch array.
 struct Layout {
-  size_t axes, tabs, gtab, trig, eq_pre, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
+  size_t axes, tabs, gtab, trig, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
       chunk_off, total, err, end;
 };
 
@@ -54,8 +54,7 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   L.tabs = o; o = align256(o + 3 * sizeof(AxisEntry) * nmax);
   L.gtab = o; o = align256(o + sizeof(double2) * gtab_n);
   L.trig = o; o = align256(o + sizeof(double2) * kTrigN);
-  L.eq_pre = o; o = align256(o + sizeof(double) * C * nv1);
-  L.eq_cache = o; o = align256(o + sizeof(double) * C * 4);
+  L.eq_cache = o; o = align256(o + sizeof(double) * C * kEqCache);
   L.cum_eq = o; o = align256(o + sizeof(double) * C * nv1);
   L.cum_dev = o; o = align256(o + sizeof(double) * C * nv1);
   L.kin = o; o = align256(o + sizeof(float) * C * nv1);
@@ -246,7 +245,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   // Maxwellian afresh, as a new context's first call does) and the error word
   uint32_t* d_err = reinterpret_cast<uint32_t*>(base + L.err);
   double* d_eq_cache = reinterpret_cast<double*>(base + L.eq_cache);
-  if ((e = cudaMemsetAsync(d_eq_cache, 0, sizeof(double) * 4 * ncells, s)) != cudaSuccess ||
+  if ((e = cudaMemsetAsync(d_eq_cache, 0, sizeof(double) * kEqCache * ncells, s)) != cudaSuccess ||
       (e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s)) != cudaSuccess)
     return status_of(e);
 
@@ -267,7 +266,6 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
 
   CdfArgs ca{};
   ca.g = g; ca.cp = cp; ca.ncells = ncells; ca.f = f; ca.props = props;
-  ca.eq_pre = reinterpret_cast<long long*>(base + L.eq_pre);
   ca.eq_cache = d_eq_cache;
   ca.cum_eq = reinterpret_cast<long long*>(base + L.cum_eq);
   ca.cum_dev = reinterpret_cast<long long*>(base + L.cum_dev);

@@ -229,6 +229,12 @@ class DVMSolver:
         _check(self.lib.dvm_last_collision_count(self.ctx, C.byref(v)), "dvm_last_collision_count")
         return v.value
 
+    def scatter_count(self):
+        """Adds into f counted by the last collision launch (dvm_last_scatter_count)."""
+        v = C.c_int64()
+        _check(self.lib.dvm_last_scatter_count(self.ctx, C.byref(v)), "dvm_last_scatter_count")
+        return v.value
+
     def error_word(self):
         v = C.c_uint32()
         _check(self.lib.dvm_get_error_word(self.ctx, C.byref(v)), "dvm_get_error_word")

@@ -93,6 +93,7 @@ ENTRY_POINTS = {
     "dvm_set_properties": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "dvm_step": (C.c_int, [_P, C.c_uint64, C.c_int]),
     "dvm_last_collision_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "dvm_last_scatter_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "dvm_synchronize": (C.c_int, [_P]),
     "dvm_get_error_word": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "dvm_profile_enable": (C.c_int, [_P, C.c_int]),

@@ -480,7 +480,7 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
         (st = dalloc(c, &c->d_cum_eq, C * (nv + 1))) || (st = dalloc(c, &c->d_cum_dev, C * (nv + 1))) ||
         (st = dalloc(c, &c->d_kin, C * (nv + 1))) || (st = dalloc(c, &c->d_ref_eq, C * kNRef)) ||
         (st = dalloc(c, &c->d_ref_dev, C * kNRef)) || (st = dalloc(c, &c->d_plan, C)) ||
-        (st = dalloc(c, &c->d_chunk_off, 3 * C + 1)) || (st = dalloc(c, &c->d_total_samples, 1))) {
+        (st = dalloc(c, &c->d_chunk_off, 3 * C + 1)) || (st = dalloc(c, &c->d_total_samples, 2))) {
       release(c);
       return st;
     }
@@ -692,7 +692,10 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
     a.chunk_off = c->d_chunk_off; a.pairs = pd; a.err = c->d_err;
-    if (c->p.precision == DVM_PREC_FP32) {
+    // d_total_samples[1]: the adds into f (df) of this call
+    a.scatter_count = reinterpret_cast<unsigned long long*>(c->d_total_samples + 1);
+    st = cuda_status(cudaMemsetAsync(a.scatter_count, 0, sizeof(unsigned long long), c->stream));
+    if (!st && c->p.precision == DVM_PREC_FP32) {
       st = launch(c, DVM_K_COLLIDE, [&] {
         return launch_collide_f32(a, c->tabs_f, c->d_df, c->collide_f32_grid, c->stream);
       });
@@ -700,7 +703,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
         ProjectArgs pa{c->g, c->ncells, c->d_f, c->d_df, c->d_props};
         st = launch(c, DVM_K_PROJECT, [&] { return launch_project(pa, c->stream); });
       }
-    } else {
+    } else if (!st) {
       st = launch(c, DVM_K_COLLIDE, [&] { return launch_collide(a, c->collide_grid, c->stream); });
     }
   }
@@ -771,6 +774,17 @@ int dvm_last_collision_count(dvm_ctx* c, int64_t* count) {
   long long v = 0;
   int st = cuda_status(cudaMemcpyAsync(&v, c->d_total_samples, sizeof(v), cudaMemcpyDeviceToHost,
                                        c->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  *count = v;
+  return st;
+}
+
+int dvm_last_scatter_count(dvm_ctx* c, int64_t* count) {
+  if (!c || !count) return DVM_ERR_PARAM;
+  if (!c->d_total_samples) { *count = 0; return DVM_OK; }
+  long long v = 0;
+  int st = cuda_status(cudaMemcpyAsync(&v, c->d_total_samples + 1, sizeof(v),
+                                       cudaMemcpyDeviceToHost, c->stream));
   if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
   *count = v;
   return st;
@@ -1107,7 +1121,7 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
     b += 2 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float)  // cum_eq, cum_dev, kin,
          + C * kEqCache * d;                                  // equilibrium cache
     b += 2 * C * kNRef * sizeof(int2) + C * sizeof(CellPlan) +
-         (3 * C + 1) * sizeof(long long) + sizeof(long long);
+         (3 * C + 1) * sizeof(long long) + 2 * sizeof(long long);
     const size_t nmax = std::max(vg->nx, std::max(vg->ny, vg->nz));
     b += 3 * nmax * sizeof(AxisEntry) + kTrigN * sizeof(double2);
     const bool cubic = (vg->nx == vg->ny && vg->ny == vg->nz);

@@ -130,6 +130,7 @@ struct CollideArgs {
   const long long* chunk_off;  // [3*C + 1]
   PairDev pairs;
   uint32_t* err;
+  unsigned long long* scatter_count;  // if set, the adds into f (df) are counted here
 };
 
 // 2-D wall ghost slabs: one per (wall side, position along the wall).

@@ -678,7 +678,7 @@ __device__ __forceinline__ void axis_terms(const SmemAxesD& A, int ax, int o, in
 __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAxesD& A, dfl u,
                                                  dfl v, dfl w, float xmin, float ymin,
                                                  float zmin, float xfac, float yfac, float zfac,
-                                                 double* f, dfl w8) {
+                                                 double* f, dfl w8, uint32_t& nat) {
   int corner = 0, bad = 0;
   int o_i = nearest_d(A, 0, u, xmin, xfac, corner, bad);
   int o_j = nearest_d(A, 1, v, ymin, yfac, corner, bad);
@@ -727,6 +727,7 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
     f_e = dfl_div(num, den);
   }
   if (bad & 2) return bad;
+  nat += 4u + static_cast<uint32_t>(fx + fy + fz);
   // weights and their contributions w * mass, scattered as they are formed (the centre
   // node takes 1 - the others, as in the reference)
   const int NX = g.nx, NXY = g.nx * g.ny;
@@ -762,6 +763,15 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
   atomicAdd(f + base, dfl_to_double_normal(dfl_mul(w8, f_o)));
   return bad;
+}
+
+// Adds a warp's scatter counts to the launch total (every thread of the block calls it).
+__device__ __forceinline__ void add_scatter_count(unsigned long long* total, uint32_t n) {
+  if (!total) return;
+  unsigned long long v = n;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(total, v);
 }
 
 // t = R - k/kTrigN (k = the top 10 bits of R) as a pair, and k, from the bits of R in [0, 1).
@@ -870,6 +880,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   const bool vss = fabs(ralpha - 1.0) > kDoubleTol;
   const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
+  uint32_t nat = 0;  // FP64 adds into f by this thread
 
   // one warp per chunk; chunks are visited in a scattered order (a bijection of
   // 0..total-1), so the warps in flight at any moment work on many cells and their FP64
@@ -938,6 +949,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
     const double kin = (negA != negB) ? -fg : fg;
     atomicAdd(f + lA, -kin);
     atomicAdd(f + lB, -kin);
+    nat += 2u;
     // replenish_collision elastic branch (replenishing_collisions.f90:206-249)
     dfl kr;
     {
@@ -1018,16 +1030,17 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
         uz = dfl_mul(hg, ct);
       }
       int rb = remap_scatter_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
-                                 xmin, ymin, zmin, xfac, yfac, zfac, f, kr);
+                                 xmin, ymin, zmin, xfac, yfac, zfac, f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
       rb = remap_scatter_dfl(g, A, dfl_sub(vc0, ux), dfl_sub(vc1, uy), dfl_sub(vc2, uz), xmin,
-                             ymin, zmin, xfac, yfac, zfac, f, kr);
+                             ymin, zmin, xfac, yfac, zfac, f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
   }
   if (bad) atomicOr(a.err, bad);
+  add_scatter_count(a.scatter_count, nat);
 }
 
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
@@ -1274,7 +1287,8 @@ __device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const Co
 // One sample of sub-integral q of a cell in FP32, scattered into df (global or shared).
 __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const CollTablesF& tf,
                                                    const F32Ctx& c, int cell, int q, long long i,
-                                                   float factor, float* df, uint32_t& bad) {
+                                                   float factor, float* df, uint32_t& bad,
+                                                   uint32_t& nat) {
   const GridInfo& g = a.g;
   const SmemAxesF& A = c.A;
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
@@ -1321,6 +1335,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   const float kin = sA * sB * factor * g_sigma;
   atomicAdd(df + lA, -kin);
   atomicAdd(df + lB, -kin);
+  nat += 2u;
   const int NR = c.NR;
   const float kr = kin / static_cast<float>(NR);
   const float vc0 = 0.5f * (xA + xB), vc1 = 0.5f * (yA + yB), vc2 = 0.5f * (zA + zB);
@@ -1380,14 +1395,14 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
     else {
 #pragma unroll
       for (int m = 0; m < 7; ++m)
-        if (sA_.node[m] >= 0) atomicAdd(df + sA_.node[m], kr * sA_.mass[m]);
+        if (sA_.node[m] >= 0) { atomicAdd(df + sA_.node[m], kr * sA_.mass[m]); ++nat; }
     }
     rb = remap_f32(g, A, vc0 - ux, vc1 - uy, vc2 - uz, sB_);
     if (rb & 2) bad |= DVM_EW_REMAP;
     else {
 #pragma unroll
       for (int m = 0; m < 7; ++m)
-        if (sB_.node[m] >= 0) atomicAdd(df + sB_.node[m], kr * sB_.mass[m]);
+        if (sB_.node[m] >= 0) { atomicAdd(df + sB_.node[m], kr * sB_.mass[m]); ++nat; }
     }
   }
 }
@@ -1401,6 +1416,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   const int nent = 3 * a.ncells;
   const long long total = a.chunk_off[nent];
   uint32_t bad = 0;
+  uint32_t nat = 0;  // FP32 adds into df by this thread
   const int wpb = blockDim.x >> 5;
   for (long long pos = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
        pos < total; pos += static_cast<long long>(gridDim.x) * wpb) {
@@ -1416,9 +1432,10 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
     const long long i = (chunk - a.chunk_off[lo]) * kChunkSamples + (threadIdx.x & 31);
     if (i >= pl.num[q]) continue;
     collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
-                       dfs + static_cast<size_t>(cell) * nv, bad);
+                       dfs + static_cast<size_t>(cell) * nv, bad, nat);
   }
   if (bad) atomicOr(a.err, bad);
+  add_scatter_count(a.scatter_count, nat);
 }
 
 int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {

@@ -645,7 +645,7 @@ def run_gpu(args):
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if ws > 1 else 0)
     dist_barrier(dist)
     clocks.start()
-    t_dev, colls = 0.0, 0
+    t_dev, colls, scat = 0.0, 0, 0
     for _ in range(args.steps):
         s.profile(False)
         s.flush_l2()
@@ -653,6 +653,7 @@ def run_gpu(args):
         s.profile(True)
         t_dev += s.time_steps(1)
         colls += s.collision_count()
+        scat += s.scatter_count()
     s.synchronize()
     clk = clocks.stop()
     prof = s.profile_read()
@@ -702,7 +703,9 @@ def run_gpu(args):
     # the collide kernel's scatter is FP64 atomics into an L2-resident f: its second
     # roofline is the measured atomic rate over a window the size of f
     atom_peak = s.atomic_rate(NCELLS * nv * 8)
-    atom_achieved = samples_per_launch * ATOMICS_PER_SAMPLE / t_launch
+    # adds per launch as counted by the kernel itself (dvm_last_scatter_count)
+    atom_per_sample = scat / max(colls, 1)
+    atom_achieved = scat / max(args.steps, 1) / t_launch
     line = {
         "metric": "MC collisions/s", "value": value, "unit": "collisions/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
@@ -715,7 +718,9 @@ def run_gpu(args):
                      "algorithmic_bytes_per_sample": BYTES_PER_SAMPLE},
         "roofline_atomic": {"kernel": "collide", "achieved": atom_achieved, "peak": atom_peak,
                             "unit": "FP64 atomic adds/s", "frac": atom_achieved / atom_peak,
-                            "atomics_per_sample": ATOMICS_PER_SAMPLE,
+                            "atomics_per_sample": atom_per_sample,
+                            "atomics_per_sample_source": "counted by the collide kernel",
+                            "atomics_per_sample_nominal": ATOMICS_PER_SAMPLE,
                             "peak_source": "measured in this run (dvm_atomic_rate, pseudo-"
                                            "random adds over a window the size of f)"},
         "kernels": kernels,

@@ -188,6 +188,12 @@ int dvm_set_properties(dvm_ctx* ctx, const double* props);
 int dvm_step(dvm_ctx* ctx, uint64_t first_step, int nsteps);
 /* Collision samples drawn by the last collision call, summed over cells (tot_colls). */
 int dvm_last_collision_count(dvm_ctx* ctx, int64_t* count);
+/* Scatter adds into f made by the last collision call, counted by the collide kernel: two
+ * depletions per sample plus the written stencil nodes of each replenishment (4 to 7;
+ * replenishing_collisions.f90:356-434). FP32 adds into the increment in the precision
+ * form. Divided by the collision count, it is the atomics per sample behind the kernel's
+ * atomic roofline. */
+int dvm_last_scatter_count(dvm_ctx* ctx, int64_t* count);
 
 /* Convergence residual of the last dvm_calculate_physical_properties: the largest, over
  * cells, relative change of n, u (on the thermal speed), T and the stress tensor (on the

@@ -326,6 +326,11 @@ static void scatter_stencil(const orc_grid* g, double* f, const int* st, const d
 #undef IDX
 }
 
+/* nodes scatter_stencil writes: the centre, three interior and the available exterior ones */
+static int stencil_size(const int* st) {
+  return 4 + (st[6] & 1) + ((st[6] >> 1) & 1) + ((st[6] >> 2) & 1);
+}
+
 int orc_remap_grid(const dvm_vgrid* vg, double u, double v, double w, double f_off, int* st,
                    double* mass) {
   orc_grid g;
@@ -402,6 +407,7 @@ typedef struct {
   double *eq_pre;   /* [C][nv+1] */
   double *cache;    /* [C][4] dens, u, v, temp */
   int64_t colls_last;
+  int64_t scatter_last;  /* adds into f by the last collision call (depletion + stencils) */
   uint32_t err;
   int nthreads;
 } orc_ctx;
@@ -468,6 +474,7 @@ void orc_set_props(orc_ctx* c, const double* p) {
   memcpy(c->props, p, sizeof(double) * (size_t)c->ncells * DVM_NPROP);
 }
 int64_t orc_last_collision_count(const orc_ctx* c) { return c->colls_last; }
+int64_t orc_last_scatter_count(const orc_ctx* c) { return c->scatter_last; }
 uint32_t orc_error_word(orc_ctx* c) { uint32_t w = c->err; c->err = 0; return w; }
 void orc_grid_info(const orc_ctx* c, double* beta3_min, int* zero_info) {
   *beta3_min = c->g.beta3_min;
@@ -590,7 +597,7 @@ static void fixed_split(int64_t S, const double* w, int nsub, long long* out) {
  * (replenishing_collisions.f90:134-354) + apply_phi_replenishment (:356-434). */
 static void collide_sample(orc_ctx* c, double* f, int lA, int lB, double sA, double sB,
                            double factor, const double* r_phi, const double* r_cos,
-                           uint32_t* bad) {
+                           uint32_t* bad, int64_t* nsc) {
   const orc_grid* g = &c->g;
   const int NX = g->nx, NXY = g->nx * g->ny;
   const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
@@ -608,6 +615,7 @@ static void collide_sample(orc_ctx* c, double* f, int lA, int lB, double sA, dou
   const double kin1 = sA * depl1, kin2 = sB * depl2;
   f[lA] = f[lA] - kin1;
   f[lB] = f[lB] - kin2;
+  *nsc += 2;
   /* replenish_collision :206-249 */
   const int NR = c->p.num_repl;
   const double kr1 = kin1 / (double)NR, kr2 = kin2 / (double)NR;
@@ -657,10 +665,12 @@ static void collide_sample(orc_ctx* c, double* f, int lA, int lB, double sA, dou
     int st[7];
     double ms[7];
     int rb = remap(g, xi0, xi1, xi2, 1.0, st, ms);
-    if (rb & 2) *bad |= DVM_EW_REMAP; else scatter_stencil(g, f, st, ms, kr1);
+    if (rb & 2) *bad |= DVM_EW_REMAP;
+    else { scatter_stencil(g, f, st, ms, kr1); *nsc += stencil_size(st); }
     if (rb & 1) *bad |= DVM_EW_SEARCH;
     rb = remap(g, et0, et1, et2, 1.0, st, ms);
-    if (rb & 2) *bad |= DVM_EW_REMAP; else scatter_stencil(g, f, st, ms, kr2);
+    if (rb & 2) *bad |= DVM_EW_REMAP;
+    else { scatter_stencil(g, f, st, ms, kr2); *nsc += stencil_size(st); }
     if (rb & 1) *bad |= DVM_EW_SEARCH;
     (void)NX;
   }
@@ -728,7 +738,7 @@ static void cdf_vr(orc_ctx* c, int cell, const double* f, orc_cellscratch* s) {
 
 /* variance_reduction_kernel (variance_reduction.f90:498-1125) for one cell, n = m = 1. */
 static int64_t vr_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist* pl,
-                       orc_cellscratch* s, uint32_t* bad) {
+                       orc_cellscratch* s, uint32_t* bad, int64_t* nsc) {
   const orc_grid* g = &c->g;
   double* f = c->f + (size_t)cell * g->nv;
   cdf_vr(c, cell, f, s);
@@ -773,7 +783,7 @@ static int64_t vr_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist* 
       *bad |= (uint32_t)sb;
       const double sA = (q == 0) ? 1.0 : s->sgn[lA + 1];
       const double sB = (q == 1) ? 1.0 : s->sgn[lB + 1];
-      collide_sample(c, f, lA, lB, sA, sB, factor, rphi, rcos, bad);
+      collide_sample(c, f, lA, lB, sA, sB, factor, rphi, rcos, bad, nsc);
     }
   }
   return tot;
@@ -781,7 +791,7 @@ static int64_t vr_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist* 
 
 /* full_monte_carlo_kernel (full_mc.f90:182-682) with compute_cdf_fmc (:110-180), one cell. */
 static int64_t fmc_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist* pl,
-                        orc_cellscratch* s, uint32_t* bad) {
+                        orc_cellscratch* s, uint32_t* bad, int64_t* nsc) {
   const orc_grid* g = &c->g;
   double* f = c->f + (size_t)cell * g->nv;
   s->cum_abs[0] = 0.0; s->sgn[0] = 1.0;
@@ -817,7 +827,7 @@ static int64_t fmc_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist*
     /* kin_depl = depl_adj*depl_frac(1)*factor*g_sigma = sA*sB*factor*g_sigma; the
      * shared sample routine forms the same value as sA*(sB*factor*g_sigma). */
     (void)adj;
-    collide_sample(c, f, lA, lB, sA, sB, factor, rphi, rcos, bad);
+    collide_sample(c, f, lA, lB, sA, sB, factor, rphi, rcos, bad, nsc);
   }
   return num;
 }
@@ -826,22 +836,23 @@ static int64_t fmc_cell(orc_ctx* c, int cell, uint64_t step, const dvm_pairlist*
  * contributions are added to f in place (the monatomic sampling reads only the CDFs built
  * at the start of the cell-step, so delta_phi = phi + sum(contributions) is the same). */
 int orc_compute_collision_integral(orc_ctx* c, uint64_t step, const dvm_pairlist* pl) {
-  if (c->p.coll_method == DVM_COLL_NONE) { c->colls_last = 0; return DVM_OK; }
+  if (c->p.coll_method == DVM_COLL_NONE) { c->colls_last = 0; c->scatter_last = 0; return DVM_OK; }
   if (c->p.num_repl < 1 || c->p.num_repl > 16) return DVM_ERR_PARAM;
-  int64_t total = 0;
+  int64_t total = 0, nsc = 0;
   uint32_t bad = 0;
-#pragma omp parallel num_threads(c->nthreads) reduction(+ : total) reduction(| : bad)
+#pragma omp parallel num_threads(c->nthreads) reduction(+ : total, nsc) reduction(| : bad)
   {
     orc_cellscratch s;
     scratch_alloc(&s, c->g.nv);
 #pragma omp for schedule(dynamic, 1)
     for (int cell = 0; cell < c->ncells; ++cell) {
-      if (c->p.coll_method == DVM_COLL_VR) total += vr_cell(c, cell, step, pl, &s, &bad);
-      else total += fmc_cell(c, cell, step, pl, &s, &bad);
+      if (c->p.coll_method == DVM_COLL_VR) total += vr_cell(c, cell, step, pl, &s, &bad, &nsc);
+      else total += fmc_cell(c, cell, step, pl, &s, &bad, &nsc);
     }
     scratch_free(&s);
   }
   c->colls_last = total;
+  c->scatter_last = nsc;
   c->err |= bad;
   return DVM_OK;
 }

@@ -47,6 +47,7 @@ def lib():
             "orc_compute_convection": (C.c_int, [P]),
             "orc_step": (C.c_int, [P, C.c_uint64, C.c_int]),
             "orc_last_collision_count": (C.c_int64, [P]),
+            "orc_last_scatter_count": (C.c_int64, [P]),
             "orc_error_word": (C.c_uint32, [P]),
             "orc_grid_info": (None, [P, D, I]),
             "orc_remap_grid": (C.c_int, [C.POINTER(abi.dvm_vgrid), C.c_double, C.c_double,
@@ -147,6 +148,11 @@ class OracleSolver:
 
     def collision_count(self):
         return int(self.L.orc_last_collision_count(self.ctx))
+
+    def scatter_count(self):
+        """Adds into f by the last collision call: 2 depletions per sample plus the stencil
+        nodes of each replenishment."""
+        return int(self.L.orc_last_scatter_count(self.ctx))
 
     def error_word(self):
         return int(self.L.orc_error_word(self.ctx))

@@ -85,6 +85,8 @@ def test_vr_pairlist_step(gpulib, pkg, oracle, nodes, grid_n):
     gpu.compute_collision_integral(0, pkg.PairList(subs))
     cpu.compute_collision_integral(0, pkg.PairList(subs))
     assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    # the kernel's own count of its adds into f: 2 per sample plus the stencil nodes
+    assert gpu.scatter_count() == cpu.scatter_count() > 0
     assert gpu.error_word() == 0
 
 
@@ -104,6 +106,7 @@ def test_philox_steps(gpulib, pkg, oracle, method, model):
         gpu.solve(1)
         cpu.solve(1)
         assert rel_err(gpu.phi(), cpu.phi()) <= REL
+        assert gpu.scatter_count() == cpu.scatter_count()
     assert gpu.collision_count() == cpu.collision_count()
     assert props_err(gpu.properties(), cpu.properties()) <= 1e-11
     assert gpu.error_word() == 0
@@ -338,5 +341,8 @@ def test_philox_steps_larger_grid(gpulib, pkg, oracle, method):
         gpu.solve(1)
         cpu.solve(1)
         assert rel_err(gpu.phi(), cpu.phi()) <= REL
-    assert gpu.collision_count() == cpu.collision_count()
+        assert gpu.scatter_count() == cpu.scatter_count()
+    n = gpu.collision_count()
+    assert n == cpu.collision_count()
+    assert 10 * 0.9 * n <= gpu.scatter_count() <= 16 * n
     assert gpu.error_word() == 0

@@ -138,3 +138,22 @@ def test_fp32_one_step_error_grid_sizes(gpulib, pkg, n):
     err = moment_errors(p32, p64)
     assert err.max() <= 1e-6, dict(zip(pkg.PROP_NAMES, err))
     assert abs(p32[0, 0] - p64[0, 0]) <= 1e-12 and e32 == 0
+
+
+def test_fp32_scatter_count_matches_fp64(gpulib, pkg):
+    """Both forms draw the same partners from the same Philox words, so the kernels' own
+    counts of their adds agree (the FP32 stencil can differ only for a velocity within FP32
+    rounding of a node midpoint)."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(16, -5.0, 5.0)
+    counts = []
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        s = pkg.DVMSolver(pkg.DVMConfig(precision=prec, iColl=pkg.DVM_COLL_VR,
+                                        samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                        samples_per_step=50000, deltat=0.01, seed=8), g)
+        s.initialize_dist_func(ph.bimodal(g))
+        s.solve(1)
+        n = s.collision_count()
+        counts.append(s.scatter_count())
+        assert 2 * n < counts[-1] <= 16 * n
+    assert abs(counts[0] - counts[1]) <= 1e-3 * counts[0]

@@ -121,3 +121,26 @@ def test_golden_fixtures_regression(oracle, pkg):
             st, ms, r = oracle.remap(g, u, v, w)
             assert list(st) == list(G["remap_%s_st" % name][t])
             assert np.allclose(ms, G["remap_%s_mass" % name][t], rtol=0, atol=1e-13)
+
+
+def test_scatter_count(oracle, pkg):
+    """The restatement counts its adds into f: 2 depletions per sample with g > 0 plus 4 to
+    7 stencil nodes per post-collision velocity; same-node pairs (g = 0) add nothing."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -5.0, 5.0)
+    rng = np.random.default_rng(3)
+    n, same = 500, 100
+    glA = rng.integers(0, g.nv, n).astype(np.int32)
+    glB = (glA + 1 + rng.integers(0, g.nv - 1, n)).astype(np.int32) % g.nv
+    node = rng.integers(0, g.nv, same).astype(np.int32)
+    sub = {"count": n + same, "num_repl": 1, "glA": np.concatenate([glA, node]),
+           "glB": np.concatenate([glB.astype(np.int32), node]),
+           "r_phi": rng.random(n + same), "r_cos": rng.random(n + same)}
+    empty = {"count": 0, "num_repl": 1, "glA": np.zeros(0, np.int32),
+             "glB": np.zeros(0, np.int32), "r_phi": np.zeros(0), "r_cos": np.zeros(0)}
+    cfg = pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, deltat=0.01)
+    cpu = oracle.OracleSolver(cfg, g)
+    cpu.initialize_dist_func(ph.bimodal(g))
+    cpu.compute_collision_integral(0, pkg.PairList([sub, empty, empty]))
+    sc = cpu.scatter_count()
+    assert 10 * n <= sc <= 16 * n

@@ -1490,6 +1490,16 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
 // reason, and f + df - w * poly is formed in FP64 from the exact doubles of the two floats.
 constexpr int kProjThreads = 256;
 
+// Threads per CTA of a kernel whose threads walk the (i, j) columns of one cell: the
+// columns split into the fewest rounds of at most max_threads, each round a whole number
+// of warps (576 columns of a 24^3 grid: 3 rounds of 192, no idle tail round).
+static int column_threads(const GridInfo& g, int max_threads) {
+  const int cols = g.nx * g.ny;
+  const int rounds = (cols + max_threads - 1) / max_threads;
+  const int per = (cols + rounds - 1) / rounds;
+  return ((per + 31) / 32) * 32;
+}
+
 // The projection of one cell, for the block: df (global or shared) is read, its projected
 // value added to f, and df zeroed when it is the global increment buffer.
 __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool zero_df,
@@ -1631,7 +1641,7 @@ __global__ void __launch_bounds__(kProjThreads, 3) k_project(ProjectArgs a) {
 }
 
 cudaError_t launch_project(const ProjectArgs& a, cudaStream_t s) {
-  k_project<<<a.ncells, kProjThreads, 0, s>>>(a);
+  k_project<<<a.ncells, column_threads(a.g, kProjThreads), 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -2161,16 +2171,6 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
   }
 }
 
-// Threads per moments CTA: the columns split into the fewest rounds of at most kMomThreads,
-// each round a whole number of warps (576 columns of a 24^3 grid: 3 rounds of 192, no
-// idle tail round).
-static int moment_threads(const GridInfo& g) {
-  const int cols = g.nx * g.ny;
-  const int rounds = (cols + kMomThreads - 1) / kMomThreads;
-  const int per = (cols + rounds - 1) / rounds;
-  return ((per + 31) / 32) * 32;
-}
-
 // Node values straight from f.
 struct MomSourceF {
   const double* f;
@@ -2186,7 +2186,7 @@ __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
 }
 
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
-  k_moments<<<a.ncells, moment_threads(a.g), 0, s>>>(a);
+  k_moments<<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@
 // Layout f[cell][v], FP64. Collision contributions are scattered straight into f with
 // FP64 atomics: in the monatomic step the sampling reads only the CDFs built at the start
 // of the cell-step, so delta_phi = phi + sum(contributions) needs no copy of phi.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "dfloat.cuh"
@@ -2027,9 +2028,14 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
 
-// The moments of one cell, for the block; src.begin(col) opens an (i, j) column and
-// src.value(k) returns the value of its node k as a pair.
-template <class Src>
+// The moments of one cell; src.begin(col) opens an (i, j) column and src.value(k) returns
+// the value of its node k as a pair. With kSplit, the cell's columns are dealt over the
+// CTAs of a thread-block cluster (few cells: more CTAs than cells fill the SMs); each CTA
+// reduces its columns and the partial totals meet in the shared memory of the cluster's
+// first CTA, which adds them in rank order and forms the properties.
+constexpr int kMomSplitMax = 4;
+
+template <bool kSplit, class Src>
 __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, Src& src) {
   __shared__ float2 s_red[kMomAcc * 32];
   __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
@@ -2063,7 +2069,13 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
 #pragma unroll
   for (int q = 0; q < kMomAcc; ++q) dacc_zero(sacc[q]);
   const float2* speed = g.speed;
-  for (int col = threadIdx.x; col < NXY; col += blockDim.x) {
+  unsigned rank = 0, nrank = 1;
+  if constexpr (kSplit) {
+    rank = cooperative_groups::this_cluster().block_rank();
+    nrank = cooperative_groups::this_cluster().num_blocks();
+  }
+  for (int col = threadIdx.x + static_cast<int>(rank * blockDim.x); col < NXY;
+       col += static_cast<int>(nrank * blockDim.x)) {
     dacc G0, G1, G2, G3, S;
     dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
     src.begin(col);
@@ -2103,6 +2115,25 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
   }
   double acc[kMomAcc];
   block_sum_dfl<kMomAcc>(sacc, s_red, acc);
+  if constexpr (kSplit) {
+    __shared__ double s_part[kMomSplitMax][kMomAcc];  // used in the cluster's first CTA
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    if (threadIdx.x == 0) {
+      double* dst = cl.map_shared_rank(&s_part[0][0], 0) + rank * kMomAcc;
+#pragma unroll
+      for (int q = 0; q < kMomAcc; ++q) dst[q] = acc[q];
+    }
+    cl.sync();  // also orders every CTA's reads of P before the first CTA writes it
+    if (rank != 0) return;
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int q = 0; q < kMomAcc; ++q) {
+        double t = s_part[0][q];
+        for (unsigned r = 1; r < nrank; ++r) t += s_part[r][q];
+        acc[q] = t;
+      }
+    }
+  }
   if (threadIdx.x == 0) {
     // the previous moments, for the residual (only this thread writes P)
     const double n_old = P[DVM_P_DENS], t_old = P[DVM_P_TEMP];
@@ -2182,12 +2213,53 @@ struct MomSourceF {
 __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
   const int cell = blockIdx.x;
   MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
-  moments_of_cell(a, cell, src);
+  moments_of_cell<false>(a, cell, src);
+}
+
+// Launched in clusters of 2 or 4 CTAs per cell.
+__global__ void __launch_bounds__(kMomThreads, 3) k_moments_split(MomentArgs a) {
+  const int cell = static_cast<int>(blockIdx.x / cooperative_groups::this_cluster().num_blocks());
+  MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
+  moments_of_cell<true>(a, cell, src);
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      n = 1;
+    cudaGetLastError();
+  }
+  return n;
 }
 
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
-  k_moments<<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
-  return cudaGetLastError();
+  // CTAs per cell: enough that a launch of few cells still covers the SMs twice over
+  int split = 1;
+  while (split < kMomSplitMax && a.ncells * split < 2 * sm_count()) split *= 2;
+  if (split == 1) {
+    k_moments<<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  GridInfo gs = a.g;  // the columns one CTA walks
+  const int cols = a.g.nx * a.g.ny;
+  gs.nx = (cols + split - 1) / split;
+  gs.ny = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(static_cast<unsigned>(a.ncells * split));
+  cfg.blockDim = dim3(static_cast<unsigned>(column_threads(gs, kMomThreads)));
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(split);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_moments_split, a);
 }
 
 // ----------------------------------------------------------------------------------------

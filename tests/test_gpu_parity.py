@@ -72,6 +72,23 @@ def test_moments_match(gpulib, pkg, oracle):
         assert np.abs(pg[:, q] - pc[:, q]).max() <= 1e-12 * sc[q], pkg.PROP_NAMES[q]
 
 
+@pytest.mark.parametrize("ncells", [1, 100, 200, 320])
+def test_moments_cluster_split(gpulib, pkg, oracle, ncells):
+    """Few cells are reduced by clusters of 2 or 4 CTAs per cell (their partial sums meet in
+    distributed shared memory), many cells by one CTA each: both match the restatement."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(12, -5.0, 5.0)
+    rng = np.random.default_rng(ncells)
+    base = ph.bimodal(g, u1=0.7, T2=2.5)
+    f0 = base[None, :] * (1.0 + 0.05 * rng.random((ncells, g.nv)))
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, nx_space=ncells, iColl=pkg.DVM_COLL_NONE)
+    pg, pc = gpu.properties(), cpu.properties()
+    sc = prop_scales(pc)
+    for q in range(17):
+        assert np.abs(pg[:, q] - pc[:, q]).max() <= 1e-12 * sc[q], pkg.PROP_NAMES[q]
+    assert gpu.error_word() == 0
+
+
 @pytest.mark.parametrize("nodes", [True, False])
 @pytest.mark.parametrize("grid_n", [8, 12, 24])
 def test_vr_pairlist_step(gpulib, pkg, oracle, nodes, grid_n):

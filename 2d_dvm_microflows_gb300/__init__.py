@@ -384,13 +384,17 @@ class DVMServer:
     grid; a native worker thread admits them by HBM footprint, keeps their state on the
     device and advances them concurrently until each reaches its residual or step limit."""
 
-    def __init__(self, hbm_budget_bytes, max_active=16, steps_per_turn=2, lib=None):
+    def __init__(self, hbm_budget_bytes, max_active=16, steps_per_turn=2, preempt_turns=0,
+                 lib=None):
         self.lib = lib or load_library()
         sv = C.c_void_p()
         _check(self.lib.dvm_server_create(C.c_uint64(int(hbm_budget_bytes)), int(max_active),
                                           int(steps_per_turn), C.byref(sv)), "dvm_server_create")
         self.sv = sv
         self._shape = {}
+        if preempt_turns:
+            _check(self.lib.dvm_server_set_preemption(self.sv, int(preempt_turns)),
+                   "dvm_server_set_preemption")
 
     def close(self):
         if getattr(self, "sv", None):
@@ -424,7 +428,7 @@ class DVMServer:
     def wait(self, rid):
         info = dvm_request_info()
         _check(self.lib.dvm_server_wait(self.sv, C.c_int64(rid), C.byref(info)), "dvm_server_wait")
-        return {k: getattr(info, k) for k, _ in dvm_request_info._fields_ if k != "reserved"}
+        return {k: getattr(info, k) for k, _ in dvm_request_info._fields_}
 
     def result(self, rid):
         """(properties[cells, DVM_NPROP], f[cells, nv]) of a finished request."""

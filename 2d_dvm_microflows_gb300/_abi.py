@@ -70,7 +70,7 @@ class dvm_pairlist(C.Structure):
 
 class dvm_request_info(C.Structure):
     _fields_ = [("status", C.c_int32), ("converged", C.c_int32), ("steps", C.c_int32),
-                ("reserved", C.c_int32), ("residual", C.c_double), ("queue_ms", C.c_double),
+                ("preempted", C.c_int32), ("residual", C.c_double), ("queue_ms", C.c_double),
                 ("latency_ms", C.c_double), ("collisions", C.c_int64),
                 ("device_bytes", C.c_uint64)]
 
@@ -130,6 +130,7 @@ ENTRY_POINTS = {
                                     C.POINTER(C.c_double)]),
     "dvm_server_stats": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                    C.POINTER(C.c_uint64)]),
+    "dvm_server_set_preemption": (C.c_int, [_P, C.c_int32]),
     "dvm_collide_noalloc": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), _P, _P,
                                       C.c_int, C.c_uint64, _P, C.POINTER(C.c_int64)]),
 }

@@ -11,9 +11,17 @@
 // its step limit is reached; its memory then goes back to the stream-ordered pool and the
 // next queued request is admitted. A request's result depends only on its own parameters,
 // seed and step count, never on what else is in the mix.
+//
+// Preemption (dvm_server_set_preemption): a request that has run a given number of turns
+// since its admission while another request waits is checkpointed to host memory
+// (dvm_checkpoint_save: f, moments, the equilibrium cache and its CDF), its device memory
+// and slot are released, and it is queued again behind the waiting requests. Readmitted, it
+// continues from the checkpoint with its Philox step counter and collision total restored,
+// so its result is that of an uninterrupted run.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -59,6 +67,12 @@ struct Request {
   int steps_issued = 0;
   int steps_done = 0;
   bool eager_tail = false;  // an odd last step was issued outside the graph
+  int turns = 0;            // turns completed since the last admission
+  // preemption
+  int preempted = 0;                // times checkpointed and requeued
+  bool parked = false;              // checkpointed, waiting to be readmitted
+  std::vector<unsigned char> ckpt;  // the checkpoint while parked
+  long long collisions_before = 0;  // collision total at the checkpoint
   // result
   int status = DVM_OK;
   int converged = 0;
@@ -89,6 +103,7 @@ struct dvm_server {
   int max_active = 1;
   int quantum = 2;
   int device = 0;
+  std::atomic<int> preempt_turns{0};  // 0: no preemption
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Request>> pending;  // submitted, not yet admitted
@@ -144,13 +159,32 @@ int admit(dvm_server* sv, Request& r) {
   cudaMemsetAsync(r.d_step, 0, sizeof(uint32_t), r.stream);
   cudaMemsetAsync(r.d_acc, 0, sizeof(long long), r.stream);
   dvm::ctx_set_step_dev(r.ctx, r.d_step);
-  st = dvm_upload_f(r.ctx, r.f0.data());  // also computes the initial moments
-  if (st) return st;
-  std::vector<double>().swap(r.f0);
+  if (r.parked) {
+    // resume: the checkpointed state, the step counter and the collision total
+    uint64_t ntime = 0;
+    st = dvm_checkpoint_load(r.ctx, r.ckpt.data(), r.ckpt.size(), &ntime);
+    if (!st && ntime != static_cast<uint64_t>(r.steps_done)) st = DVM_ERR_PARAM;
+    const uint32_t step = static_cast<uint32_t>(r.steps_done);
+    if (!st)
+      st = cuda_st(cudaMemcpyAsync(r.d_step, &step, sizeof(step), cudaMemcpyHostToDevice,
+                                   r.stream));
+    if (!st)
+      st = cuda_st(cudaMemcpyAsync(r.d_acc, &r.collisions_before, sizeof(long long),
+                                   cudaMemcpyHostToDevice, r.stream));
+    if (!st) st = cuda_st(cudaStreamSynchronize(r.stream));
+    if (st) return st;
+    std::vector<unsigned char>().swap(r.ckpt);
+    r.parked = false;
+  } else {
+    st = dvm_upload_f(r.ctx, r.f0.data());  // also computes the initial moments
+    if (st) return st;
+    std::vector<double>().swap(r.f0);
+  }
+  r.turns = 0;
   // an even number of steps per graph when convection swaps f and f_conv
   r.quantum = sv->quantum;
   if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) ++r.quantum;
-  r.quantum = std::min(r.quantum, std::max(1, r.max_steps));
+  r.quantum = std::min(r.quantum, std::max(1, r.max_steps - r.steps_done));
   if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) r.quantum = 0;  // eager only
   if (r.quantum > 0) st = capture_quantum(r);
   if (!st) st = cuda_st(cudaEventCreateWithFlags(&r.ev, cudaEventDisableTiming));
@@ -181,6 +215,49 @@ int issue(dvm_server* sv, Request& r) {
   return st;
 }
 
+// Releases a request's graph, event, counters and context (after its stream is drained).
+void release_device(Request& r) {
+  cudaStreamSynchronize(r.stream);
+  if (r.exec) cudaGraphExecDestroy(r.exec);
+  if (r.ev) cudaEventDestroy(r.ev);
+  if (r.d_step) cudaFreeAsync(r.d_step, r.stream);
+  if (r.d_acc) cudaFreeAsync(r.d_acc, r.stream);
+  dvm::ctx_destroy(r.ctx);
+  r.exec = nullptr;
+  r.ev = nullptr;
+  r.d_step = nullptr;
+  r.d_acc = nullptr;
+  r.ctx = nullptr;
+}
+
+// Checkpoints an admitted request between turns and queues it again behind the waiting
+// requests; returns nonzero (and leaves the request admitted) if the checkpoint fails.
+int preempt(dvm_server* sv, Request& r) {
+  uint64_t bytes = 0;
+  int st = dvm_checkpoint_size(r.ctx, &bytes);
+  if (st) return st;
+  std::vector<unsigned char> buf(bytes);
+  st = dvm_checkpoint_save(r.ctx, static_cast<uint64_t>(r.steps_done), buf.data(), bytes);
+  long long acc = 0;
+  if (!st)
+    st = cuda_st(cudaMemcpyAsync(&acc, r.d_acc, sizeof(acc), cudaMemcpyDeviceToHost, r.stream));
+  if (!st) st = cuda_st(cudaStreamSynchronize(r.stream));
+  if (st) return st;
+  release_device(r);
+  r.ckpt.swap(buf);
+  r.collisions_before = acc;
+  r.parked = true;
+  r.preempted++;
+  r.eager_tail = false;
+  r.quantum = 0;
+  if (r.slot >= 0) sv->free_slots.push_back(r.slot);
+  r.slot = -1;
+  sv->used -= r.bytes;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  sv->pending.push_back(sv->all.at(r.id));
+  return DVM_OK;
+}
+
 void retire(dvm_server* sv, Request& r) {
   if (r.ctx) {
     if (r.status == DVM_OK) {
@@ -196,13 +273,7 @@ void retire(dvm_server* sv, Request& r) {
                                      cudaMemcpyDeviceToHost, r.stream));
       r.status = st;
     }
-    cudaStreamSynchronize(r.stream);
-    if (r.exec) cudaGraphExecDestroy(r.exec);
-    if (r.ev) cudaEventDestroy(r.ev);
-    if (r.d_step) cudaFreeAsync(r.d_step, r.stream);
-    if (r.d_acc) cudaFreeAsync(r.d_acc, r.stream);
-    dvm::ctx_destroy(r.ctx);
-    r.ctx = nullptr;
+    release_device(r);
   }
   if (r.slot >= 0) sv->free_slots.push_back(r.slot);
   r.slot = -1;
@@ -230,7 +301,7 @@ void worker_loop(dvm_server* sv) {
         std::shared_ptr<Request> r = sv->pending.front();
         sv->pending.pop_front();
         lk.unlock();
-        r->t_admit = Clock::now();
+        if (!r->parked) r->t_admit = Clock::now();  // the first admission
         r->slot = sv->free_slots.back();
         sv->free_slots.pop_back();
         sv->used += r->bytes;
@@ -265,15 +336,27 @@ void worker_loop(dvm_server* sv) {
           retire(sv, r);
           continue;
         }
+        // preemption between turns, while another request waits
+        const int pt = sv->preempt_turns.load();
+        if (pt > 0 && ++r.turns >= pt && !r.eager_tail) {
+          bool waiting;
+          {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            waiting = !sv->pending.empty();
+          }
+          if (waiting && preempt(sv, r) == DVM_OK) continue;
+        }
       }
-      if (!r.done && !r.inflight) {
+      if (!r.done && !r.parked && !r.inflight) {
         r.status = issue(sv, r);
         if (r.status) retire(sv, r);
         progress = true;
       }
     }
     sv->active.erase(std::remove_if(sv->active.begin(), sv->active.end(),
-                                    [](const std::shared_ptr<Request>& r) { return r->done; }),
+                                    [](const std::shared_ptr<Request>& r) {
+                                      return r->done || r->parked;
+                                    }),
                      sv->active.end());
     if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
@@ -376,6 +459,13 @@ int dvm_server_wait(dvm_server* sv, int64_t id, dvm_request_info* info) {
   info->latency_ms = ms_between(r->t_submit, r->t_done);
   info->collisions = r->collisions;
   info->device_bytes = r->device_bytes;
+  info->preempted = r->preempted;
+  return DVM_OK;
+}
+
+int dvm_server_set_preemption(dvm_server* sv, int32_t turns) {
+  if (!sv || turns < 0) return DVM_ERR_PARAM;
+  sv->preempt_turns.store(turns);
   return DVM_OK;
 }
 

@@ -480,6 +480,7 @@ SERVE_BUDGET = 64 << 30  # admission budget, bytes of HBM
 SERVE_SLOTS = 4   # concurrent requests: enough to overlap small kernels and host gaps
 SERVE_QUANTUM = 8    # steps per graph replay; the residual is checked between replays
                      # (measured: 4.7e9 collisions/s at 8 against 4.5e9 at 2)
+SERVE_PREEMPT = 0    # turns before a request yields its slot to a waiting one (0: never)
 
 
 def serving_workload(pkg, nreq=SERVE_REQUESTS, seed=SEED):
@@ -541,7 +542,8 @@ def run_serving(pkg, args):
     reqs = serving_workload(pkg)
     # served: submissions at their arrival times
     served = []
-    with pkg.DVMServer(SERVE_BUDGET, max_active=SERVE_SLOTS, steps_per_turn=SERVE_QUANTUM) as sv:
+    with pkg.DVMServer(SERVE_BUDGET, max_active=SERVE_SLOTS, steps_per_turn=SERVE_QUANTUM,
+                       preempt_turns=SERVE_PREEMPT) as sv:
         t0 = time.perf_counter()
         ids = []
         for t, cfg, g, f0, _ in reqs:

@@ -253,7 +253,7 @@ typedef struct dvm_request_info {
   int32_t status;         /* DVM_OK or the status that ended the request               */
   int32_t converged;      /* 1: the residual reached the tolerance                     */
   int32_t steps;          /* steps taken                                               */
-  int32_t reserved;
+  int32_t preempted;      /* times checkpointed and requeued (dvm_server_set_preemption) */
   double residual;        /* residual after the last step                              */
   double queue_ms;        /* submission to admission                                   */
   double latency_ms;      /* submission to result ready on the host                    */
@@ -276,6 +276,12 @@ int dvm_server_wait(dvm_server* server, int64_t id, dvm_request_info* info);
 int dvm_server_result(dvm_server* server, int64_t id, double* props, double* f);
 int dvm_server_stats(dvm_server* server, int64_t* completed, int32_t* peak_active,
                      uint64_t* peak_bytes);
+/* Preemption through the checkpoint (input_output/restart.f90:93-250): a request that has
+ * run `turns` turns since its admission while another request waits is checkpointed to
+ * host memory, its device memory and slot are released, and it is queued again behind the
+ * waiting requests; readmitted, it resumes from the checkpoint with its step counter, so
+ * its result is that of an uninterrupted run. 0 (the default) turns preemption off. */
+int dvm_server_set_preemption(dvm_server* server, int32_t turns);
 
 /* ---- errors, synchronisation, instrumentation -------------------------------------- */
 int dvm_synchronize(dvm_ctx* ctx);

@@ -125,3 +125,33 @@ def test_residual_ends_a_relaxation(gpulib, pkg):
         sv.result(rid)
     assert info["status"] == 0 and info["converged"] == 1
     assert info["steps"] < 400 and info["residual"] <= 2e-3
+
+
+def test_preemption_resumes_exactly(gpulib, pkg):
+    """Round-robin through the checkpoint: one slot and preemption after every turn, so the
+    requests take turns and each is checkpointed to host memory and resumed several times.
+    Every result equals its uninterrupted run (FP64: 1e-12 relative), with the same steps
+    and collision count."""
+    reqs = _requests(pkg, pkg.DVM_PREC_FP64)
+    with pkg.DVMServer(8 << 30, max_active=1, steps_per_turn=2, preempt_turns=1) as sv:
+        ids = [sv.submit(cfg, g, f0, steps) for (cfg, g, f0), steps in reqs]
+        res = []
+        for rid in ids:
+            info = sv.wait(rid)
+            props, f = sv.result(rid)
+            res.append((info, props, f))
+        assert sv.stats()["completed"] == len(reqs)
+    assert sum(info["preempted"] for info, _, _ in res) >= len(reqs) - 1
+    for ((cfg, g, f0), steps), (info, props, f) in zip(reqs, res):
+        alone, _ = _serve(pkg, [((cfg, g, f0), steps)], 1)
+        ainfo, aprops, af = alone[0]
+        assert info["status"] == 0 and info["steps"] == steps == ainfo["steps"]
+        assert info["collisions"] == ainfo["collisions"]
+        assert np.abs(f - af).max() <= 1e-12 * np.abs(af).max()
+        assert np.abs(props[:, :17] - aprops[:, :17]).max() <= 1e-11
+
+
+def test_preemption_off_by_default(gpulib, pkg):
+    reqs = _requests(pkg, pkg.DVM_PREC_FP64)[:3]
+    res, _ = _serve(pkg, reqs, max_active=1)
+    assert all(info["preempted"] == 0 for info, _, _ in res)

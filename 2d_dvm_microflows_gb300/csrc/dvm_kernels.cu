@@ -31,9 +31,7 @@ namespace dvm {
 // independent of the order of summation, so the parallel scan gives the sequential sum
 // bit for bit; the quantum 2^-k is below 1e-17 n, finer than the FP64 rounding of the
 // reference's running sum. The partner search (k_collide) then compares integers only.
-constexpr int kCdfThreads = 256;
 constexpr int kCdfPer = 4;
-constexpr int kCdfChunk = kCdfThreads * kCdfPer;  // nodes per scan chunk
 constexpr int kCdfPitch = kCdfPer + 1;            // padded per-thread row in shared memory
 constexpr int kCdfCoarseMax = 512;   // entries of the shared-memory coarse index per table
 
@@ -96,6 +94,18 @@ __device__ __forceinline__ float sign_float(double v) {
   return __int_as_float(static_cast<int>((hi & 0x80000000u) | 0x3f800000u));
 }
 
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      n = 1;
+    cudaGetLastError();
+  }
+  return n;
+}
+
 // Block-wide exclusive scan of two int64 per thread; tot gets the block totals.
 __device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long long& tot_a,
                                                 long long& tot_b, long long* s_scan) {
@@ -129,7 +139,12 @@ __device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long
   b = wpb + ib - b;
 }
 
-__global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
+// T threads per CTA (256, or 512 / 1024 for launches of few cells: the per-cell scan then
+// walks fewer, wider chunks).
+template <int T>
+__global__ void __launch_bounds__(T) k_cdf(CdfArgs a) {
+  constexpr int kCdfThreads = T;
+  constexpr int kCdfChunk = T * kCdfPer;  // nodes per scan chunk
   // chunk staging: node m of a chunk sits at (m / kCdfPer) * kCdfPitch + m % kCdfPer, so
   // global memory is read and written in coalesced rows while each thread scans
   // kCdfPer consecutive nodes
@@ -456,13 +471,23 @@ __global__ void __launch_bounds__(kCdfThreads) k_cdf(CdfArgs a) {
   }
 }
 
-cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
-  constexpr int smem = 2 * kCdfThreads * kCdfPitch * static_cast<int>(sizeof(long long)) +
-                       2 * kCdfChunk * static_cast<int>(sizeof(double));
-  const cudaError_t e = cudaFuncSetAttribute(k_cdf, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+template <int T>
+static cudaError_t launch_cdf_t(const CdfArgs& a, cudaStream_t s) {
+  constexpr int smem = 2 * T * kCdfPitch * static_cast<int>(sizeof(long long)) +
+                       2 * T * kCdfPer * static_cast<int>(sizeof(double));
+  const cudaError_t e = cudaFuncSetAttribute(k_cdf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_cdf<<<a.ncells, kCdfThreads, smem, s>>>(a);
+  k_cdf<T><<<a.ncells, T, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
+  // one CTA per cell: as wide as still lets every cell's CTA be resident at once (1024
+  // threads, one per SM; 512, two; otherwise 256, four)
+  const int nsm = sm_count();
+  if (a.ncells <= nsm) return launch_cdf_t<1024>(a, s);
+  if (a.ncells <= 2 * nsm) return launch_cdf_t<512>(a, s);
+  return launch_cdf_t<256>(a, s);
 }
 
 // ----------------------------------------------------------------------------------------
@@ -2223,17 +2248,6 @@ __global__ void __launch_bounds__(kMomThreads, 3) k_moments_split(MomentArgs a) 
   moments_of_cell<true>(a, cell, src);
 }
 
-static int sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
-      n = 1;
-    cudaGetLastError();
-  }
-  return n;
-}
 
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
   // CTAs per cell: enough that a launch of few cells still covers the SMs twice over

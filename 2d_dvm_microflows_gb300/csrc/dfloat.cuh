@@ -105,6 +105,15 @@ __device__ __forceinline__ double dfl_to_double_normal(dfl a) {
   return dbl_from_normal_float(a.hi) + dbl_from_normal_float(a.lo);
 }
 
+// Pair -> double for a hi of any finite, infinite or NaN value with a lo below it: inf and
+// NaN carry over through hi, and an FP32-subnormal part (below 1.2e-38) may come out off
+// by up to its own size, far below the FP64 rounding of any value the kernels keep.
+__device__ __forceinline__ double dfl_to_double_fast(dfl a) {
+  const uint32_t u = static_cast<uint32_t>(__float_as_int(a.hi));
+  if ((u & 0x7f800000u) == 0x7f800000u) return dbl_from_float(a.hi);
+  return dbl_from_normal_float(a.hi) + dbl_from_normal_float(a.lo);
+}
+
 // Knuth's TwoSum: s + e = a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);

@@ -1878,6 +1878,18 @@ __global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
   }
   const float2 cxf = __ldg(a.cfl + i), cyf = __ldg(a.cfl + NX + j);
   const dfl AX = dfl_make(cxf.x, cxf.y), AY = dfl_make(cyf.x, cyf.y);
+  if (hx && hy && px && py) {
+    // both upwind sources present (every interior column): no per-node tests
+#pragma unroll 4
+    for (int k = 0; k < NZ; ++k) {
+      const size_t o = static_cast<size_t>(NXY) * k;
+      const dfl F0 = dfl_from_double(f0p[o]);
+      const dfl acc = dfl_add(dfl_add(F0, dfl_mul(AX, dfl_sub(dfl_from_double(px[o]), F0))),
+                              dfl_mul(AY, dfl_sub(dfl_from_double(py[o]), F0)));
+      out[o] = dfl_to_double_fast(acc);
+    }
+    return;
+  }
 #pragma unroll 4
   for (int k = 0; k < NZ; ++k) {
     const size_t o = static_cast<size_t>(NXY) * k;
@@ -1887,7 +1899,7 @@ __global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
     // reference's zero-initialised neighbour
     if (hx) acc = dfl_add(acc, dfl_mul(AX, dfl_sub(px ? dfl_from_double(px[o]) : dfl_make(0.f, 0.f), F0)));
     if (hy) acc = dfl_add(acc, dfl_mul(AY, dfl_sub(py ? dfl_from_double(py[o]) : dfl_make(0.f, 0.f), F0)));
-    out[o] = dfl_to_double(acc);
+    out[o] = dfl_to_double_fast(acc);
   }
 }
 

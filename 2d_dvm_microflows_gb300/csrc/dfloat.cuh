@@ -105,6 +105,15 @@ __device__ __forceinline__ double dfl_to_double_normal(dfl a) {
   return dbl_from_normal_float(a.hi) + dbl_from_normal_float(a.lo);
 }
 
+// float -> double for any float: inf and NaN carry over exactly, a subnormal (below
+// 1.2e-38) may come out off by up to its own size; the short form for values added into
+// FP64 state, where that is far below the FP64 rounding of the state.
+__device__ __forceinline__ double dbl_from_float_fast(float v) {
+  const uint32_t u = static_cast<uint32_t>(__float_as_int(v));
+  if ((u & 0x7f800000u) == 0x7f800000u) return dbl_from_float(v);
+  return dbl_from_normal_float(v);
+}
+
 // Pair -> double for a hi of any finite, infinite or NaN value with a lo below it: inf and
 // NaN carry over through hi, and an FP32-subnormal part (below 1.2e-38) may come out off
 // by up to its own size, far below the FP64 rounding of any value the kernels keep.

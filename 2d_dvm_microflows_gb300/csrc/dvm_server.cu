@@ -1,15 +1,17 @@
 // dvm_server.cu -- request server for independent solves (dvm_server_* in include/dvm_gpu.h).
 //
-// Continuous batching: a worker thread admits queued requests in arrival order whenever the
-// sum of the admitted requests' device footprints stays within the budget and a slot is
-// free, keeps every admitted request's f, CDFs and moments resident in its own context on
-// its own stream, and advances all admitted requests in turns of a few steps, each turn one
-// replay of a CUDA graph captured for that request. The turns of different requests run on
-// different streams, so their kernels overlap on the device. After every turn the worker
-// reads the request's convergence residual (an asynchronous 8-byte copy to pinned memory,
-// polled with an event) and retires the request once the residual reaches its tolerance or
-// its step limit is reached; its memory then goes back to the stream-ordered pool and the
-// next queued request is admitted. A request's result depends only on its own parameters,
+// Continuous batching: queued requests are admitted in arrival order whenever the sum of
+// the admitted requests' device footprints stays within the budget and a slot is free;
+// every admitted request keeps its f, CDFs and moments resident in its own context on its
+// own stream and advances in turns of a few steps, each turn one replay of a CUDA graph
+// captured for that request. The turns of different requests run on different streams, so
+// their kernels overlap on the device. After every turn the request's convergence residual
+// comes back by an asynchronous 8-byte copy to pinned memory, polled with an event; the
+// request is retired once the residual reaches its tolerance or its step limit is reached,
+// its memory going back to the stream-ordered pool. Three host threads share the work so
+// that the one issuing turns never waits on the others: a preparer admits requests (context,
+// upload, graph capture), the worker polls and issues turns, a retirer downloads results and
+// releases contexts. A request's result depends only on its own parameters,
 // seed and step count, never on what else is in the mix.
 //
 // Preemption (dvm_server_set_preemption): a request that has run a given number of turns
@@ -81,6 +83,7 @@ struct Request {
   uint64_t device_bytes = 0;
   std::vector<double> props, f;
   bool done = false;
+  bool handed = false;  // the worker gave it to the retirer
 
   dvm_vgrid vgrid() const {
     dvm_vgrid v;
@@ -104,17 +107,22 @@ struct dvm_server {
   int quantum = 2;
   int device = 0;
   std::atomic<int> preempt_turns{0};  // 0: no preemption
-  std::mutex mu;
-  std::condition_variable cv_work, cv_done;
-  std::deque<std::shared_ptr<Request>> pending;  // submitted, not yet admitted
+  std::mutex mu;  // guards everything below but `active`
+  std::condition_variable cv_work, cv_done, cv_prep, cv_retire;
+  std::deque<std::shared_ptr<Request>> pending;   // submitted (or preempted), not admitted
+  std::deque<std::shared_ptr<Request>> ready;     // admitted and prepared, for the worker
+  std::deque<std::shared_ptr<Request>> finished;  // for the retirer
   std::map<int64_t, std::shared_ptr<Request>> all;
-  std::vector<std::shared_ptr<Request>> active;  // worker thread only
+  std::vector<std::shared_ptr<Request>> active;   // worker thread only
   int64_t next_id = 1;
   bool stop = false;
-  std::thread worker;
+  int live = 0;               // requests holding a slot (admission to retirement or parking)
+  std::thread worker, preparer, retirer;
   double* h_slots = nullptr;  // pinned, one residual per slot
   std::vector<int> free_slots;
-  uint64_t used = 0;          // worker thread only
+  uint64_t used = 0;
+  // every thread ends once destruction was asked for and no request is left
+  bool drained() const { return stop && pending.empty() && live == 0; }
   // statistics
   int64_t completed = 0;
   int peak_active = 0;
@@ -250,14 +258,19 @@ int preempt(dvm_server* sv, Request& r) {
   r.preempted++;
   r.eager_tail = false;
   r.quantum = 0;
-  if (r.slot >= 0) sv->free_slots.push_back(r.slot);
-  r.slot = -1;
-  sv->used -= r.bytes;
-  std::lock_guard<std::mutex> lk(sv->mu);
-  sv->pending.push_back(sv->all.at(r.id));
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (r.slot >= 0) sv->free_slots.push_back(r.slot);
+    r.slot = -1;
+    sv->used -= r.bytes;
+    sv->live--;
+    sv->pending.push_back(sv->all.at(r.id));
+  }
+  sv->cv_prep.notify_one();
   return DVM_OK;
 }
 
+// The retirer's part: results to the host, the context released, the slot given back.
 void retire(dvm_server* sv, Request& r) {
   if (r.ctx) {
     if (r.status == DVM_OK) {
@@ -275,47 +288,99 @@ void retire(dvm_server* sv, Request& r) {
     }
     release_device(r);
   }
-  if (r.slot >= 0) sv->free_slots.push_back(r.slot);
-  r.slot = -1;
-  sv->used -= r.bytes;
   r.t_done = Clock::now();
-  std::lock_guard<std::mutex> lk(sv->mu);
-  r.done = true;
-  sv->completed++;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (r.slot >= 0) sv->free_slots.push_back(r.slot);
+    r.slot = -1;
+    sv->used -= r.bytes;
+    sv->live--;
+    r.done = true;
+    sv->completed++;
+  }
   sv->cv_done.notify_all();
+  sv->cv_prep.notify_one();
+  sv->cv_work.notify_one();
+  sv->cv_retire.notify_one();
+}
+
+// Hands a request that ended (or failed) to the retirer.
+void finish(dvm_server* sv, const std::shared_ptr<Request>& r) {
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->finished.push_back(r);
+  }
+  sv->cv_retire.notify_one();
+}
+
+void preparer_loop(dvm_server* sv) {
+  cudaSetDevice(sv->device);
+  std::unique_lock<std::mutex> lk(sv->mu);
+  for (;;) {
+    sv->cv_prep.wait(lk, [&] {
+      return sv->drained() ||
+             (!sv->pending.empty() && !sv->free_slots.empty() &&
+              sv->used + sv->pending.front()->bytes <= sv->budget);
+    });
+    if (sv->pending.empty()) {
+      if (sv->drained()) break;
+      continue;
+    }
+    std::shared_ptr<Request> r = sv->pending.front();
+    sv->pending.pop_front();
+    r->slot = sv->free_slots.back();
+    sv->free_slots.pop_back();
+    sv->used += r->bytes;
+    sv->live++;
+    sv->peak_active = std::max(sv->peak_active, sv->live);
+    sv->peak_bytes = std::max(sv->peak_bytes, sv->used);
+    lk.unlock();
+    if (!r->parked) r->t_admit = Clock::now();  // the first admission
+    r->status = admit(sv, *r);
+    lk.lock();
+    if (r->status) {
+      sv->finished.push_back(r);
+      sv->cv_retire.notify_one();
+    } else {
+      sv->ready.push_back(r);
+      sv->cv_work.notify_one();
+    }
+  }
+  lk.unlock();
+  sv->cv_work.notify_all();
+  sv->cv_retire.notify_all();
+}
+
+void retirer_loop(dvm_server* sv) {
+  cudaSetDevice(sv->device);
+  std::unique_lock<std::mutex> lk(sv->mu);
+  for (;;) {
+    sv->cv_retire.wait(lk, [&] { return !sv->finished.empty() || sv->drained(); });
+    if (sv->finished.empty()) break;
+    std::shared_ptr<Request> r = sv->finished.front();
+    sv->finished.pop_front();
+    lk.unlock();
+    retire(sv, *r);
+    lk.lock();
+  }
+  lk.unlock();
+  sv->cv_work.notify_all();
+  sv->cv_prep.notify_all();
 }
 
 void worker_loop(dvm_server* sv) {
   cudaSetDevice(sv->device);
   for (;;) {
-    // admission, in arrival order, while the footprint budget and a slot allow
+    // take the prepared requests; with none running, wait for one (or for the end)
     {
       std::unique_lock<std::mutex> lk(sv->mu);
-      if (sv->active.empty() && sv->pending.empty()) {
-        if (sv->stop) return;
-        sv->cv_work.wait(lk, [&] { return sv->stop || !sv->pending.empty(); });
-        if (sv->pending.empty()) return;
+      if (sv->active.empty())
+        sv->cv_work.wait(lk, [&] { return !sv->ready.empty() || sv->drained(); });
+      while (!sv->ready.empty()) {
+        sv->active.push_back(sv->ready.front());
+        sv->ready.pop_front();
       }
-      while (!sv->pending.empty() && static_cast<int>(sv->active.size()) < sv->max_active &&
-             sv->used + sv->pending.front()->bytes <= sv->budget) {
-        std::shared_ptr<Request> r = sv->pending.front();
-        sv->pending.pop_front();
-        lk.unlock();
-        if (!r->parked) r->t_admit = Clock::now();  // the first admission
-        r->slot = sv->free_slots.back();
-        sv->free_slots.pop_back();
-        sv->used += r->bytes;
-        r->status = admit(sv, *r);
-        if (r->status) {
-          retire(sv, *r);
-          lk.lock();
-        } else {
-          sv->active.push_back(r);
-          lk.lock();
-          sv->peak_active = std::max(sv->peak_active, static_cast<int>(sv->active.size()));
-          sv->peak_bytes = std::max(sv->peak_bytes, sv->used);
-        }
-      }
+      if (sv->active.empty() && sv->drained()) break;
     }
     bool progress = false;
     for (auto& rp : sv->active) {
@@ -333,7 +398,8 @@ void worker_loop(dvm_server* sv) {
           if (r.residual <= r.tol) r.converged = 1;
         }
         if (r.status || r.converged || r.steps_done >= r.max_steps) {
-          retire(sv, r);
+          r.handed = true;
+          finish(sv, rp);
           continue;
         }
         // preemption between turns, while another request waits
@@ -347,19 +413,24 @@ void worker_loop(dvm_server* sv) {
           if (waiting && preempt(sv, r) == DVM_OK) continue;
         }
       }
-      if (!r.done && !r.parked && !r.inflight) {
+      if (!r.handed && !r.parked && !r.inflight) {
         r.status = issue(sv, r);
-        if (r.status) retire(sv, r);
+        if (r.status) {
+          r.handed = true;
+          finish(sv, rp);
+        }
         progress = true;
       }
     }
     sv->active.erase(std::remove_if(sv->active.begin(), sv->active.end(),
                                     [](const std::shared_ptr<Request>& r) {
-                                      return r->done || r->parked;
+                                      return r->handed || r->parked;
                                     }),
                      sv->active.end());
     if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
+  sv->cv_prep.notify_all();
+  sv->cv_retire.notify_all();
 }
 
 double ms_between(Clock::time_point a, Clock::time_point b) {
@@ -396,6 +467,8 @@ int dvm_server_create(uint64_t hbm_budget_bytes, int max_active, int steps_per_t
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   sv->worker = std::thread(worker_loop, sv);
+  sv->preparer = std::thread(preparer_loop, sv);
+  sv->retirer = std::thread(retirer_loop, sv);
   *out = sv;
   return DVM_OK;
 }
@@ -407,7 +480,11 @@ int dvm_server_destroy(dvm_server* sv) {
     sv->stop = true;
   }
   sv->cv_work.notify_all();
+  sv->cv_prep.notify_all();
+  sv->cv_retire.notify_all();
   if (sv->worker.joinable()) sv->worker.join();
+  if (sv->preparer.joinable()) sv->preparer.join();
+  if (sv->retirer.joinable()) sv->retirer.join();
   cudaFreeHost(sv->h_slots);
   delete sv;
   return DVM_OK;
@@ -438,7 +515,7 @@ int dvm_server_submit(dvm_server* sv, const dvm_params* params, const dvm_vgrid*
     sv->all[r->id] = r;
     sv->pending.push_back(r);
   }
-  sv->cv_work.notify_one();
+  sv->cv_prep.notify_one();
   *id = r->id;
   return DVM_OK;
 }

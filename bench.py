@@ -477,7 +477,7 @@ SERVE_RATE = 50.0        # Poisson arrivals per second
 SERVE_MAX_STEPS = 40
 SERVE_TOL = 1e-6
 SERVE_BUDGET = 64 << 30  # admission budget, bytes of HBM
-SERVE_SLOTS = 4   # concurrent requests: enough to overlap small kernels and host gaps
+SERVE_SLOTS = 6   # concurrent requests (measured: 4.98e9 collisions/s at 6, 4.85e9 at 4 and 8)
 SERVE_QUANTUM = 8    # steps per graph replay; the residual is checked between replays
                      # (measured: 4.7e9 collisions/s at 8 against 4.5e9 at 2)
 SERVE_PREEMPT = 0    # turns before a request yields its slot to a waiting one (0: never)

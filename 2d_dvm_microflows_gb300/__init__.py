@@ -381,8 +381,8 @@ def footprint_bytes(config, grid, lib=None):
 
 class DVMServer:
     """Continuous-batching request server (dvm_server_*): submit solves of any geometry and
-    grid; a native worker thread admits them by HBM footprint, keeps their state on the
-    device and advances them concurrently until each reaches its residual or step limit."""
+    grid; native host threads admit them by HBM footprint, keep their state on the
+    device and advance them concurrently until each reaches its residual or step limit."""
 
     def __init__(self, hbm_budget_bytes, max_active=16, steps_per_turn=2, preempt_turns=0,
                  lib=None):

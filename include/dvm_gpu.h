@@ -241,8 +241,8 @@ int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisio
 int dvm_footprint_bytes(const dvm_params* params, const dvm_vgrid* vgrid, uint64_t* bytes);
 
 /* Independent solves (any geometry, grid, Knudsen or Mach number) served with continuous
- * batching. No reference counterpart: the reference runs one solve per process. A worker
- * thread admits submitted requests in arrival order while the admitted footprints fit in
+ * batching. No reference counterpart: the reference runs one solve per process. Native
+ * host threads admit submitted requests in arrival order while the admitted footprints fit in
  * hbm_budget_bytes and fewer than max_active run; each admitted request keeps its state on
  * the device in its own context and stream and advances steps_per_turn steps per turn (one
  * CUDA-graph replay), so the turns of different requests overlap on the device. A request

@@ -104,6 +104,7 @@ ENTRY_POINTS = {
     "dvm_time_steps": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_double)]),
     "dvm_flush_l2": (C.c_int, [_P]),
     "dvm_get_residual": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "dvm_wait_selftest": (C.c_int, [_P]),
     "dvm_atomic_rate": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_double)]),
     "dvm_checkpoint_size": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "dvm_checkpoint_save": (C.c_int, [_P, C.c_uint64, C.c_void_p, C.c_uint64]),

@@ -965,6 +965,13 @@ int dvm_flush_l2(dvm_ctx* c) {
   return cuda_status(launch_flush(c->d_flush, c->flush_n, c->stream));
 }
 
+int dvm_wait_selftest(dvm_ctx* c) {
+  if (!c) return DVM_ERR_PARAM;
+  int st = cuda_status(launch_wait_selftest(c->d_err, c->stream));
+  if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+  return st;
+}
+
 int dvm_atomic_rate(dvm_ctx* c, uint64_t window_bytes, double* per_s) {
   if (!c || !per_s || window_bytes < sizeof(double)) return DVM_ERR_PARAM;
   int st = dvm_flush_l2(c);  // allocates the scratch buffer

@@ -357,16 +357,25 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       : "memory");
 }
 
-// Waits for the barrier phase with parity `parity` to complete; gives up after a bounded
-// number of polls and returns false (the caller reports it and carries on).
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the barrier phase with parity `parity` to complete; gives up after about one
+// second (each poll may suspend the thread for at most 1 us, and the poll count and the
+// global timer are both bounded) and returns false (the caller reports it and carries on).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_addr(bar);
+  const uint64_t t0 = global_ns();
   for (int it = 0; it < (1 << 20); ++it) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}" : "=r"(done) : "r"(a), "r"(parity), "r"(1000u) : "memory");
     if (done) return true;
+    if ((it & 63) == 63 && global_ns() - t0 > 1000000000ull) return false;
   }
   return false;
 }

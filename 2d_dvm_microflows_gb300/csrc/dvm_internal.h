@@ -200,6 +200,7 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s);         // diff
 cudaError_t launch_bc1d_nodes(const Convect1DArgs& a, cudaStream_t s);   // the other ends
 cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s);
 cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s);
+cudaError_t launch_wait_selftest(uint32_t* err, cudaStream_t s);
 cudaError_t launch_atomic_probe(double* buf, size_t n, int blocks, int per_thread,
                                 cudaStream_t s);
 int collide_blocks_per_sm(size_t smem);

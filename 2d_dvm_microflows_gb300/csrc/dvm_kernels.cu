@@ -2364,6 +2364,21 @@ __global__ void __launch_bounds__(256) k_atomic_probe(double* buf, size_t n, int
   }
 }
 
+// Failure-path check: waits on a barrier that nothing completes, with the bounded wait the
+// bulk-copy kernels use; the wait gives up and reports DVM_EW_WAIT in the error word.
+__global__ void k_wait_selftest(uint32_t* err) {
+  __shared__ __align__(8) uint64_t s_bar;
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+  __syncthreads();
+  if (!mbar_wait(&s_bar, 0u) && threadIdx.x == 0) atomicOr(err, static_cast<uint32_t>(DVM_EW_WAIT));
+  __syncthreads();
+}
+
+cudaError_t launch_wait_selftest(uint32_t* err, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_atomic_probe(double* buf, size_t n, int blocks, int per_thread,
                                 cudaStream_t s) {
   k_atomic_probe<<<blocks, 256, 0, s>>>(buf, n, per_thread);

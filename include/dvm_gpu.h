@@ -307,6 +307,11 @@ int dvm_flush_l2(dvm_ctx* ctx);
  * window_bytes of device memory: the roofline of a scatter whose target stays in L2.
  * Instrumentation; no reference counterpart. */
 int dvm_atomic_rate(dvm_ctx* ctx, uint64_t window_bytes, double* per_s);
+/* Failure-path check of the bounded device waits: runs a wait on a barrier that nothing
+ * completes, on the context's stream. The wait gives up after its bounded number of polls
+ * and sets DVM_EW_WAIT in the error word (read it with dvm_get_error_word); the context
+ * stays usable. */
+int dvm_wait_selftest(dvm_ctx* ctx);
 
 /* ---- collisions without device allocation ------------------------------------------ */
 /* No counterpart in the reference. The collision integral of dvm_compute_collision_integral

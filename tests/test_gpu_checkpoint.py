@@ -59,3 +59,18 @@ def test_restart_refuses_other_shapes(gpulib, pkg):
         other.restore(ck)
     with pytest.raises(pkg.DVMError):
         a.restore(b"not a checkpoint" * 100)
+
+
+def test_bounded_wait_reports_and_context_survives(gpulib, pkg):
+    """Failure detection without a fault: a device wait on a barrier that nothing completes
+    gives up after its bound and sets DVM_EW_WAIT; the context then steps normally."""
+    cfg, g, f0 = _drifting_relaxation(pkg)
+    s = pkg.DVMSolver(cfg, g)
+    s.initialize_dist_func(f0)
+    assert s.error_word() == 0
+    _ok = s.lib.dvm_wait_selftest(s.ctx)
+    assert _ok == 0
+    assert s.error_word() == pkg.DVM_EW_WAIT
+    s.solve(2)
+    assert s.error_word() == 0
+    assert np.isfinite(s.properties()[:, :17]).all()

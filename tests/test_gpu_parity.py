@@ -363,3 +363,78 @@ def test_philox_steps_larger_grid(gpulib, pkg, oracle, method):
     assert n == cpu.collision_count()
     assert 10 * 0.9 * n <= gpu.scatter_count() <= 16 * n
     assert gpu.error_word() == 0
+
+
+def _stretched_axis(n, vmax, beta=1.6):
+    """Nodes clustered near 0: vmax * tanh(beta s) / tanh(beta), s uniform on [-1, 1]."""
+    s = np.linspace(-1.0, 1.0, n)
+    return vmax * np.tanh(beta * s) / np.tanh(beta)
+
+
+@pytest.mark.parametrize("kind", ["noncubic", "stretched"])
+@pytest.mark.parametrize("method", ["VR", "FMC"])
+def test_philox_steps_irregular_grids(gpulib, pkg, oracle, kind, method):
+    """Grids the g-table and the uniform guesses do not cover: unequal axes (10 x 8 x 12
+    nodes over different ranges) and tanh-stretched axes. Steps agree within 1e-12."""
+    ph = pkg.physics
+    if kind == "noncubic":
+        g = ph.VelocityGrid(np.linspace(-5.0, 5.0, 10), np.linspace(-4.5, 4.5, 8),
+                            np.linspace(-5.5, 5.5, 12))
+    else:
+        g = ph.VelocityGrid(_stretched_axis(11, 5.0), _stretched_axis(11, 5.0, 1.2),
+                            _stretched_axis(13, 5.5))
+    f0 = np.stack([ph.bimodal(g, u1=0.6, T2=2.0), ph.bimodal(g, u1=-0.4, T2=1.5)])
+    coll = pkg.DVM_COLL_VR if method == "VR" else pkg.DVM_COLL_FMC
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, nx_space=2, iColl=coll,
+                            samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=15000,
+                            omega=0.81, seed=29, deltat=0.02, cdf_tolerance=0.01)
+    for _ in range(2):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+        assert gpu.scatter_count() == cpu.scatter_count()
+    assert props_err(gpu.properties(), cpu.properties()) <= 1e-11
+    assert gpu.error_word() == 0
+
+
+def test_longest_axis(gpulib, pkg, oracle):
+    """The largest axis the tables hold (128 nodes) works; one more is refused."""
+    ph = pkg.physics
+    g = ph.VelocityGrid(np.linspace(-6.0, 6.0, 128), np.linspace(-4.0, 4.0, 6),
+                        np.linspace(-4.0, 4.0, 6))
+    f0 = ph.bimodal(g, u1=0.8, T2=2.0)
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, iColl=pkg.DVM_COLL_VR,
+                            samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=10000,
+                            seed=31, deltat=0.02)
+    gpu.solve(1)
+    cpu.solve(1)
+    assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert gpu.error_word() == 0
+    g2 = ph.VelocityGrid(np.linspace(-6.0, 6.0, 129), np.linspace(-4.0, 4.0, 6),
+                         np.linspace(-4.0, 4.0, 6))
+    with pytest.raises(pkg.DVMError):
+        pkg.DVMSolver(pkg.DVMConfig(iColl=pkg.DVM_COLL_VR), g2)
+
+
+def test_empty_cell(gpulib, pkg, oracle):
+    """A cell with no molecules (as the restatement: zero density means zero moments, not an
+    error) draws no samples and stays empty; the other cells step as in the restatement."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -5.0, 5.0)
+    full = np.stack([ph.bimodal(g), ph.bimodal(g, u1=0.5)])
+    with_empty = np.stack([full[0], np.zeros(g.nv), full[1]])
+    kw = dict(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FORMULA, ColnRMS=0.05,
+              deltat=0.02, seed=37)
+    a = pkg.DVMSolver(pkg.DVMConfig(nx_space=3, **kw), g)
+    a.initialize_dist_func(with_empty)
+    assert a.error_word() == 0
+    a.compute_collision_integral(0)
+    pa = a.properties()
+    assert np.all(pa[1, :17] == 0.0)
+    assert np.all(a.phi()[1] == 0.0)
+    assert a.error_word() == 0
+    cpu = oracle.OracleSolver(pkg.DVMConfig(nx_space=3, **kw), g)
+    cpu.initialize_dist_func(with_empty)
+    cpu.compute_collision_integral(0)
+    assert rel_err(a.phi(), cpu.phi()) <= REL
+    assert a.collision_count() == cpu.collision_count()

@@ -438,3 +438,37 @@ def test_empty_cell(gpulib, pkg, oracle):
     cpu.compute_collision_integral(0)
     assert rel_err(a.phi(), cpu.phi()) <= REL
     assert a.collision_count() == cpu.collision_count()
+
+
+@pytest.mark.parametrize("geometry", ["2d", "1d"])
+def test_full_steps_stretched_grid(gpulib, pkg, oracle, geometry):
+    """Walls, ends, convection and collisions on a tanh-stretched velocity grid (node
+    spacings and the wall remaps no longer uniform), the exact-pi mode, partial
+    accommodation: several full steps agree with the restatement."""
+    ph = pkg.physics
+    g = ph.VelocityGrid(_stretched_axis(9, 4.5), _stretched_axis(9, 4.5, 1.3),
+                        _stretched_axis(10, 4.5))
+    common = dict(deltat=0.03, omega=0.81, iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                  samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=2500,
+                  pi_mode=pkg.DVM_PI_EXACT, seed=41)
+    if geometry == "2d":
+        nxs, nys = 4, 3
+        f0 = np.stack([ph.maxwellian(g, 1.0, 0.1 * c, 0.0, 0.0, 1.0 + 0.05 * c)
+                       for c in range(nxs * nys)])
+        walls = ((1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.1), (1, 0, 0, 0, 0.9), (1, 0.3, 0, 0, 1.0))
+        gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_2D, nx_space=nxs,
+                                ny_space=nys, dx=0.5, dy=0.5, Kn=0.2, acc_coeff=0.7,
+                                walls=walls, **common)
+    else:
+        f0, up, dn = ph.shock_profile(g, 8, 0.5, 1.6, 1.5)
+        walls = ((dn["n"], dn["u"], 0, 0, dn["T"]), (up["n"], up["u"], 0, 0, up["T"]),
+                 (1, 0, 0, 0, 1), (1, 0, 0, 0, 1))
+        gpu, cpu = pair_solvers(pkg, oracle, g, f0, geometry=pkg.DVM_GEOM_1D, nx_space=8,
+                                dx=0.5, walls=walls, acc_coeff=0.8,
+                                bc=(pkg.DVM_BC1D_DIFFUSE, pkg.DVM_BC1D_INOUT, 0, 0), **common)
+    for _ in range(3):
+        gpu.solve(1)
+        cpu.solve(1)
+        assert rel_err(gpu.phi(), cpu.phi()) <= REL
+    assert props_err(gpu.properties(), cpu.properties()) <= 1e-10
+    assert gpu.error_word() == 0

@@ -1652,20 +1652,26 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
   double tot[20];
   block_sum_dfl<20>(acc, s_red, tot);
   if (threadIdx.x == 0) {
-    // Cholesky of M; no correction if M is not positive definite (e.g. no collisions
-    // landed in this cell)
-    double M[5][5], L[5][5] = {{0}}, y[5], lam[5];
+    // Cholesky of M in FP32; no correction if M is not positive definite (e.g. no
+    // collisions landed in this cell). FP32 suffices: M only shapes the correction, whose
+    // values are formed in FP32 anyway, and M lambda = r to FP32 rounding leaves some 1e-7
+    // of a non-conservation that is itself some 1e-7 of the increment.
+    float M[5][5], L[5][5] = {{0.f}}, y[5], lam[5];
     int m = 5;
     for (int r = 0; r < 5; ++r)
-      for (int c = r; c < 5; ++c) { M[r][c] = tot[m]; M[c][r] = tot[m]; ++m; }
+      for (int c = r; c < 5; ++c) {
+        M[r][c] = static_cast<float>(tot[m]);
+        M[c][r] = M[r][c];
+        ++m;
+      }
     bool ok = true;
     for (int r = 0; r < 5 && ok; ++r) {
       for (int c = 0; c <= r; ++c) {
-        double sum = M[r][c];
+        float sum = M[r][c];
         for (int k = 0; k < c; ++k) sum -= L[r][k] * L[c][k];
         if (r == c) {
-          if (!(sum > 1e-300)) { ok = false; break; }
-          L[r][r] = sqrt(sum);
+          if (!(sum > 1e-30f)) { ok = false; break; }
+          L[r][r] = sqrtf(sum);
         } else {
           L[r][c] = sum / L[c][c];
         }
@@ -1673,19 +1679,19 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
     }
     if (ok) {
       for (int r = 0; r < 5; ++r) {
-        double sum = tot[r];
+        float sum = static_cast<float>(tot[r]);
         for (int k = 0; k < r; ++k) sum -= L[r][k] * y[k];
         y[r] = sum / L[r][r];
       }
       for (int r = 4; r >= 0; --r) {
-        double sum = y[r];
+        float sum = y[r];
         for (int k = r + 1; k < 5; ++k) sum -= L[k][r] * lam[k];
         lam[r] = sum / L[r][r];
       }
     } else {
-      for (int r = 0; r < 5; ++r) lam[r] = 0.0;
+      for (int r = 0; r < 5; ++r) lam[r] = 0.f;
     }
-    for (int r = 0; r < 5; ++r) s_lam[r] = static_cast<float>(lam[r]);
+    for (int r = 0; r < 5; ++r) s_lam[r] = isfinite(lam[r]) ? lam[r] : 0.f;
   }
   __syncthreads();
   const float l0 = s_lam[0], l1 = s_lam[1], l2 = s_lam[2], l3 = s_lam[3], l4 = s_lam[4];

@@ -2234,7 +2234,8 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
       return;  // (thread 0, after the block reduction)
     }
     const double m = a.mass;
-    const double dx = acc[1] / n, dy = acc[2] / n, dz = acc[3] / n;
+    const double inv_n = 1.0 / n;  // one FP64 division for the per-density quotients
+    const double dx = acc[1] * inv_n, dy = acc[2] * inv_n, dz = acc[3] * inv_n;
     const double d[3] = {dx, dy, dz};
     // central second moments C_ab = M_ab - n d_a d_b
     double C[3][3];
@@ -2253,13 +2254,13 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
       const double mix = d[0] * M1[ii][0] + d[1] * M1[ii][1] + d[2] * M1[ii][2];
       Q[ii] = T3 - 2.0 * mix - d[ii] * S2 + 2.0 * n * d[ii] * dd;
     }
-    const double t = 2.0 * m * (C[0][0] + C[1][1] + C[2][2]) / (3.0 * n);
+    const double t = 2.0 * m * (C[0][0] + C[1][1] + C[2][2]) * (inv_n * (1.0 / 3.0));
     const double p = 0.5 * n * t;
     P[DVM_P_DENS] = n;
     P[DVM_P_U] = u0 + dx; P[DVM_P_V] = v0 + dy; P[DVM_P_W] = w0 + dz;
     P[DVM_P_TEMP] = t;
     P[DVM_P_SPECIES_TEMP] = (3.0 * t + 0.0 * 0.0 + 0.0 * 0.0) / (3.0 + 0.0 + 0.0);
-    P[DVM_P_AVG_SPEED] = acc[13] / n;
+    P[DVM_P_AVG_SPEED] = acc[13] * inv_n;
     P[DVM_P_PRESSURE] = p;
     P[DVM_P_QX] = Q[0] * (0.5 * m); P[DVM_P_QY] = Q[1] * (0.5 * m); P[DVM_P_QZ] = Q[2] * (0.5 * m);
     P[DVM_P_TXX] = p - m * C[0][0]; P[DVM_P_TYY] = p - m * C[1][1]; P[DVM_P_TZZ] = p - m * C[2][2];
@@ -2271,11 +2272,11 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
     if (bad) atomicOr(a.err, bad);
     if (a.residual) {
       // relative change of n, u (on the thermal speed) and T since the last moments
-      const double su = sqrt(fabs(t) / m) + 1e-300;
-      double r = fabs(n - n_old) / fabs(n);
-      r = fmax(r, fabs(dx) / su);
-      r = fmax(r, fabs(dy) / su);
-      r = fmax(r, fabs(dz) / su);
+      const double isu = 1.0 / (sqrt(fabs(t) / m) + 1e-300);
+      double r = fabs(n - n_old) * fabs(inv_n);
+      r = fmax(r, fabs(dx) * isu);
+      r = fmax(r, fabs(dy) * isu);
+      r = fmax(r, fabs(dz) * isu);
       r = fmax(r, fabs(t - t_old) / (fabs(t) + 1e-300));
       // and of the shear stresses on the pressure (the only moments a homogeneous
       // relaxation changes)

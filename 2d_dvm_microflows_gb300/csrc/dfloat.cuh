@@ -248,4 +248,42 @@ __device__ __forceinline__ void block_sum_dfl(dacc (&v)[NV], float2* s_red, doub
   }
 }
 
+// Block-wide sums of NV pairs through shared memory: every thread stores its NV pairs,
+// then warp w sums quantities w, w + warps, ... (each lane a strided subset of the threads,
+// then a butterfly), so a thread does the butterfly for NV / warps quantities instead of
+// all NV. s_buf holds NV * blockDim.x float2, s_out NV float2; thread 0 gets the totals.
+template <int NV>
+__device__ __forceinline__ void block_sum_dfl_t(dacc (&v)[NV], float2* s_buf, float2* s_out,
+                                                double (&out)[NV]) {
+  const int t = threadIdx.x, nt = blockDim.x, lane = t & 31, warp = t >> 5, nw = nt >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const dfl x = dfl_norm(v[q].hi, v[q].lo);
+    s_buf[q * nt + t] = make_float2(x.hi, x.lo);
+  }
+  __syncthreads();
+  for (int q = warp; q < NV; q += nw) {
+    dacc acc;
+    dacc_zero(acc);
+    for (int i = lane; i < nt; i += 32) {
+      const float2 y = s_buf[q * nt + i];
+      dacc_add(acc, dfl_make(y.x, y.y));
+    }
+    dfl x = dfl_norm(acc.hi, acc.lo);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dfl y;
+      y.hi = __shfl_xor_sync(0xffffffffu, x.hi, o);
+      y.lo = __shfl_xor_sync(0xffffffffu, x.lo, o);
+      x = dfl_add(x, y);
+    }
+    if (lane == 0) s_out[q] = make_float2(x.hi, x.lo);
+  }
+  __syncthreads();
+  if (t == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) out[q] = dfl_to_double(dfl_make(s_out[q].x, s_out[q].y));
+  }
+}
+
 }  // namespace dvm

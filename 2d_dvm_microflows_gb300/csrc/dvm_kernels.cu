@@ -1650,7 +1650,10 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
     for (int q = 0; q < 15; ++q) acc[5 + q].hi += m[q];
   }
   double tot[20];
-  block_sum_dfl<20>(acc, s_red, tot);
+  {
+    __shared__ float2 s_sum[20 * kProjThreads];
+    block_sum_dfl_t<20>(acc, s_sum, s_red, tot);
+  }
   if (threadIdx.x == 0) {
     // Cholesky of M in FP32; no correction if M is not positive definite (e.g. no
     // collisions landed in this cell). FP32 suffices: M only shapes the correction, whose
@@ -2203,7 +2206,10 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
     dacc_add(sacc[13], dfl_norm(S.hi, S.lo));
   }
   double acc[kMomAcc];
-  block_sum_dfl<kMomAcc>(sacc, s_red, acc);
+  {
+    __shared__ float2 s_sum[kMomAcc * kMomThreads];
+    block_sum_dfl_t<kMomAcc>(sacc, s_sum, s_red, acc);
+  }
   if constexpr (kSplit) {
     __shared__ double s_part[kMomSplitMax][kMomAcc];  // used in the cluster's first CTA
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();

@@ -378,22 +378,49 @@ __global__ void __launch_bounds__(T) k_cdf(CdfArgs a) {
     const long long* cum = (ti == 0) ? ce : cd;
     const long long T = (ti == 0) ? carry_e : carry_d;
     const long long Tq = T / 1000, Tr = T % 1000;
-    for (int r = threadIdx.x + 1; r <= kNRef; r += kCdfThreads) {
-      const long long target = Tq * r + (Tr * r) / 1000;
-      int lo = 0, hi = ncoarse + 1;  // first coarse entry >= target
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (target > s_coarse[ti][mid]) lo = mid + 1; else hi = mid;
+    // a thread's targets (up to kPer) are searched in lockstep: the coarse index in shared
+    // memory first, then the fine searches in global memory advance together, so their
+    // dependent loads overlap instead of following one another
+    constexpr int kPer = (kNRef + kCdfThreads - 1) / kCdfThreads;
+    long long tg[kPer];
+    int plo[kPer], phi[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int r = threadIdx.x + 1 + j * kCdfThreads;
+      plo[j] = 1;
+      phi[j] = 1;  // empty: nothing to search
+      tg[j] = 0;
+      if (r <= kNRef) {
+        const long long target = Tq * r + (Tr * r) / 1000;
+        tg[j] = target;
+        int lo = 0, hi = ncoarse + 1;  // first coarse entry >= target
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (target > s_coarse[ti][mid]) lo = mid + 1; else hi = mid;
+        }
+        int pl = (lo == 0) ? 1 : (lo - 1) * cstep + 1;
+        int ph = (lo > ncoarse) ? nv : lo * cstep;
+        if (pl < 1) pl = 1;
+        plo[j] = pl;
+        phi[j] = ph > nv ? nv : ph;
       }
-      int plo = (lo == 0) ? 1 : (lo - 1) * cstep + 1;
-      int phi = (lo > ncoarse) ? nv : lo * cstep;
-      if (plo < 1) plo = 1;
-      phi = phi > nv ? nv : phi;
-      while (plo < phi) {  // first p in [plo, phi] with cum(p) >= target
-        const int mid = (plo + phi) >> 1;
-        if (target > cum[mid]) plo = mid + 1; else phi = mid;
+    }
+    for (int it = 0; it < 64; ++it) {  // first p in [plo, phi] with cum(p) >= target
+      bool open = false;
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        if (plo[j] < phi[j]) {
+          open = true;
+          const int mid = (plo[j] + phi[j]) >> 1;
+          if (tg[j] > cum[mid]) plo[j] = mid + 1; else phi[j] = mid;
+        }
       }
-      s_right[t][r - 1] = plo;
+      if (!open) break;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int r = threadIdx.x + 1 + j * kCdfThreads;
+      if (r <= kNRef) s_right[t][r - 1] = plo[j];
     }
   }
   __syncthreads();

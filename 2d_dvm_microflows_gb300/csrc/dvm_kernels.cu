@@ -45,29 +45,28 @@ __device__ long long num_coll_pairs(const CollParams& cp, double ct, double dens
   return llround(val);
 }
 
-// x 2^k truncated to an integer, for x >= 0, from the bits of x (no FP64 op). Terms that
-// would not fit below 2^62 are clamped and reported.
+// |x| 2^k truncated to an integer, from the bits of x (no FP64 op). Terms that would not
+// fit below 2^62 are clamped to 2^58 and reported; zero and FP64 subnormals give 0.
+// Without branches: the 53-bit significand is placed at bit 9 (a 62-bit integer) and
+// shifted right by 9 - sh, clamped to 63, which leaves 0 for every sh <= -54.
 __device__ __forceinline__ long long to_fixed(double x, int k, uint32_t& bad) {
   const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x)) &
                                0x7fffffffffffffffull;
   const int e = static_cast<int>(b >> 52);
-  if (e == 0) return 0;  // zero or FP64 subnormal
-  if (e == 2047) { bad |= DVM_EW_NONFINITE; return 1ll << 58; }
-  const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
   const int sh = e - 1075 + k;
-  if (sh >= 0) {
-    if (sh > 9) { bad |= DVM_EW_NONFINITE; return 1ll << 58; }
-    return static_cast<long long>(mant << sh);
-  }
-  if (sh <= -64) return 0;
-  return static_cast<long long>(mant >> (-sh));
+  const unsigned long long mant = ((b & ((1ull << 52) - 1)) | (1ull << 52)) << 9;
+  const int rs = min(max(9 - sh, 0), 63);
+  long long r = static_cast<long long>(mant >> rs);
+  if (e == 0) return 0;  // zero or FP64 subnormal
+  if (e == 2047 || sh > 9) { bad |= DVM_EW_NONFINITE; r = 1ll << 58; }
+  return r;
 }
 
 // x 2^k truncated towards zero, signed, for a double x (bit operations only).
 __device__ __forceinline__ long long to_fixed_s(double x, int k, uint32_t& bad) {
-  const unsigned long long sb = static_cast<unsigned long long>(__double_as_longlong(x));
-  const long long v = to_fixed(x, k, bad);  // |x| 2^k
-  return (sb >> 63) ? -v : v;
+  const long long sg = __double_as_longlong(x) >> 63;  // 0 or -1
+  const long long v = to_fixed(x, k, bad);              // |x| 2^k
+  return (v ^ sg) - sg;
 }
 
 // v 2^k truncated towards zero, signed, for a float v (bit operations only).
@@ -86,6 +85,22 @@ __device__ __forceinline__ long long to_fixed_f(float v, int k, uint32_t& bad) {
     r = (sh <= -64) ? 0ull : (m >> (-sh));
   }
   return (b >> 31) ? -static_cast<long long>(r) : static_cast<long long>(r);
+}
+
+// 2^a as a float, for -126 <= a <= 127.
+__device__ __forceinline__ float pow2f(int a) { return __int_as_float((a + 127) << 23); }
+
+// to_fixed_f through the FP32 multiplier, for a scale 2^k = s1 s2 with s1, s2 normal
+// powers of two: v s1 s2 is exact (flushing to zero drops only values below 2^-126, whose
+// truncation is 0, and a subnormal v gives 0 as above), |v| 2^k >= 2^62 is exactly the
+// overflow of to_fixed_f, and the conversion truncates towards zero.
+__device__ __forceinline__ long long to_fixed_f_mul(float v, float s1, float s2,
+                                                    uint32_t& bad) {
+  float p;
+  asm("mul.rn.ftz.f32 %0, %1, %2;" : "=f"(p) : "f"(v), "f"(s1));
+  asm("mul.rn.ftz.f32 %0, %0, %1;" : "+f"(p) : "f"(s2));
+  if (!(fabsf(p) < 0x1p62f)) { bad |= DVM_EW_NONFINITE; return 0; }
+  return __float2ll_rz(p);
 }
 
 // Sign of v as +-1.0f (the collision kernels read only the sign bit of kin).
@@ -142,7 +157,7 @@ __device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long
 // T threads per CTA (256, or 512 / 1024 for launches of few cells: the per-cell scan then
 // walks fewer, wider chunks).
 template <int T>
-__global__ void __launch_bounds__(T) k_cdf(CdfArgs a) {
+__global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
   constexpr int kCdfThreads = T;
   constexpr int kCdfChunk = T * kCdfPer;  // nodes per scan chunk
   // chunk staging: node m of a chunk sits at (m / kCdfPer) * kCdfPitch + m % kCdfPer, so
@@ -248,6 +263,10 @@ __global__ void __launch_bounds__(T) k_cdf(CdfArgs a) {
   // uses the scale of the cached equilibrium's density (the cache is renewed whenever
   // the density moves by more than cdf_tolerance, well inside the scale's 16x margin).
   const int kc = vr ? ke : k;
+  // the equilibrium's scale 2^ke as two float factors (every cell of a sane density; the
+  // bit-operation conversion covers the rest)
+  const bool mul_scale = (ke >= -252 && ke <= 252);
+  const float s1 = mul_scale ? pow2f(ke / 2) : 1.f, s2 = mul_scale ? pow2f(ke - ke / 2) : 1.f;
   // f arrives chunk by chunk in shared memory through bulk asynchronous copies, double
   // buffered so that the copy of the next chunk overlaps the scan of this one (a cell's
   // slab is contiguous; the copies need 16-byte alignment, i.e. an even node count)
@@ -299,7 +318,9 @@ __global__ void __launch_bounds__(T) k_cdf(CdfArgs a) {
           if (vr) {
             const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
                                    s_fac[2 * kMaxAxis + kk]);
-            const long long E = to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
+            const long long E =
+                mul_scale ? to_fixed_f_mul(ev.hi, s1, s2, bad) + to_fixed_f_mul(ev.lo, s1, s2, bad)
+                          : to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
             if (recompute) te = E;
             const long long d = F - E;
             kin[l + 1] = d < 0 ? -1.f : 1.f;

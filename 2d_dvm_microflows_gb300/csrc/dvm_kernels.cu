@@ -397,8 +397,8 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
     if (vr && t == 0 && !recompute) continue;  // cached equilibrium: table unchanged
     const int ti = (vr && t == 0) ? 0 : 1;
     const long long* cum = (ti == 0) ? ce : cd;
-    const long long T = (ti == 0) ? carry_e : carry_d;
-    const long long Tq = T / 1000, Tr = T % 1000;
+    const long long tot = (ti == 0) ? carry_e : carry_d;
+    const long long Tq = tot / 1000, Tr = tot % 1000;
     // a thread's targets (up to kPer) are searched in lockstep: the coarse index in shared
     // memory first, then the fine searches in global memory advance together, so their
     // dependent loads overlap instead of following one another
@@ -719,13 +719,22 @@ __device__ __forceinline__ dfl dfl_sqrt(dfl a) {
   return dfl_norm(s, __fmul_rn(r, 0.5f * y));
 }
 
+// Nearest integer (ties to even) of x, as __float2int_rn for |x| <= 2^22, by the FP32 adder:
+// x + 1.5 2^23 lies in [2^23, 2^24], where the float spacing is 1 and the even offset keeps
+// the parity of the tie rule. Larger |x| (and NaN) are clamped to +-2^22 first; the callers
+// clamp the result to an axis much shorter than that.
+__device__ __forceinline__ int round_small(float x) {
+  x = fminf(fmaxf(x, -4194304.f), 4194304.f);
+  return __float_as_int(__fadd_rn(x, 12582912.f)) - 0x4B400000;
+}
+
 // Nearest node, as nearest() but on pair keys.
 __device__ __forceinline__ int nearest_d(const SmemAxesD& A, int ax, dfl u, float vmin,
                                          float factor, int& corner, int& bad) {
   const int mx = A.n[ax] - 1;
   const long long* mid = A.mid[ax];
   const long long vk = dkey(u);
-  int o = __float2int_rn(factor * (u.hi - vmin));
+  int o = round_small(factor * (u.hi - vmin));
   o = o < 0 ? 0 : (o > mx ? mx : o);
   if (u.hi != u.hi) bad |= 1;
   int it = 0;
@@ -877,6 +886,51 @@ __device__ __forceinline__ dfl angle_fraction(double R, int& k) {
   return dfl_norm(fh * 0x1.0p-33f, fl * 0x1.0p-53f);
 }
 
+// Quotient n / d for 0 <= n < 2^22 (every node index: at most 128^3 nodes) from the float
+// reciprocal rd = 1/d: n is formed exactly by the FP32 adder, n rd lies within 2^-23
+// relative of n / d, so its truncation is the quotient or one below it, and one integer
+// step corrects it (no integer division sequence, no conversion instruction).
+static_assert(kMaxAxis * kMaxAxis * kMaxAxis < (1 << 22), "node indices must stay below 2^22");
+__device__ __forceinline__ int quot_small(int n, int d, float rd) {
+  const float nf = __fsub_rn(__int_as_float(0x4B000000 | n), 8388608.f);
+  int q = __float_as_int(__fadd_rz(__fmul_rn(nf, rd), 8388608.f)) - 0x4B000000;
+  if (n - q * d >= d) ++q;
+  return q;
+}
+
+// (i, j, k) of node l on an NX x NY x NZ grid, with the reciprocals of NX and NX NY.
+__device__ __forceinline__ void node_ijk(int l, int NX, int NXY, float rNX, float rNXY, int& i,
+                                         int& j, int& k) {
+  k = quot_small(l, NXY, rNXY);
+  const int r = l - k * NXY;
+  j = quot_small(r, NX, rNX);
+  i = r - j * NX;
+}
+
+// Visiting order of the sample chunks: chunk(pos) = pos P mod total, a bijection of
+// 0..total-1 for a prime P that does not divide total. A warp's positions advance by a fixed
+// stride, so its chunks follow a running sum mod total: one 64-bit remainder per thread at
+// the start instead of one per chunk.
+struct ChunkWalk {
+  unsigned long long cur = 0, step = 0;
+  __device__ ChunkWalk(long long pos0, long long stride, long long tot) {
+    if (tot <= 0) return;
+    const unsigned long long total = static_cast<unsigned long long>(tot);
+    const unsigned long long P = (total % 2147483647ull == 0) ? 2147483629ull : 2147483647ull;
+    const unsigned __int128 pm = P % total;
+    cur = static_cast<unsigned long long>(
+        (static_cast<unsigned __int128>(static_cast<unsigned long long>(pos0) % total) * pm) % total);
+    step = static_cast<unsigned long long>(
+        (static_cast<unsigned __int128>(static_cast<unsigned long long>(stride) % total) * pm) % total);
+  }
+  __device__ __forceinline__ long long next(long long tot) {
+    const unsigned long long c = cur;
+    cur += step;
+    if (cur >= static_cast<unsigned long long>(tot)) cur -= static_cast<unsigned long long>(tot);
+    return static_cast<long long>(c);
+  }
+};
+
 struct CollideSmem {
   size_t axes, axes_d, keys, tabs, gtab, trig, total;
 };
@@ -957,6 +1011,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   const dfl one_sixth = dfl_make(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 to 2^-50
 
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
+  const float rNX = 1.f / static_cast<float>(NX), rNXY = 1.f / static_cast<float>(NXY);
   const int nent = 3 * a.ncells;
   const long long total = a.chunk_off[nent];
   const bool vr = (a.cp.method == DVM_COLL_VR);
@@ -973,10 +1028,11 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   // 0..total-1), so the warps in flight at any moment work on many cells and their FP64
   // atomics spread over many f slabs instead of piling onto the busiest nodes of one cell
   const int wpb = blockDim.x >> 5;
-  for (long long pos = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
-       pos < total; pos += static_cast<long long>(gridDim.x) * wpb) {
-    const long long chunk = static_cast<long long>(
-        (static_cast<unsigned long long>(pos) * 2147483647ull) % static_cast<unsigned long long>(total));
+  const long long pos0 = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
+  const long long stride = static_cast<long long>(gridDim.x) * wpb;
+  ChunkWalk walk(pos0, stride, total);
+  for (long long pos = pos0; pos < total; pos += stride) {
+    const long long chunk = walk.next(total);
     int lo = 0, hi = nent;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -1008,8 +1064,9 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
                                   (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                   nv, rB, bad);
     }
-    const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
-    const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
+    int iA, jA, kA, iB, jB, kB;
+    node_ijk(lA, NX, NXY, rNX, rNXY, iA, jA, kA);
+    node_ijk(lB, NX, NXY, rNX, rNXY, iB, jB, kB);
     // compute_relative_velocity (collision_utilities.f90:188-218) and g^(2-2 omega)
     double gg, g_sigma;
     if (gtab) {
@@ -1040,7 +1097,9 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
     // replenish_collision elastic branch (replenishing_collisions.f90:206-249)
     dfl kr;
     {
-      const dfl t = dfl_from_double((NR == 1) ? kin : kin / static_cast<double>(NR));
+      double kin_r = kin;
+      if (NR != 1) kin_r = kin / static_cast<double>(NR);
+      const dfl t = dfl_from_double(kin_r);
       kr = dfl_norm(t.hi, t.lo);
     }
     // v_com of a like-species pair: (xi_A + xi_B) / 2
@@ -1204,7 +1263,7 @@ __device__ __forceinline__ int nearest_f(const SmemAxesF& A, int ax, float u, fl
   const int mx = A.n[ax] - 1;
   const int* mid = A.mid[ax];
   const int vk = okeyf(u);
-  int o = __float2int_rn(factor * (u - vmin));
+  int o = round_small(factor * (u - vmin));
   o = o < 0 ? 0 : (o > mx ? mx : o);
   if (u != u) bad |= 1;
   int it = 0;
@@ -1376,6 +1435,7 @@ struct F32Ctx {
   const float2* gtab;
   const float2* strig;
   float vhs, ralpha;
+  float rNX, rNXY;  // reciprocals of NX and NX NY
   bool vss, vr;
   int NR;
   uint32_t step;
@@ -1420,6 +1480,8 @@ __device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const Co
   c.vr = (a.cp.method == DVM_COLL_VR);
   c.NR = a.cp.num_repl;
   c.step = a.step_dev ? *a.step_dev : a.step;
+  c.rNX = 1.f / static_cast<float>(g.nx);
+  c.rNXY = 1.f / static_cast<float>(g.nx * g.ny);
   return c;
 }
 
@@ -1450,8 +1512,9 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
                                  (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
                                  nv, rB, bad);
   }
-  const int kA = lA / NXY, jA = (lA - kA * NXY) / NX, iA = lA - kA * NXY - jA * NX;
-  const int kB = lB / NXY, jB = (lB - kB * NXY) / NX, iB = lB - kB * NXY - jB * NX;
+  int iA, jA, kA, iB, jB, kB;
+  node_ijk(lA, NX, NXY, c.rNX, c.rNXY, iA, jA, kA);
+  node_ijk(lB, NX, NXY, c.rNX, c.rNXY, iB, jB, kB);
   const float xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
   const float xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
   float gg, g_sigma;
@@ -1551,10 +1614,11 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   uint32_t bad = 0;
   uint32_t nat = 0;  // FP32 adds into df by this thread
   const int wpb = blockDim.x >> 5;
-  for (long long pos = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
-       pos < total; pos += static_cast<long long>(gridDim.x) * wpb) {
-    const long long chunk = static_cast<long long>(
-        (static_cast<unsigned long long>(pos) * 2147483647ull) % static_cast<unsigned long long>(total));
+  const long long pos0 = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
+  const long long stride = static_cast<long long>(gridDim.x) * wpb;
+  ChunkWalk walk(pos0, stride, total);
+  for (long long pos = pos0; pos < total; pos += stride) {
+    const long long chunk = walk.next(total);
     int lo = 0, hi = nent;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;

@@ -32,7 +32,8 @@ namespace dvm {
 // bit for bit; the quantum 2^-k is below 1e-17 n, finer than the FP64 rounding of the
 // reference's running sum. The partner search (k_collide) then compares integers only.
 constexpr int kCdfPer = 4;
-constexpr int kCdfPitch = kCdfPer + 1;            // padded per-thread row in shared memory
+constexpr int kCdfPitch = kCdfPer + 1;  // padded row of a lane's values in the transpose
+constexpr int kCdfTrWarp = 2 * 32 * kCdfPitch + (32 * kCdfPitch + 1) / 2;  // words per warp
 constexpr int kCdfCoarseMax = 512;   // entries of the shared-memory coarse index per table
 
 // compute_num_coll_pairs, collisions/collision_utilities.f90:106-140 (n = m); ct is
@@ -103,6 +104,27 @@ __device__ __forceinline__ long long to_fixed_f_mul(float v, float s1, float s2,
   return __float2ll_rz(p);
 }
 
+// Quotient n / d for 0 <= n < 2^22 (every node index: at most 128^3 nodes) from the float
+// reciprocal rd = 1/d: n is formed exactly by the FP32 adder, n rd lies within 2^-23
+// relative of n / d, so its truncation is the quotient or one below it, and one integer
+// step corrects it (no integer division sequence, no conversion instruction).
+static_assert(kMaxAxis * kMaxAxis * kMaxAxis < (1 << 22), "node indices must stay below 2^22");
+__device__ __forceinline__ int quot_small(int n, int d, float rd) {
+  const float nf = __fsub_rn(__int_as_float(0x4B000000 | n), 8388608.f);
+  int q = __float_as_int(__fadd_rz(__fmul_rn(nf, rd), 8388608.f)) - 0x4B000000;
+  if (n - q * d >= d) ++q;
+  return q;
+}
+
+// (i, j, k) of node l on an NX x NY x NZ grid, with the reciprocals of NX and NX NY.
+__device__ __forceinline__ void node_ijk(int l, int NX, int NXY, float rNX, float rNXY, int& i,
+                                         int& j, int& k) {
+  k = quot_small(l, NXY, rNXY);
+  const int r = l - k * NXY;
+  j = quot_small(r, NX, rNX);
+  i = r - j * NX;
+}
+
 // Sign of v as +-1.0f (the collision kernels read only the sign bit of kin).
 __device__ __forceinline__ float sign_float(double v) {
   const uint32_t hi = static_cast<uint32_t>(__double_as_longlong(v) >> 32);
@@ -160,23 +182,19 @@ template <int T>
 __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
   constexpr int kCdfThreads = T;
   constexpr int kCdfChunk = T * kCdfPer;  // nodes per scan chunk
-  // chunk staging: node m of a chunk sits at (m / kCdfPer) * kCdfPitch + m % kCdfPer, so
-  // global memory is read and written in coalesced rows while each thread scans
-  // kCdfPer consecutive nodes
-  extern __shared__ __align__(16) long long s_stage[];  // 2 * kCdfThreads * kCdfPitch, 2 f chunks
-  long long* s_e = s_stage;
-  long long* s_d = s_stage + kCdfThreads * kCdfPitch;
-  double* s_f = reinterpret_cast<double*>(s_stage + 2 * kCdfThreads * kCdfPitch);
-  // the bucket tables are built after the scan, in the staging rows it no longer needs
-  int (*s_right)[kNRef] = reinterpret_cast<int (*)[kNRef]>(s_stage);
-  static_assert(2 * kNRef * sizeof(int) <= 2 * kCdfThreads * kCdfPitch * sizeof(long long),
-                "bucket tables must fit in the staging rows");
-  __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ long long s_scan[2][128];
   __shared__ double s_par[6];
   __shared__ int s_new, s_k, s_ke;
   __shared__ dfl s_fac[3 * kMaxAxis];
   __shared__ long long s_coarse[2][kCdfCoarseMax + 1];
+  __shared__ int s_right[2][kNRef];  // bucket boundaries right(r) of the two tables
+  // per warp: its 4 x 32 cumulative values of both CDFs and signs, transposed so that every
+  // store instruction writes 32 consecutive positions
+  extern __shared__ __align__(16) long long s_tr[];  // (T / 32) * kCdfTrWarp words
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long* tr_e = s_tr + warp * kCdfTrWarp;
+  long long* tr_d = tr_e + 32 * kCdfPitch;
+  float* tr_k = reinterpret_cast<float*>(tr_d + 32 * kCdfPitch);
   const GridInfo& g = a.g;
   const int cell = blockIdx.x;
   const int nv = g.nv;
@@ -254,9 +272,11 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
   }
   const int k = s_k, ke = s_ke;
   uint32_t bad = 0;
-  // deviation and CDFs: each thread takes kCdfPer consecutive nodes of a chunk, scans them
-  // in sequence, and the thread sums are scanned across the block (cumul_df of
-  // variance_reduction.f90:454-456, full_mc.f90:151-152)
+  // deviation and CDFs (cumul_df of variance_reduction.f90:454-456, full_mc.f90:151-152):
+  // each thread takes kCdfPer consecutive nodes of a chunk, forms and scans them in
+  // sequence, and the thread sums are scanned across the block. f is read straight into
+  // registers as 16-byte pairs (8-byte reads where a cell's slab is not 16-byte aligned),
+  // one chunk ahead of the one being scanned.
   // The node terms are formed without FP64 instructions: f enters the fixed point from
   // its bits, f_eq = e_x e_y e_z is a pair product converted to fixed point, and f - f_eq
   // and its magnitude are integer operations. For VR every term
@@ -267,117 +287,94 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
   // bit-operation conversion covers the rest)
   const bool mul_scale = (ke >= -252 && ke <= 252);
   const float s1 = mul_scale ? pow2f(ke / 2) : 1.f, s2 = mul_scale ? pow2f(ke - ke / 2) : 1.f;
-  // f arrives chunk by chunk in shared memory through bulk asynchronous copies, double
-  // buffered so that the copy of the next chunk overlaps the scan of this one (a cell's
-  // slab is contiguous; the copies need 16-byte alignment, i.e. an even node count)
-  const bool bulk = (nv % 2 == 0);
-  if (bulk && threadIdx.x == 0) {
-    mbar_init(&s_bar[0], 1);
-    mbar_init(&s_bar[1], 1);
-    fence_proxy_async();
-    bulk_load(s_f, f, static_cast<uint32_t>(min(kCdfChunk, nv)) * 8u, &s_bar[0]);
-  }
-  __syncthreads();
-  uint32_t parity[2] = {0u, 0u};
-  int chunk_no = 0;
-  // (i, j, k) steps of a row of kCdfThreads nodes
   const int NY = g.ny;
-  const int st_i = kCdfThreads % NX, st_j = (kCdfThreads / NX) % NY, st_k = kCdfThreads / NXY;
-  long long carry_e = 0, carry_d = 0;
-  for (int base = 0; base < nv; base += kCdfChunk, ++chunk_no) {
-    const int buf = chunk_no & 1;
-    const double* fchunk = s_f + buf * kCdfChunk;
-    if (bulk) {
-      if (threadIdx.x == 0 && base + kCdfChunk < nv) {
-        // the other buffer was last read before the barrier that ended the previous chunk
-        fence_proxy_async();
-        bulk_load(s_f + (buf ^ 1) * kCdfChunk, f + base + kCdfChunk,
-                  static_cast<uint32_t>(min(kCdfChunk, nv - base - kCdfChunk)) * 8u,
-                  &s_bar[buf ^ 1]);
-      }
-      if (!mbar_wait(&s_bar[buf], parity[buf])) bad |= DVM_EW_WAIT;
-      parity[buf] ^= 1u;
-    }
-    // 1. node terms in coalesced rows: f and f_eq to fixed point, kin, the cached f_eq
-    {
-      int ii = 0, jj = 0, kk = 0;
-      if (vr) {
-        const int l0 = base + threadIdx.x;
-        kk = l0 / NXY;
-        jj = (l0 - kk * NXY) / NX;
-        ii = l0 - kk * NXY - jj * NX;
-      }
-#pragma unroll 4
-      for (int r = 0; r < kCdfPer; ++r) {
-        const int m = threadIdx.x + r * kCdfThreads;
-        const int l = base + m;
-        long long te = 0, td = 0;
-        if (l < nv) {
-          const double fv = bulk ? fchunk[m] : f[l];
-          const long long F = to_fixed_s(fv, kc, bad);
-          if (vr) {
-            const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
-                                   s_fac[2 * kMaxAxis + kk]);
-            const long long E =
-                mul_scale ? to_fixed_f_mul(ev.hi, s1, s2, bad) + to_fixed_f_mul(ev.lo, s1, s2, bad)
-                          : to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
-            if (recompute) te = E;
-            const long long d = F - E;
-            kin[l + 1] = d < 0 ? -1.f : 1.f;
-            td = d < 0 ? -d : d;
-          } else {
-            kin[l + 1] = sign_float(fv);
-            td = F < 0 ? -F : F;
-          }
-        }
-        const int pos = (m / kCdfPer) * kCdfPitch + (m % kCdfPer);
-        s_e[pos] = te;
-        s_d[pos] = td;
-        if (vr) {
-          ii += st_i; if (ii >= NX) { ii -= NX; ++jj; }
-          jj += st_j; if (jj >= NY) { jj -= NY; ++kk; }
-          kk += st_k;
-        }
-      }
-    }
-    __syncthreads();
-    // 2. each thread scans its kCdfPer consecutive nodes, the block scans the thread sums
-    long long pe[kCdfPer], ad[kCdfPer];
-    const int row = threadIdx.x * kCdfPitch;
+  const float rNX = 1.f / static_cast<float>(NX), rNXY = 1.f / static_cast<float>(NXY);
+  const bool pairs = (reinterpret_cast<uintptr_t>(f) & 15u) == 0;
+  auto load_f = [&](int base, double (&v)[kCdfPer]) {
+    const int l0 = base + static_cast<int>(threadIdx.x) * kCdfPer;
+    if (pairs && l0 + kCdfPer <= nv) {
 #pragma unroll
-    for (int q = 0; q < kCdfPer; ++q) {
-      pe[q] = s_e[row + q] + (q ? pe[q - 1] : 0);
-      ad[q] = s_d[row + q] + (q ? ad[q - 1] : 0);
+      for (int r = 0; r < kCdfPer; r += 2) {
+        const double2 q = __ldg(reinterpret_cast<const double2*>(f + l0 + r));
+        v[r] = q.x;
+        v[r + 1] = q.y;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < kCdfPer; ++r) v[r] = (l0 + r < nv) ? __ldg(f + l0 + r) : 0.0;
     }
+  };
+  double fv[kCdfPer];
+  load_f(0, fv);
+  long long carry_e = 0, carry_d = 0;
+  for (int base = 0; base < nv; base += kCdfChunk) {
+    double fn[kCdfPer];
+    if (base + kCdfChunk < nv) load_f(base + kCdfChunk, fn);
+    const int l0 = base + static_cast<int>(threadIdx.x) * kCdfPer;
+    int ii = 0, jj = 0, kk = 0;
+    if (vr && l0 < nv) node_ijk(l0, NX, NXY, rNX, rNXY, ii, jj, kk);
+    long long pe[kCdfPer], ad[kCdfPer];
+#pragma unroll
+    for (int r = 0; r < kCdfPer; ++r) {
+      const int l = l0 + r;
+      long long te = 0, td = 0;
+      if (l < nv) {
+        const long long F = to_fixed_s(fv[r], kc, bad);
+        if (vr) {
+          const dfl ev = dfl_mul(dfl_mul(s_fac[ii], s_fac[kMaxAxis + jj]),
+                                 s_fac[2 * kMaxAxis + kk]);
+          const long long E =
+              mul_scale ? to_fixed_f_mul(ev.hi, s1, s2, bad) + to_fixed_f_mul(ev.lo, s1, s2, bad)
+                        : to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
+          if (recompute) te = E;
+          const long long d = F - E;
+          tr_k[lane * kCdfPitch + r] = d < 0 ? -1.f : 1.f;
+          td = d < 0 ? -d : d;
+          if (++ii == NX) { ii = 0; if (++jj == NY) { jj = 0; ++kk; } }
+        } else {
+          tr_k[lane * kCdfPitch + r] = sign_float(fv[r]);
+          td = F < 0 ? -F : F;
+        }
+      }
+      pe[r] = te + (r ? pe[r - 1] : 0);
+      ad[r] = td + (r ? ad[r - 1] : 0);
+    }
+    // the scan's shared words are rewritten by the next chunk only after every thread has
+    // passed this chunk's second barrier, i.e. read its totals
     long long oe = pe[kCdfPer - 1], od = ad[kCdfPer - 1], te, td;
     block_scan2_i64(oe, od, te, td, &s_scan[0][0]);
     oe += carry_e;
     od += carry_d;
+    // the cumulative sums at positions p = node + 1 and the signs, through the warp's
+    // transpose, and the coarse index
 #pragma unroll
-    for (int q = 0; q < kCdfPer; ++q) {
-      s_e[row + q] = oe + pe[q];
-      s_d[row + q] = od + ad[q];
-    }
-    __syncthreads();
-    // 3. coalesced stores of the cumulative sums (position p = node + 1) and the coarse index
-#pragma unroll 4
     for (int r = 0; r < kCdfPer; ++r) {
-      const int m = threadIdx.x + r * kCdfThreads;
-      const int p = base + m + 1;
+      tr_e[lane * kCdfPitch + r] = oe + pe[r];
+      tr_d[lane * kCdfPitch + r] = od + ad[r];
+    }
+    __syncwarp();
+    const int wbase = base + warp * 32 * kCdfPer;
+#pragma unroll
+    for (int r = 0; r < kCdfPer; ++r) {
+      const int v = r * 32 + lane;
+      const int p = wbase + v + 1;
       if (p <= nv) {
-        const int pos = (m / kCdfPer) * kCdfPitch + (m % kCdfPer);
-        const long long ve = s_e[pos], vd = s_d[pos];
+        const int idx = (v / kCdfPer) * kCdfPitch + v % kCdfPer;
+        const long long ve = tr_e[idx], vd = tr_d[idx];
         if (recompute) ce[p] = ve;
         cd[p] = vd;
+        kin[p] = tr_k[idx];
         if ((p & (cstep - 1)) == 0) {
           s_coarse[0][p / cstep] = ve;
           s_coarse[1][p / cstep] = vd;
         }
       }
     }
+    __syncwarp();  // the transpose is rewritten by the next chunk
     carry_e += te;
     carry_d += td;
-    __syncthreads();  // s_e, s_d and s_scan are reused by the next chunk
+#pragma unroll
+    for (int r = 0; r < kCdfPer; ++r) fv[r] = fn[r];
   }
   if (threadIdx.x == 0) {
     if (recompute) ce[0] = 0;
@@ -521,8 +518,7 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
 
 template <int T>
 static cudaError_t launch_cdf_t(const CdfArgs& a, cudaStream_t s) {
-  constexpr int smem = 2 * T * kCdfPitch * static_cast<int>(sizeof(long long)) +
-                       2 * T * kCdfPer * static_cast<int>(sizeof(double));
+  constexpr int smem = (T / 32) * kCdfTrWarp * static_cast<int>(sizeof(long long));
   const cudaError_t e = cudaFuncSetAttribute(k_cdf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   k_cdf<T><<<a.ncells, T, smem, s>>>(a);
@@ -884,27 +880,6 @@ __device__ __forceinline__ dfl angle_fraction(double R, int& k) {
   const float fh = __fsub_rn(__int_as_float(static_cast<int>(0x4B000000u | th)), 8388608.f);
   const float fl = __fsub_rn(__int_as_float(static_cast<int>(0x4B000000u | tl)), 8388608.f);
   return dfl_norm(fh * 0x1.0p-33f, fl * 0x1.0p-53f);
-}
-
-// Quotient n / d for 0 <= n < 2^22 (every node index: at most 128^3 nodes) from the float
-// reciprocal rd = 1/d: n is formed exactly by the FP32 adder, n rd lies within 2^-23
-// relative of n / d, so its truncation is the quotient or one below it, and one integer
-// step corrects it (no integer division sequence, no conversion instruction).
-static_assert(kMaxAxis * kMaxAxis * kMaxAxis < (1 << 22), "node indices must stay below 2^22");
-__device__ __forceinline__ int quot_small(int n, int d, float rd) {
-  const float nf = __fsub_rn(__int_as_float(0x4B000000 | n), 8388608.f);
-  int q = __float_as_int(__fadd_rz(__fmul_rn(nf, rd), 8388608.f)) - 0x4B000000;
-  if (n - q * d >= d) ++q;
-  return q;
-}
-
-// (i, j, k) of node l on an NX x NY x NZ grid, with the reciprocals of NX and NX NY.
-__device__ __forceinline__ void node_ijk(int l, int NX, int NXY, float rNX, float rNXY, int& i,
-                                         int& j, int& k) {
-  k = quot_small(l, NXY, rNXY);
-  const int r = l - k * NXY;
-  j = quot_small(r, NX, rNX);
-  i = r - j * NX;
 }
 
 // Visiting order of the sample chunks: chunk(pos) = pos P mod total, a bijection of

@@ -1966,7 +1966,8 @@ __device__ __forceinline__ int axis_class(int i, int neg, int pos, int zero, int
 // (about 2^-46 relative per step) with one FP64 add to form the output. A thread owns one
 // (i, j) column of the cell's slab and walks it along k, so the upwind choice, the CFL
 // factors and the perimeter classification are worked out once per column.
-constexpr int kConvThreads = 128;
+constexpr int kConvThreads = 256;  // at most; launched as wide as column_threads says
+constexpr int kConvAhead = 4;      // column nodes read ahead of the update
 
 __global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
   const GridInfo& g = a.g;
@@ -2021,14 +2022,38 @@ __global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
   const float2 cxf = __ldg(a.cfl + i), cyf = __ldg(a.cfl + NX + j);
   const dfl AX = dfl_make(cxf.x, cxf.y), AY = dfl_make(cyf.x, cyf.y);
   if (hx && hy && px && py) {
-    // both upwind sources present (every interior column): no per-node tests
-#pragma unroll 4
-    for (int k = 0; k < NZ; ++k) {
-      const size_t o = static_cast<size_t>(NXY) * k;
-      const dfl F0 = dfl_from_double(f0p[o]);
-      const dfl acc = dfl_add(dfl_add(F0, dfl_mul(AX, dfl_sub(dfl_from_double(px[o]), F0))),
-                              dfl_mul(AY, dfl_sub(dfl_from_double(py[o]), F0)));
-      out[o] = dfl_to_double_fast(acc);
+    // both upwind sources present (every interior column): no per-node tests; the three
+    // values of the next kConvAhead nodes are read while these are formed, so every thread
+    // keeps 3 kConvAhead loads in flight
+    double b0[kConvAhead], bx[kConvAhead], by[kConvAhead];
+#pragma unroll
+    for (int u = 0; u < kConvAhead; ++u) {
+      const size_t o = static_cast<size_t>(NXY) * u;
+      b0[u] = (u < NZ) ? __ldg(f0p + o) : 0.0;
+      bx[u] = (u < NZ) ? __ldg(px + o) : 0.0;
+      by[u] = (u < NZ) ? __ldg(py + o) : 0.0;
+    }
+    for (int k0 = 0; k0 < NZ; k0 += kConvAhead) {
+      double n0[kConvAhead], nx[kConvAhead], ny[kConvAhead];
+#pragma unroll
+      for (int u = 0; u < kConvAhead; ++u) {
+        const int k = k0 + kConvAhead + u;
+        const size_t o = static_cast<size_t>(NXY) * k;
+        n0[u] = (k < NZ) ? __ldg(f0p + o) : 0.0;
+        nx[u] = (k < NZ) ? __ldg(px + o) : 0.0;
+        ny[u] = (k < NZ) ? __ldg(py + o) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kConvAhead; ++u) {
+        const int k = k0 + u;
+        if (k >= NZ) break;
+        const dfl F0 = dfl_from_double(b0[u]);
+        const dfl acc = dfl_add(dfl_add(F0, dfl_mul(AX, dfl_sub(dfl_from_double(bx[u]), F0))),
+                                dfl_mul(AY, dfl_sub(dfl_from_double(by[u]), F0)));
+        out[static_cast<size_t>(NXY) * k] = dfl_to_double_fast(acc);
+      }
+#pragma unroll
+      for (int u = 0; u < kConvAhead; ++u) { b0[u] = n0[u]; bx[u] = nx[u]; by[u] = ny[u]; }
     }
     return;
   }
@@ -2046,8 +2071,10 @@ __global__ void __launch_bounds__(kConvThreads) k_convect2d(Convect2DArgs a) {
 }
 
 cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s) {
-  dim3 grid((a.g.nx * a.g.ny + kConvThreads - 1) / kConvThreads, ncells);
-  k_convect2d<<<grid, kConvThreads, 0, s>>>(a);
+  // a cell's columns in equal CTAs of whole warps (576 columns: 3 x 192, not 4.5 x 128)
+  const int threads = column_threads(a.g, kConvThreads);
+  dim3 grid((a.g.nx * a.g.ny + threads - 1) / threads, ncells);
+  k_convect2d<<<grid, threads, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -2206,9 +2233,10 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 // about 47 bits; only the per-thread totals go back to FP64 for the block reduction.
 constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
+constexpr int kMomAhead = 6;  // column nodes read ahead of the sums
 
-// The moments of one cell; src.begin(col) opens an (i, j) column and src.value(k) returns
-// the value of its node k as a pair. With kSplit, the cell's columns are dealt over the
+// The moments of one cell; src.begin(col) opens an (i, j) column and src.raw(k) returns
+// the value of its node k. With kSplit, the cell's columns are dealt over the
 // CTAs of a thread-block cluster (few cells: more CTAs than cells fill the SMs); each CTA
 // reduces its columns and the partial totals meet in the shared memory of the cluster's
 // first CTA, which adds them in rank order and forms the properties.
@@ -2258,16 +2286,30 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
     dacc G0, G1, G2, G3, S;
     dacc_zero(G0); dacc_zero(G1); dacc_zero(G2); dacc_zero(G3); dacc_zero(S);
     src.begin(col);
-#pragma unroll 4
-    for (int k = 0; k < NZ; ++k) {
-      const int l = col + NXY * k;
-      const dfl fv = src.value(k);
-      dacc_add(G0, fv);
-      dacc_fma(G1, fv, s_z[k]);
-      dacc_fma(G2, fv, s_z[kMaxAxis + k]);
-      dacc_fma(G3, fv, s_z[2 * kMaxAxis + k]);
-      const float2 sp = __ldg(speed + l);
-      dacc_fma(S, fv, dfl_make(sp.x, sp.y));
+    // the column's values are read kMomAhead nodes ahead of the ones being summed, so that
+    // every thread keeps that many loads in flight
+    double fb[kMomAhead];
+#pragma unroll
+    for (int u = 0; u < kMomAhead; ++u) fb[u] = (u < NZ) ? src.raw(u) : 0.0;
+    for (int k0 = 0; k0 < NZ; k0 += kMomAhead) {
+      double fn[kMomAhead];
+#pragma unroll
+      for (int u = 0; u < kMomAhead; ++u)
+        fn[u] = (k0 + kMomAhead + u < NZ) ? src.raw(k0 + kMomAhead + u) : 0.0;
+#pragma unroll
+      for (int u = 0; u < kMomAhead; ++u) {
+        const int k = k0 + u;
+        if (k >= NZ) break;
+        const dfl fv = dfl_from_double(fb[u]);
+        dacc_add(G0, fv);
+        dacc_fma(G1, fv, s_z[k]);
+        dacc_fma(G2, fv, s_z[kMaxAxis + k]);
+        dacc_fma(G3, fv, s_z[2 * kMaxAxis + k]);
+        const float2 sp = __ldg(speed + col + NXY * k);
+        dacc_fma(S, fv, dfl_make(sp.x, sp.y));
+      }
+#pragma unroll
+      for (int u = 0; u < kMomAhead; ++u) fb[u] = fn[u];
     }
     const int j = col / NX, i = col - j * NX;
     const dfl X = s_ax[i], X2 = s_ax[kMaxAxis + i];
@@ -2390,7 +2432,7 @@ struct MomSourceF {
   const double* f;
   int NXY, col;
   __device__ void begin(int c) { col = c; }
-  __device__ dfl value(int k) const { return dfl_from_double(f[col + NXY * k]); }
+  __device__ double raw(int k) const { return __ldg(f + col + NXY * k); }
 };
 
 __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {

@@ -1659,6 +1659,9 @@ static int column_threads(const GridInfo& g, int max_threads) {
   return ((per + 31) / 32) * 32;
 }
 
+constexpr int kProjAhead1 = 8;  // column increments read ahead of the sums
+constexpr int kProjAhead2 = 4;  // column nodes read ahead of the update
+
 // The projection of one cell, for the block: df (global or shared) is read, its projected
 // value added to f, and df zeroed when it is the global increment buffer.
 __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool zero_df,
@@ -1700,9 +1703,20 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
     dacc D0, D1, D2;
     dacc_zero(D0); dacc_zero(D1); dacc_zero(D2);
     float W0 = 0.f, W1 = 0.f, W2 = 0.f, W3 = 0.f, W4 = 0.f;
-#pragma unroll 4
-    for (int k = 0; k < NZ; ++k) {
-      const float d = df[col + NXY * k];
+    // the column's increments are read kProjAhead1 nodes ahead of the sums
+    float fb[kProjAhead1];
+#pragma unroll
+    for (int u = 0; u < kProjAhead1; ++u) fb[u] = (u < NZ) ? df[col + NXY * u] : 0.f;
+    for (int k0 = 0; k0 < NZ; k0 += kProjAhead1) {
+      float fn[kProjAhead1];
+#pragma unroll
+      for (int u = 0; u < kProjAhead1; ++u)
+        fn[u] = (k0 + kProjAhead1 + u < NZ) ? df[col + NXY * (k0 + kProjAhead1 + u)] : 0.f;
+#pragma unroll
+      for (int u = 0; u < kProjAhead1; ++u) {
+      const int k = k0 + u;
+      if (k >= NZ) break;
+      const float d = fb[u];
       if (d == 0.f) continue;
       const dfl dd = dfl_make(d, 0.f);
       dacc_add(D0, dd);
@@ -1714,6 +1728,9 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
       W2 = fmaf(wt, s_zf[kMaxAxis + k], W2);
       W3 = fmaf(wt, s_zf[2 * kMaxAxis + k], W3);
       W4 = fmaf(wt, s_zf[3 * kMaxAxis + k], W4);
+      }
+#pragma unroll
+      for (int u = 0; u < kProjAhead1; ++u) fb[u] = fn[u];
     }
     const int j = col / NX, i = col - j * NX;
     const dfl X = s_axd[i], Y = s_axd[kMaxAxis + j];
@@ -1789,15 +1806,37 @@ __device__ __forceinline__ void project_cell(const GridInfo& g, float* df, bool 
     const int j = col / NX, i = col - j * NX;
     const float X = s_axf[i], Y = s_axf[kMaxAxis + j];
     const float base = fmaf(l4, X * X + Y * Y, fmaf(l2, Y, fmaf(l1, X, l0)));
-#pragma unroll 4
-    for (int k = 0; k < NZ; ++k) {
-      const int l = col + NXY * k;
-      const float d = df[l];
-      if (d == 0.f) continue;
-      const float poly = fmaf(l4, s_zf[kMaxAxis + k], fmaf(l3, s_zf[k], base));
-      const float corr = fabsf(d) * poly;
-      f[l] = (f[l] + dbl_from_float_fast(d)) - dbl_from_float_fast(corr);
-      if (zero_df) df[l] = 0.f;
+    // increments and f read kProjAhead2 nodes ahead of the update
+    float db[kProjAhead2];
+    double fbb[kProjAhead2];
+#pragma unroll
+    for (int u = 0; u < kProjAhead2; ++u) {
+      db[u] = (u < NZ) ? df[col + NXY * u] : 0.f;
+      fbb[u] = (u < NZ) ? f[col + NXY * u] : 0.0;
+    }
+    for (int k0 = 0; k0 < NZ; k0 += kProjAhead2) {
+      float dn[kProjAhead2];
+      double fnn[kProjAhead2];
+#pragma unroll
+      for (int u = 0; u < kProjAhead2; ++u) {
+        const int k = k0 + kProjAhead2 + u;
+        dn[u] = (k < NZ) ? df[col + NXY * k] : 0.f;
+        fnn[u] = (k < NZ) ? f[col + NXY * k] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kProjAhead2; ++u) {
+        const int k = k0 + u;
+        if (k >= NZ) break;
+        const int l = col + NXY * k;
+        const float d = db[u];
+        if (d == 0.f) continue;
+        const float poly = fmaf(l4, s_zf[kMaxAxis + k], fmaf(l3, s_zf[k], base));
+        const float corr = fabsf(d) * poly;
+        f[l] = (fbb[u] + dbl_from_float_fast(d)) - dbl_from_float_fast(corr);
+        if (zero_df) df[l] = 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < kProjAhead2; ++u) { db[u] = dn[u]; fbb[u] = fnn[u]; }
     }
   }
 }
@@ -2233,7 +2272,7 @@ cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
 // about 47 bits; only the per-thread totals go back to FP64 for the block reduction.
 constexpr int kMomThreads = 256;
 constexpr int kMomAcc = 14;
-constexpr int kMomAhead = 6;  // column nodes read ahead of the sums
+constexpr int kMomAhead = 4;  // column nodes read ahead of the sums
 
 // The moments of one cell; src.begin(col) opens an (i, j) column and src.raw(k) returns
 // the value of its node k. With kSplit, the cell's columns are dealt over the

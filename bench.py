@@ -342,7 +342,7 @@ def one_step_error(pkg, cfg, g, f0, steps_before=3):
 
 
 def run_cavity(pkg, args):
-    """Configuration 3 in the precision form and in FP64 from the same start and seed."""
+    """The 2-D microcavity in the precision form and in FP64 from the same start and seed."""
     import dataclasses
     cfg, g, f0 = cavity_config(pkg)
     res = {}

@@ -741,26 +741,37 @@ __device__ __forceinline__ int nearest_d(const SmemAxesD& A, int ax, dfl u, floa
   return o;
 }
 
-// Per-axis terms of the remap: interior difference, its reciprocal, exterior difference
-// and denominator term.
-__device__ __forceinline__ void axis_terms(const SmemAxesD& A, int ax, int o, int s, int avail,
-                                           dfl& int_d, dfl& inv_d, dfl& ext_d, dfl& t_d) {
-  const dfl zero = dfl_make(0.f, 0.f);
-  ext_d = zero;
-  t_d = zero;
+// Per-axis terms of the remap, in two parts so that each is loaded when it is needed:
+// the interior difference and the denominator term (for f_e), then the reciprocal of the
+// interior difference and the exterior difference (for the axis weight).
+__device__ __forceinline__ void axis_den(const SmemAxesD& A, int ax, int o, int s, int avail,
+                                         dfl& int_d, dfl& t_d) {
+  t_d = dfl_make(0.f, 0.f);
   if (s >= -kTabS && s <= kTabS) {
     const AxisEntryD& e = A.tab[ax][o];
     int_d = e.D[kTabS + s];
-    inv_d = e.invD[kTabS + s];
-    if (avail) { ext_d = e.D[kTabS - s]; t_d = e.T[kTabS + s]; }
+    if (avail) t_d = e.T[kTabS + s];
   } else {
     const dfl* v = A.v[ax];
     int_d = dfl_sub(v[o + s], v[o]);
-    inv_d = dfl_div(dfl_make(1.f, 0.f), int_d);
     if (avail) {
-      ext_d = dfl_sub(v[o - s], v[o]);
+      const dfl ext_d = dfl_sub(v[o - s], v[o]);
       t_d = dfl_mul(ext_d, dfl_sub(ext_d, int_d));
     }
+  }
+}
+
+__device__ __forceinline__ void axis_ext(const SmemAxesD& A, int ax, int o, int s, int avail,
+                                         dfl& inv_d, dfl& ext_d) {
+  ext_d = dfl_make(0.f, 0.f);
+  if (s >= -kTabS && s <= kTabS) {
+    const AxisEntryD& e = A.tab[ax][o];
+    inv_d = e.invD[kTabS + s];
+    if (avail) ext_d = e.D[kTabS - s];
+  } else {
+    const dfl* v = A.v[ax];
+    inv_d = dfl_div(dfl_make(1.f, 0.f), dfl_sub(v[o + s], v[o]));
+    if (avail) ext_d = dfl_sub(v[o - s], v[o]);
   }
 }
 
@@ -801,15 +812,15 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   const int fx = (o_i - sa <= i_max && o_i - sa >= 0);
   const int fy = (o_j - sb <= j_max && o_j - sb >= 0);
   const int fz = (o_k - sc <= k_max && o_k - sc >= 0);
-  dfl int_x, inv_x, ext_x, t_x, int_y, inv_y, ext_y, t_y, int_z, inv_z, ext_z, t_z;
-  axis_terms(A, 0, o_i, sa, fx, int_x, inv_x, ext_x, t_x);
-  axis_terms(A, 1, o_j, sb, fy, int_y, inv_y, ext_y, t_y);
-  axis_terms(A, 2, o_k, sc, fz, int_z, inv_z, ext_z, t_z);
   const dfl zero = dfl_make(0.f, 0.f);
   dfl f_e = zero;
   if (!(fx | fy | fz)) {
     bad |= 2;
   } else {
+    dfl int_x, t_x, int_y, t_y, int_z, t_z;
+    axis_den(A, 0, o_i, sa, fx, int_x, t_x);
+    axis_den(A, 1, o_j, sb, fy, int_y, t_y);
+    axis_den(A, 2, o_k, sc, fz, int_z, t_z);
     // (a^2 + b^2 + c^2 - a int_x - b int_y - c int_z) / den, den = the available T terms
     const dfl num = dfl_add(dfl_add(dfl_mul(a, dfl_sub(a, int_x)), dfl_mul(b, dfl_sub(b, int_y))),
                             dfl_mul(c, dfl_sub(c, int_z)));
@@ -838,16 +849,22 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
     sum = dfl_add(sum, f_e);
   }
   {
+    dfl inv_x, ext_x;
+    axis_ext(A, 0, o_i, sa, fx, inv_x, ext_x);
     const dfl f_ix = dfl_mul(dfl_sub(a, fx ? dfl_mul(f_e, ext_x) : zero), inv_x);
     atomicAdd(f + base + sa, dfl_to_double_normal(dfl_mul(w8, f_ix)));
     sum = dfl_add(sum, f_ix);
   }
   {
+    dfl inv_y, ext_y;
+    axis_ext(A, 1, o_j, sb, fy, inv_y, ext_y);
     const dfl f_iy = dfl_mul(dfl_sub(b, fy ? dfl_mul(f_e, ext_y) : zero), inv_y);
     atomicAdd(f + base + NX * sb, dfl_to_double_normal(dfl_mul(w8, f_iy)));
     sum = dfl_add(sum, f_iy);
   }
   {
+    dfl inv_z, ext_z;
+    axis_ext(A, 2, o_k, sc, fz, inv_z, ext_z);
     const dfl f_iz = dfl_mul(dfl_sub(c, fz ? dfl_mul(f_e, ext_z) : zero), inv_z);
     atomicAdd(f + base + NXY * sc, dfl_to_double_normal(dfl_mul(w8, f_iz)));
     sum = dfl_add(sum, f_iz);
@@ -1150,12 +1167,14 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
         uy = dfl_mul(hs, sphi);
         uz = dfl_mul(hg, ct);
       }
+      // the second velocity is formed before the first scatter, so that only it (not the
+      // centre of mass and the relative half-velocity) stays live across that scatter
+      const dfl pB0 = dfl_sub(vc0, ux), pB1 = dfl_sub(vc1, uy), pB2 = dfl_sub(vc2, uz);
       int rb = remap_scatter_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
                                  xmin, ymin, zmin, xfac, yfac, zfac, f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_scatter_dfl(g, A, dfl_sub(vc0, ux), dfl_sub(vc1, uy), dfl_sub(vc2, uz), xmin,
-                             ymin, zmin, xfac, yfac, zfac, f, kr, nat);
+      rb = remap_scatter_dfl(g, A, pB0, pB1, pB2, xmin, ymin, zmin, xfac, yfac, zfac, f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }

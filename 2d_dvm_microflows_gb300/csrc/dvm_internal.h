@@ -131,6 +131,10 @@ struct CollideArgs {
   PairDev pairs;
   uint32_t* err;
   unsigned long long* scatter_count;  // if set, the adds into f (df) are counted here
+  // FP32 copies of grid constants, filled by launch_collide / launch_collide_f32 so that
+  // the kernels read them as parameters rather than hold them in registers
+  float vmin[3], vfac[3];  // axis minima and nearest-node factors
+  float rnx, rnxy;         // 1 / NX and 1 / (NX NY)
 };
 
 // 2-D wall ghost slabs: one per (wall side, position along the wall).

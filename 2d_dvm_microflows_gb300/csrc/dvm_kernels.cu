@@ -991,10 +991,6 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   A.tab[0] = st; A.tab[1] = st + a.t.nmax; A.tab[2] = st + 2 * a.t.nmax;
   A.n[0] = g.nx; A.n[1] = g.ny; A.n[2] = g.nz;
   const double2* gtab = a.t.gtab_smem ? sg : a.t.gtab;
-  const float xmin = static_cast<float>(g.xv_min), ymin = static_cast<float>(g.yv_min);
-  const float zmin = static_cast<float>(g.zv_min);
-  const float xfac = static_cast<float>(g.xv_factor), yfac = static_cast<float>(g.yv_factor);
-  const float zfac = static_cast<float>(g.zv_factor);
   dfl two_pi;
   {
     const dfl t = dfl_from_double(a.t.two_pi);
@@ -1003,7 +999,6 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   const dfl one_sixth = dfl_make(0x1.555556p-3f, -0x1.555556p-28f);  // 1/6 to 2^-50
 
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
-  const float rNX = 1.f / static_cast<float>(NX), rNXY = 1.f / static_cast<float>(NXY);
   const int nent = 3 * a.ncells;
   const long long total = a.chunk_off[nent];
   const bool vr = (a.cp.method == DVM_COLL_VR);
@@ -1057,8 +1052,8 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
                                   nv, rB, bad);
     }
     int iA, jA, kA, iB, jB, kB;
-    node_ijk(lA, NX, NXY, rNX, rNXY, iA, jA, kA);
-    node_ijk(lB, NX, NXY, rNX, rNXY, iB, jB, kB);
+    node_ijk(lA, NX, NXY, a.rnx, a.rnxy, iA, jA, kA);
+    node_ijk(lB, NX, NXY, a.rnx, a.rnxy, iB, jB, kB);
     // compute_relative_velocity (collision_utilities.f90:188-218) and g^(2-2 omega)
     double gg, g_sigma;
     if (gtab) {
@@ -1171,10 +1166,12 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
       // centre of mass and the relative half-velocity) stays live across that scatter
       const dfl pB0 = dfl_sub(vc0, ux), pB1 = dfl_sub(vc1, uy), pB2 = dfl_sub(vc2, uz);
       int rb = remap_scatter_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
-                                 xmin, ymin, zmin, xfac, yfac, zfac, f, kr, nat);
+                                 a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0], a.vfac[1],
+                                 a.vfac[2], f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_scatter_dfl(g, A, pB0, pB1, pB2, xmin, ymin, zmin, xfac, yfac, zfac, f, kr, nat);
+      rb = remap_scatter_dfl(g, A, pB0, pB1, pB2, a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0],
+                             a.vfac[1], a.vfac[2], f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
@@ -1199,6 +1196,20 @@ int collide_blocks_per_sm(size_t smem) {
   return n > 0 ? n : 1;
 }
 
+// The FP32 grid constants of the collide kernels, formed on the host.
+static CollideArgs with_collide_consts(const CollideArgs& a) {
+  CollideArgs b = a;
+  b.vmin[0] = static_cast<float>(a.g.xv_min);
+  b.vmin[1] = static_cast<float>(a.g.yv_min);
+  b.vmin[2] = static_cast<float>(a.g.zv_min);
+  b.vfac[0] = static_cast<float>(a.g.xv_factor);
+  b.vfac[1] = static_cast<float>(a.g.yv_factor);
+  b.vfac[2] = static_cast<float>(a.g.zv_factor);
+  b.rnx = 1.f / static_cast<float>(a.g.nx);
+  b.rnxy = 1.f / static_cast<float>(a.g.nx * a.g.ny);
+  return b;
+}
+
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s) {
   const size_t smem = collide_smem_bytes(a.g, a.t);
   if (smem > 48 * 1024) {
@@ -1206,7 +1217,7 @@ cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s) {
         k_collide, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
-  k_collide<<<grid, kCollideChunk, smem, s>>>(a);
+  k_collide<<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a));
   return cudaGetLastError();
 }
 
@@ -1269,12 +1280,13 @@ __device__ __forceinline__ int nearest_f(const SmemAxesF& A, int ax, float u, fl
 }
 
 // compute_remapping_quantities (collisions/remapping.f90:92-394) in FP32.
-__device__ __forceinline__ int remap_f32(const GridInfo& g, const SmemAxesF& A, float u, float v,
-                                         float w, StencilF& s) {
+__device__ __forceinline__ int remap_f32(const GridInfo& g, const float (&vmin)[3],
+                                         const float (&vfac)[3], const SmemAxesF& A, float u,
+                                         float v, float w, StencilF& s) {
   int corner = 0, bad = 0;
-  int o_i = nearest_f(A, 0, u, static_cast<float>(g.xv_min), static_cast<float>(g.xv_factor), corner, bad);
-  int o_j = nearest_f(A, 1, v, static_cast<float>(g.yv_min), static_cast<float>(g.yv_factor), corner, bad);
-  int o_k = nearest_f(A, 2, w, static_cast<float>(g.zv_min), static_cast<float>(g.zv_factor), corner, bad);
+  int o_i = nearest_f(A, 0, u, vmin[0], vfac[0], corner, bad);
+  int o_j = nearest_f(A, 1, v, vmin[1], vfac[1], corner, bad);
+  int o_k = nearest_f(A, 2, w, vmin[2], vfac[2], corner, bad);
   const int i_max = g.nx - 1, j_max = g.ny - 1, k_max = g.nz - 1;
   if (corner == 3) {
     o_i -= isign1(o_i - 1);
@@ -1429,7 +1441,6 @@ struct F32Ctx {
   const float2* gtab;
   const float2* strig;
   float vhs, ralpha;
-  float rNX, rNXY;  // reciprocals of NX and NX NY
   bool vss, vr;
   int NR;
   uint32_t step;
@@ -1474,8 +1485,6 @@ __device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const Co
   c.vr = (a.cp.method == DVM_COLL_VR);
   c.NR = a.cp.num_repl;
   c.step = a.step_dev ? *a.step_dev : a.step;
-  c.rNX = 1.f / static_cast<float>(g.nx);
-  c.rNXY = 1.f / static_cast<float>(g.nx * g.ny);
   return c;
 }
 
@@ -1507,8 +1516,8 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
                                  nv, rB, bad);
   }
   int iA, jA, kA, iB, jB, kB;
-  node_ijk(lA, NX, NXY, c.rNX, c.rNXY, iA, jA, kA);
-  node_ijk(lB, NX, NXY, c.rNX, c.rNXY, iB, jB, kB);
+  node_ijk(lA, NX, NXY, a.rnx, a.rnxy, iA, jA, kA);
+  node_ijk(lB, NX, NXY, a.rnx, a.rnxy, iB, jB, kB);
   const float xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
   const float xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
   float gg, g_sigma;
@@ -1588,10 +1597,10 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
     // the cell's slab of df is 16-byte aligned when the node count is a multiple of 4
     const bool vec = (g.nv & 3) == 0;
     StencilF sA_, sB_;
-    int rb = remap_f32(g, A, vc0 + ux, vc1 + uy, vc2 + uz, sA_);
+    int rb = remap_f32(g, a.vmin, a.vfac, A, vc0 + ux, vc1 + uy, vc2 + uz, sA_);
     if (rb & 2) bad |= DVM_EW_REMAP;
     else nat += scatter_stencil_f32(df, sA_, kr, vec);
-    rb = remap_f32(g, A, vc0 - ux, vc1 - uy, vc2 - uz, sB_);
+    rb = remap_f32(g, a.vmin, a.vfac, A, vc0 - ux, vc1 - uy, vc2 - uz, sB_);
     if (rb & 2) bad |= DVM_EW_REMAP;
     else nat += scatter_stencil_f32(df, sB_, kr, vec);
   }
@@ -1651,7 +1660,7 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
         k_collide_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
-  k_collide_f32<<<grid, kCollideChunk, smem, s>>>(a, tf, df);
+  k_collide_f32<<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a), tf, df);
   return cudaGetLastError();
 }
 

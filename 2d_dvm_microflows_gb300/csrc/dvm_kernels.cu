@@ -617,8 +617,10 @@ __device__ __forceinline__ unsigned long long u53_bits(double R) {
 // is unique (the last index whose cumulative value is below the target), so any exact
 // search returns the reference's bisection answer. Here the bucket is narrowed four ways
 // per step (three independent loads), which takes about half the dependent load rounds
-// of bisection on the wide tail buckets that set a warp's pace; the reference's test
-// cum(idx) < target <= cum(idx+1) then confirms the result.
+// of bisection on the wide tail buckets that set a warp's pace. The reference's test
+// cum(idx) < target <= cum(idx+1) is made on the bucket's ends instead, loaded beside the
+// first round: every step keeps cum(lo) < target <= cum(hi) and the sums never decrease,
+// so the test on the ends holds exactly when it holds on the result.
 __device__ __forceinline__ int referenced_search_fixed(const long long* __restrict__ cum,
                                                        const int2* __restrict__ ref, int n,
                                                        double R, uint32_t& bad) {
@@ -633,7 +635,8 @@ __device__ __forceinline__ int referenced_search_fixed(const long long* __restri
   const long long adj = static_cast<long long>((__umul64hi(m, T) << 11) | ((m * T) >> 53));
   // cum(lo) < adj <= cum(hi) holds for a valid bucket; each step keeps it
   int lo = left, hi = right;
-  if (lo >= 0 && hi <= n) {
+  if (lo >= 0 && hi <= n && lo < hi) {
+    const long long c_lo = __ldg(cum + lo), c_hi = __ldg(cum + hi);
     for (int it = 0; hi - lo > 1 && it < kMaxSearchIters; ++it) {
       const int span = hi - lo;
       int nlo = lo, nhi = hi;
@@ -645,7 +648,7 @@ __device__ __forceinline__ int referenced_search_fixed(const long long* __restri
       lo = nlo;
       hi = nhi;
     }
-    if (lo >= 0 && lo < n && adj > __ldg(cum + lo) && adj <= __ldg(cum + lo + 1)) return lo;
+    if (hi - lo == 1 && lo < n && adj > c_lo && adj <= c_hi) return lo;
   }
   bad |= DVM_EW_SEARCH;
   int blo = 0, bhi = n;

@@ -839,16 +839,17 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   const int NX = g.nx, NXY = g.nx * g.ny;
   const int base = o_i + NX * o_j + NXY * o_k;
   dfl sum = zero;
+  const double c_e = dfl_to_double_normal(dfl_mul(w8, f_e));  // the exterior nodes' share
   if (fx) {
-    atomicAdd(f + base - sa, dfl_to_double_normal(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - sa, c_e);
     sum = f_e;
   }
   if (fy) {
-    atomicAdd(f + base - NX * sb, dfl_to_double_normal(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - NX * sb, c_e);
     sum = dfl_add(sum, f_e);
   }
   if (fz) {
-    atomicAdd(f + base - NXY * sc, dfl_to_double_normal(dfl_mul(w8, f_e)));
+    atomicAdd(f + base - NXY * sc, c_e);
     sum = dfl_add(sum, f_e);
   }
   {

@@ -176,6 +176,17 @@ __device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
   return dfl_norm(p, e);
 }
 
+// a * b as a double for pairs of normal floats: the product's hi and its error term go to
+// FP64 unnormalised, since the FP64 add rounds their exact sum, which renormalising (an
+// error-free transformation) would not change.
+__device__ __forceinline__ double dfl_mul_to_double(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return dbl_from_normal_float(p) + dbl_from_normal_float(e);
+}
+
 // A running sum, renormalised after every term so that lo stays within half an ulp of hi
 // and each term adds at most about 2^-48 of the sum in rounding.
 struct dacc {

@@ -839,7 +839,7 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   const int NX = g.nx, NXY = g.nx * g.ny;
   const int base = o_i + NX * o_j + NXY * o_k;
   dfl sum = zero;
-  const double c_e = dfl_to_double_normal(dfl_mul(w8, f_e));  // the exterior nodes' share
+  const double c_e = dfl_mul_to_double(w8, f_e);  // the exterior nodes' share
   if (fx) {
     atomicAdd(f + base - sa, c_e);
     sum = f_e;
@@ -856,25 +856,25 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
     dfl inv_x, ext_x;
     axis_ext(A, 0, o_i, sa, fx, inv_x, ext_x);
     const dfl f_ix = dfl_mul(dfl_sub(a, fx ? dfl_mul(f_e, ext_x) : zero), inv_x);
-    atomicAdd(f + base + sa, dfl_to_double_normal(dfl_mul(w8, f_ix)));
+    atomicAdd(f + base + sa, dfl_mul_to_double(w8, f_ix));
     sum = dfl_add(sum, f_ix);
   }
   {
     dfl inv_y, ext_y;
     axis_ext(A, 1, o_j, sb, fy, inv_y, ext_y);
     const dfl f_iy = dfl_mul(dfl_sub(b, fy ? dfl_mul(f_e, ext_y) : zero), inv_y);
-    atomicAdd(f + base + NX * sb, dfl_to_double_normal(dfl_mul(w8, f_iy)));
+    atomicAdd(f + base + NX * sb, dfl_mul_to_double(w8, f_iy));
     sum = dfl_add(sum, f_iy);
   }
   {
     dfl inv_z, ext_z;
     axis_ext(A, 2, o_k, sc, fz, inv_z, ext_z);
     const dfl f_iz = dfl_mul(dfl_sub(c, fz ? dfl_mul(f_e, ext_z) : zero), inv_z);
-    atomicAdd(f + base + NXY * sc, dfl_to_double_normal(dfl_mul(w8, f_iz)));
+    atomicAdd(f + base + NXY * sc, dfl_mul_to_double(w8, f_iz));
     sum = dfl_add(sum, f_iz);
   }
   const dfl f_o = dfl_sub(dfl_make(1.f, 0.f), sum);
-  atomicAdd(f + base, dfl_to_double_normal(dfl_mul(w8, f_o)));
+  atomicAdd(f + base, dfl_mul_to_double(w8, f_o));
   return bad;
 }
 

@@ -838,20 +838,16 @@ __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAx
   // node takes 1 - the others, as in the reference)
   const int NX = g.nx, NXY = g.nx * g.ny;
   const int base = o_i + NX * o_j + NXY * o_k;
-  dfl sum = zero;
   const double c_e = dfl_mul_to_double(w8, f_e);  // the exterior nodes' share
-  if (fx) {
-    atomicAdd(f + base - sa, c_e);
-    sum = f_e;
-  }
-  if (fy) {
-    atomicAdd(f + base - NX * sb, c_e);
-    sum = dfl_add(sum, f_e);
-  }
-  if (fz) {
-    atomicAdd(f + base - NXY * sc, c_e);
-    sum = dfl_add(sum, f_e);
-  }
+  if (fx) atomicAdd(f + base - sa, c_e);
+  if (fy) atomicAdd(f + base - NX * sb, c_e);
+  if (fz) atomicAdd(f + base - NXY * sc, c_e);
+  // the weights' running sum starts from (number of exterior nodes) x f_e, the doubling
+  // exact
+  const int ne = fx + fy + fz;
+  dfl sum = f_e;
+  if (ne >= 2) sum = dfl_scale(f_e, 2.f);
+  if (ne == 3) sum = dfl_add(sum, f_e);
   {
     dfl inv_x, ext_x;
     axis_ext(A, 0, o_i, sa, fx, inv_x, ext_x);

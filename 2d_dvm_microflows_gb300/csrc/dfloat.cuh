@@ -176,15 +176,17 @@ __device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
   return dfl_norm(p, e);
 }
 
-// a * b as a double for pairs of normal floats: the product's hi and its error term go to
-// FP64 unnormalised, since the FP64 add rounds their exact sum, which renormalising (an
-// error-free transformation) would not change.
+// a * b as a double: the product's hi and its error term go to FP64 unnormalised, since the
+// FP64 add rounds their exact sum, which renormalising (an error-free transformation) would
+// not change. The two float-to-double conversions are the hardware's (exact, on the FP64
+// pipe, which the collide kernel leaves three-quarters idle) rather than the integer ones,
+// saving issue slots there.
 __device__ __forceinline__ double dfl_mul_to_double(dfl a, dfl b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return dbl_from_normal_float(p) + dbl_from_normal_float(e);
+  return static_cast<double>(p) + static_cast<double>(e);
 }
 
 // A running sum, renormalised after every term so that lo stays within half an ulp of hi

@@ -55,14 +55,37 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-// m 2^-53 from the top 53 bits of (hi, lo), built from the bits (exact; no FP64 op).
-__device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
-  const uint64_t m = ((static_cast<uint64_t>(hi) << 32) | lo) >> 11;
+// m 2^-53 for a 53-bit integer m, built from the bits (exact; no FP64 op).
+__device__ __forceinline__ double u53m(uint64_t m) {
   if (m == 0) return 0.0;
   const int p = 63 - __clzll(static_cast<long long>(m));  // top bit, 0..52
   const uint64_t mant = (m << (52 - p)) & ((1ull << 52) - 1);
   return __longlong_as_double(static_cast<long long>((static_cast<uint64_t>(p + 970) << 52) | mant));
 }
+
+// m 2^-53 from the top 53 bits of (hi, lo).
+__device__ __forceinline__ double u53(uint32_t lo, uint32_t hi) {
+  return u53m(((static_cast<uint64_t>(hi) << 32) | lo) >> 11);
+}
+
+// The two 53-bit integers m behind philox_uniform2's uniforms (u = m 2^-53), for callers
+// that work on the integers directly.
+__device__ __forceinline__ void philox_u53x2(uint64_t seed, uint32_t sample, uint32_t cell,
+                                             uint32_t step, uint32_t sub, uint32_t call,
+                                             unsigned long long& m0, unsigned long long& m1) {
+  uint32_t o[4];
+  philox4x32_10(sample, cell, step, (sub & 3u) | (call << 2), static_cast<uint32_t>(seed),
+                static_cast<uint32_t>(seed >> 32), o);
+  m0 = ((static_cast<uint64_t>(o[1]) << 32) | o[0]) >> 11;
+  m1 = ((static_cast<uint64_t>(o[3]) << 32) | o[2]) >> 11;
+}
+
+// u < kDoubleTol for u = m 2^-53 exactly when m < kTolU53 = ceil(kDoubleTol 2^53).
+constexpr double kTolScaled = kDoubleTol * 9007199254740992.0;
+constexpr unsigned long long kTolU53 =
+    static_cast<double>(static_cast<unsigned long long>(kTolScaled)) < kTolScaled
+        ? static_cast<unsigned long long>(kTolScaled) + 1
+        : static_cast<unsigned long long>(kTolScaled);
 
 __device__ __forceinline__ void philox_uniform2(uint64_t seed, uint32_t sample, uint32_t cell,
                                                 uint32_t step, uint32_t sub, uint32_t call,

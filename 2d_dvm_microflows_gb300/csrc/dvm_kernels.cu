@@ -621,11 +621,13 @@ __device__ __forceinline__ unsigned long long u53_bits(double R) {
 // cum(idx) < target <= cum(idx+1) is made on the bucket's ends instead, loaded beside the
 // first round: every step keeps cum(lo) < target <= cum(hi) and the sums never decrease,
 // so the test on the ends holds exactly when it holds on the result.
+// R enters as m = R 2^53 truncated and the test R < tol, made by the caller (on m for the
+// Philox uniforms, on the double for recorded ones).
 __device__ __forceinline__ int referenced_search_fixed(const long long* __restrict__ cum,
                                                        const int2* __restrict__ ref, int n,
-                                                       double R, uint32_t& bad) {
-  if (__double_as_longlong(R) < __double_as_longlong(kDoubleTol)) return 0;  // R < tol
-  const unsigned long long m = u53_bits(R);
+                                                       unsigned long long m, bool below_tol,
+                                                       uint32_t& bad) {
+  if (below_tol) return 0;  // R < tol
   int i = static_cast<int>((1000ull * m + ((1ull << 53) - 1)) >> 53);
   i = i < 1 ? 1 : (i > kNRef ? kNRef : i);
   const int2 lr = __ldg(ref + i - 1);
@@ -883,13 +885,8 @@ __device__ __forceinline__ void add_scatter_count(unsigned long long* total, uin
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(total, v);
 }
 
-// t = R - k/kTrigN (k = the top 10 bits of R) as a pair, and k, from the bits of R in [0, 1).
-__device__ __forceinline__ dfl angle_fraction(double R, int& k) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(R));
-  const int e = static_cast<int>((b >> 52) & 0x7ff);
-  unsigned long long m = 0;  // R 2^53, truncated
-  if (e > 0 && e <= 1022 && 1022 - e < 64)
-    m = ((b & ((1ull << 52) - 1)) | (1ull << 52)) >> (1022 - e);
+// t = R - k/kTrigN (k = the top 10 bits of R) as a pair, and k, from m = R 2^53 truncated.
+__device__ __forceinline__ dfl angle_fraction(unsigned long long m, int& k) {
   k = static_cast<int>(m >> 43);
   const unsigned long long t = m & ((1ull << 43) - 1);
   const uint32_t th = static_cast<uint32_t>(t >> 20), tl = static_cast<uint32_t>(t & 0xfffffu);
@@ -1034,22 +1031,28 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
     double* f = a.f + static_cast<size_t>(cell) * nv;
 
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
-    double rA = 0.0, rB = 0.0;
+    unsigned long long mA = 0, mB = 0;
     const bool rec = a.pairs.active;
-    if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, rA, rB);
+    if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
       lA = a.pairs.glA[q][i];
       lB = a.pairs.glB[q][i];
     } else {
-      if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
+      bool tA = mA < kTolU53, tB = mB < kTolU53;
+      if (rec) {
+        const double rA = a.pairs.rA[q][i], rB = a.pairs.rB[q][i];
+        mA = u53_bits(rA); mB = u53_bits(rB);
+        tA = __double_as_longlong(rA) < __double_as_longlong(kDoubleTol);
+        tB = __double_as_longlong(rB) < __double_as_longlong(kDoubleTol);
+      }
       const bool aeq = vr && q == 0, beq = vr && q == 1;
       lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
                                   (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                  nv, rA, bad);
+                                  nv, mA, tA, bad);
       lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
                                   (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                  nv, rB, bad);
+                                  nv, mB, tB, bad);
     }
     int iA, jA, kA, iB, jB, kB;
     node_ijk(lA, NX, NXY, a.rnx, a.rnxy, iA, jA, kA);
@@ -1099,16 +1102,20 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
       hg = dfl_scale(dfl_norm(t.hi, t.lo), 0.5f);
     }
     for (int r = 0; r < NR; ++r) {
-      double rphi, rcos;
+      // the uniforms as 53-bit integers (Philox) or recorded doubles
+      unsigned long long mphi = 0, mcos = 0;
+      double rphi_rec = 0.0, rcos_rec = 0.0;
       if (rec) {
-        rphi = a.pairs.rphi[q][i * NR + r];
-        rcos = a.pairs.rcos[q][i * NR + r];
+        rphi_rec = a.pairs.rphi[q][i * NR + r];
+        rcos_rec = a.pairs.rcos[q][i * NR + r];
+        mphi = u53_bits(rphi_rec);
       } else {
-        philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 1u + r, rphi, rcos);
+        philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
       }
       dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
       if (vss) {
         // VSS branch (pick_random_velocity_on_sphere :314-328) in FP64
+        const double rphi = rec ? rphi_rec : u53m(mphi), rcos = rec ? rcos_rec : u53m(mcos);
         const double xA = A.vd[0][iA], yA = A.vd[1][jA], zA = A.vd[2][kA];
         const double xB = A.vd[0][iB], yB = A.vd[1][jB], zB = A.vd[2][kB];
         const double v0 = 0.5 * xA + 0.5 * xB, v1 = 0.5 * yA + 0.5 * yB, v2 = 0.5 * zA + 0.5 * zB;
@@ -1137,7 +1144,7 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
         // sin of 2 pi k/kTrigN from the table, of th = 2 pi t (< 0.0062) by Taylor series
         // (the dropped terms are below 1e-17), then the angle-addition formulas
         int k;
-        const dfl th = dfl_mul(two_pi, angle_fraction(rphi, k));
+        const dfl th = dfl_mul(two_pi, angle_fraction(mphi, k));
         const dfl t2 = dfl_mul(th, th);
         const float t2h = t2.hi;
         // sin th = th - th (t2/6 - t2^2/120), cos th = 1 - (t2/2 - t2^2/24 + t2^3/720)
@@ -1153,7 +1160,11 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
         // cos theta = 2 R - 1 (exact in FP64), sin theta = sqrt(1 - cos^2)
         dfl ct;
         {
-          const dfl t = dfl_from_double(fma(2.0, rcos, -1.0));
+          // 2 R - 1, exact: from the recorded double, or as (2 m - 2^53) 2^-53
+          const double x = rec ? fma(2.0, rcos_rec, -1.0)
+                               : static_cast<double>(static_cast<long long>(2 * mcos) -
+                                                     (1ll << 53)) * 0x1.0p-53;
+          const dfl t = dfl_from_double(x);
           ct = dfl_norm(t.hi, t.lo);
         }
         const dfl stt = dfl_sqrt(dfl_sub(dfl_make(1.f, 0.f), dfl_mul(ct, ct)));
@@ -1498,22 +1509,28 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
   const bool vr = c.vr;
-  double rA = 0.0, rB = 0.0;
+  unsigned long long mA = 0, mB = 0;
   const bool rec = a.pairs.active;
-  if (!rec) philox_uniform2(a.cp.seed, static_cast<uint32_t>(i), cell, c.step, q, 0u, rA, rB);
+  if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, c.step, q, 0u, mA, mB);
   int lA, lB;
   if (rec && a.pairs.glA[q]) {
     lA = a.pairs.glA[q][i];
     lB = a.pairs.glB[q][i];
   } else {
-    if (rec) { rA = a.pairs.rA[q][i]; rB = a.pairs.rB[q][i]; }
+    bool tA = mA < kTolU53, tB = mB < kTolU53;
+    if (rec) {
+      const double rA = a.pairs.rA[q][i], rB = a.pairs.rB[q][i];
+      mA = u53_bits(rA); mB = u53_bits(rB);
+      tA = __double_as_longlong(rA) < __double_as_longlong(kDoubleTol);
+      tB = __double_as_longlong(rB) < __double_as_longlong(kDoubleTol);
+    }
     const bool aeq = vr && q == 0, beq = vr && q == 1;
     lA = referenced_search_fixed((aeq ? a.cum_eq : a.cum_dev) + cs,
                                  (aeq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                 nv, rA, bad);
+                                 nv, mA, tA, bad);
     lB = referenced_search_fixed((beq ? a.cum_eq : a.cum_dev) + cs,
                                  (beq ? a.ref_eq : a.ref_dev) + static_cast<size_t>(cell) * kNRef,
-                                 nv, rB, bad);
+                                 nv, mB, tB, bad);
   }
   int iA, jA, kA, iB, jB, kB;
   node_ijk(lA, NX, NXY, a.rnx, a.rnxy, iA, jA, kA);

@@ -178,15 +178,16 @@ __device__ __forceinline__ dfl dfl_mul(dfl a, dfl b) {
 
 // a * b as a double: the product's hi and its error term go to FP64 unnormalised, since the
 // FP64 add rounds their exact sum, which renormalising (an error-free transformation) would
-// not change. The two float-to-double conversions are the hardware's (exact, on the FP64
-// pipe, which the collide kernel leaves three-quarters idle) rather than the integer ones,
-// saving issue slots there.
+// not change. The hi goes through the hardware's float-to-double conversion (exact, on the
+// FP64 pipe) and the error term through the integer one: the collide kernel, which alone
+// uses this, balances its issue slots and its FP64 pipe best that way (measured against
+// both conversions of either kind).
 __device__ __forceinline__ double dfl_mul_to_double(dfl a, dfl b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return static_cast<double>(p) + static_cast<double>(e);
+  return static_cast<double>(p) + dbl_from_normal_float(e);
 }
 
 // A running sum, renormalised after every term so that lo stays within half an ulp of hi

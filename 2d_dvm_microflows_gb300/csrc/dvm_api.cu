@@ -311,9 +311,7 @@ int build_collision_tables(dvm_ctx* c) {
     h2d(c, c->d_gtab, gt.data(), gt.size() * sizeof(double2));
     c->tabs.gtab = c->d_gtab;
     c->tabs.gtab_n = ns;
-    // staged in shared memory only while the collide CTA stays small enough for three
-    // CTAs per SM; larger tables are read through L1
-    c->tabs.gtab_smem = (static_cast<size_t>(ns) * sizeof(double2) <= 32 * 1024) ? 1 : 0;
+    c->tabs.gtab_smem = gtab_staged(ns);
   }
   if (c->p.precision == DVM_PREC_FP32) {
     // FP32 copies of the same tables for k_collide_f32

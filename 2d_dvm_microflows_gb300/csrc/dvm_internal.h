@@ -88,6 +88,15 @@ struct CollTables {
   double two_pi;           // 2*pi_used
 };
 
+// The FP64 (g, g^(2-2 omega)) table is staged in shared memory only up to this size, which
+// keeps the collide CTA small enough for several CTAs per SM; larger tables are read
+// through L1. Every launch set-up decides by this one rule.
+constexpr size_t kGtabSmemMaxBytes = 32 * 1024;
+inline int gtab_staged(int gtab_n) {
+  return (gtab_n > 0 && static_cast<size_t>(gtab_n) * sizeof(double2) <= kGtabSmemMaxBytes) ? 1
+                                                                                            : 0;
+}
+
 constexpr int kTrigN = 1024;
 
 // FP32 copies of the collision tables for the precision form.

@@ -12,9 +12,18 @@
 // Host code cannot use that array's name as a device address (it is a host-side
 // stand-in), so the first call on each device looks the address up with
 // cudaGetSymbolAddress, with that device current, and caches it; that first call should
-// therefore come before any stream capture. All calls share the array and it keeps the
-// last call's contents: everything that must start from zero is cleared on every call,
-// and calls that overlap on the GPU (other streams, other host threads) race on it.
+// therefore come before any stream capture. The cached address belongs to the device's
+// context as it was at that first call: do not use this entry point across a
+// cudaDeviceReset (or anything else that tears the primary context down), after which the
+// address would be stale. All calls share the array and it keeps the last call's
+// contents: everything that must start from zero is cleared on every call, except the
+// error word, which accumulates until a call that waits for its result reads and clears
+// it. Calls that overlap on the GPU (other streams, other host threads) race on the array.
+//
+// Size: 20*(Nv+1) + 16112 bytes per cell (two 64-bit cumulative sums and one FP32 sign
+// array per node, two 1000-entry bucket tables, the equilibrium cache, plan and chunk
+// offsets) plus the grid tables (under 0.2 MB), in 32 MiB: 341 cells of 16^3, 114 of
+// 24^3, 49 of 32^3, 25 of 40^3.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -38,10 +47,11 @@ int g_collide_grid[kMaxDevices] = {0};
 
 size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 
-// Offsets of every buffer inside the scratch array.
+// Offsets of every buffer inside the scratch array. The error word comes first, at a fixed
+// offset, so that calls of any size find the bits earlier calls left there.
 struct Layout {
-  size_t axes, tabs, gtab, trig, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
-      chunk_off, total, err, end;
+  size_t err, axes, tabs, gtab, trig, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
+      chunk_off, total, end;
 };
 
 Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
@@ -50,6 +60,7 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   const int nmax = nx > ny ? (nx > nz ? nx : nz) : (ny > nz ? ny : nz);
   Layout L;
   size_t o = 0;
+  L.err = o; o = align256(o + sizeof(uint32_t));
   L.axes = o; o = align256(o + 2 * sizeof(double) * (nx + ny + nz));
   L.tabs = o; o = align256(o + 3 * sizeof(AxisEntry) * nmax);
   L.gtab = o; o = align256(o + sizeof(double2) * gtab_n);
@@ -63,7 +74,6 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   L.plan = o; o = align256(o + sizeof(CellPlan) * C);
   L.chunk_off = o; o = align256(o + sizeof(long long) * (3 * C + 1));
   L.total = o; o = align256(o + sizeof(long long));
-  L.err = o; o = align256(o + sizeof(uint32_t));
   L.end = o;
   return L;
 }
@@ -241,12 +251,14 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
                                                      d_trig, 2.0 * pi);
     if ((e = cudaGetLastError()) != cudaSuccess) return status_of(e);
   }
-  // state that must start from zero: the equilibrium cache (so every call builds the
-  // Maxwellian afresh, as a new context's first call does) and the error word
+  // state that must start from zero: the equilibrium cache, so every call builds the
+  // Maxwellian afresh, as a new context's first call does. The error word is not cleared
+  // here: it collects the bits of every call since the last call that read it (one with
+  // `collisions` set), so an error of a call that did not wait is reported by the next
+  // call that does.
   uint32_t* d_err = reinterpret_cast<uint32_t*>(base + L.err);
   double* d_eq_cache = reinterpret_cast<double*>(base + L.eq_cache);
-  if ((e = cudaMemsetAsync(d_eq_cache, 0, sizeof(double) * kEqCache * ncells, s)) != cudaSuccess ||
-      (e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s)) != cudaSuccess)
+  if ((e = cudaMemsetAsync(d_eq_cache, 0, sizeof(double) * kEqCache * ncells, s)) != cudaSuccess)
     return status_of(e);
 
   CollParams cp;
@@ -284,7 +296,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   a.t.axis = d_tab; a.t.nmax = nmax;
   a.t.gtab = cubic ? d_gtab : nullptr;
   a.t.gtab_n = gtab_n;
-  a.t.gtab_smem = (cubic && static_cast<size_t>(gtab_n) * sizeof(double2) <= 48 * 1024) ? 1 : 0;
+  a.t.gtab_smem = cubic ? gtab_staged(gtab_n) : 0;
   a.t.phi_scale = 2.0 * pi / kPiExact;
   a.t.trig = d_trig;
   a.t.two_pi = 2.0 * pi;
@@ -302,6 +314,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
             cudaSuccess ||
         (e = cudaMemcpyAsync(&word, d_err, sizeof(word), cudaMemcpyDeviceToHost, s)) !=
             cudaSuccess ||
+        (e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
       return status_of(e);
     *collisions = total;

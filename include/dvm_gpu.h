@@ -321,15 +321,19 @@ int dvm_wait_selftest(dvm_ctx* ctx);
  * memory, f[ncells][Nv] (updated in place) and props[ncells][DVM_NPROP] (the cell
  * properties, e.g. from dvm_get_properties); every intermediate lives in one fixed 32 MiB
  * device array that the library holds on each GPU that loads it, until exit.
- *   Limit: the grid tables plus 4*(Nv+1)*8 + 16064 bytes per cell must fit in 32 MiB
- *   (about 70 cells of 24^3 or 30 cells of 32^3); larger problems get DVM_ERR_TOO_LARGE.
+ *   Limit: the grid tables (under 0.2 MB) plus 20*(Nv+1) + 16112 bytes per cell must fit
+ *   in 32 MiB: at most 341 cells of 16^3, 114 of 24^3, 49 of 32^3 or 25 of 40^3; larger
+ *   problems get DVM_ERR_TOO_LARGE before anything is launched.
  *   The first call on a device looks up that array's address (cudaGetSymbolAddress) with
- *   the device current; make that first call before any stream capture.
+ *   the device current and keeps it; make that first call before any stream capture, and
+ *   do not use this entry point across a cudaDeviceReset of that device.
  *   Every call shares the array and rebuilds what it needs (the equilibrium is recomputed,
  *   as on a new context's first call); calls that overlap on the GPU race on it.
  *   Work is queued on `stream` (a cudaStream_t; NULL = default stream). If `collisions` is
- *   not NULL the call synchronises that stream, stores the samples drawn and returns
- *   DVM_ERR_NUMERIC if the device error word was set. */
+ *   not NULL the call synchronises that stream, stores the samples drawn, and returns
+ *   DVM_ERR_NUMERIC if the device error word is set; the word collects the bits of every
+ *   call since the last call that read it, so a fault in a call made with `collisions`
+ *   NULL is reported by the next call that passes it. */
 int dvm_collide_noalloc(const dvm_params* params, const dvm_vgrid* grid, double* f,
                         const double* props, int ncells, uint64_t step, void* stream,
                         int64_t* collisions);

@@ -406,6 +406,13 @@ typedef struct {
   /* VR per-cell equilibrium cache (cdf_eq(nx,ny,...), variance_reduction.f90:37) */
   double *eq_pre;   /* [C][nv+1] */
   double *cache;    /* [C][4] dens, u, v, temp */
+  /* Test aid, off by default: when set, the equilibrium node values that the deviation
+   * and the equilibrium CDF use are the Maxwellian values themselves rather than the
+   * differences of the running sum eq_df (variance_reduction.f90:400, phi_eq =
+   * eq_df(l) - eq_df(l-1)). That is how the GPU kernels form them; comparing the two
+   * modes isolates what the running sum's rounding alone does to the partner choice. */
+  int eq_nodes_direct;
+  double *eq_node;  /* [C][nv+1], only in that mode */
   int64_t colls_last;
   int64_t scatter_last;  /* adds into f by the last collision call (depletion + stencils) */
   uint32_t err;
@@ -450,7 +457,21 @@ void orc_destroy(orc_ctx* c) {
   if (!c) return;
   grid_free(&c->g);
   free(c->f); free(c->fconv); free(c->props); free(c->eq_pre); free(c->cache);
+  free(c->eq_node);
   free(c);
+}
+
+/* Equilibrium node values: 0 = the reference's differences of the running sum (default),
+ * 1 = the Maxwellian values directly (see orc_ctx.eq_nodes_direct). Clears the cache. */
+int orc_set_eq_node_mode(orc_ctx* c, int mode) {
+  if (mode != 0 && mode != 1) return DVM_ERR_PARAM;
+  if (mode == 1 && !c->eq_node) {
+    c->eq_node = calloc((size_t)c->ncells * (c->g.nv + 1), sizeof(double));
+    if (!c->eq_node) return DVM_ERR_OOM;
+  }
+  c->eq_nodes_direct = mode;
+  memset(c->cache, 0, sizeof(double) * (size_t)c->ncells * 4);
+  return DVM_OK;
 }
 
 void orc_set_threads(orc_ctx* c, int n) { c->nthreads = n > 0 ? n : 1; }
@@ -701,6 +722,7 @@ static void cdf_vr(orc_ctx* c, int cell, const double* f, orc_cellscratch* s) {
   const double* P = c->props + (size_t)cell * DVM_NPROP;
   double* eq = c->eq_pre + (size_t)cell * (g->nv + 1);
   double* cache = c->cache + (size_t)cell * 4;
+  double* node = c->eq_nodes_direct ? c->eq_node + (size_t)cell * (g->nv + 1) : NULL;
   const double mass = c->p.mass;
   const double dens = P[DVM_P_DENS], u = P[DVM_P_U], v = P[DVM_P_V], w = P[DVM_P_W];
   double temp = P[DVM_P_SPECIES_TEMP];
@@ -720,12 +742,13 @@ static void cdf_vr(orc_ctx* c, int cell, const double* f, orc_cellscratch* s) {
                                    : 0.0;
           pe = pe * b3;
           eq[l] = eq[l - 1] + pe;
+          if (node) node[l] = pe;
         }
     cache[0] = dens; cache[1] = u; cache[2] = v; cache[3] = temp;
   }
   s->cum_eq[0] = 0.0; s->cum_dev[0] = 0.0; s->kin[0] = 0.0; s->sgn[0] = 1.0;
   for (int l = 1; l <= g->nv; ++l) {
-    const double pe = eq[l] - eq[l - 1];
+    const double pe = node ? node[l] : eq[l] - eq[l - 1];
     const double pn = f[l - 1] - pe;
     s->kin[l] = pn;
     s->sgn[l] = dsgn(pn);

@@ -61,6 +61,7 @@ def lib():
             "orc_build_ref_table": (None, [D, C.c_int, I]),
             "orc_wall_ghost_2d": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D]),
             "orc_cell_cdf_vr": (C.c_int, [P, C.c_int, D, D, D, I, I]),
+            "orc_set_eq_node_mode": (C.c_int, [P, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -94,6 +95,12 @@ class OracleSolver:
         self.ncells = config.nx_space * config.ny_space
         self.nv = grid.nv
         self.ntime = 0
+
+    def set_eq_node_mode(self, direct):
+        """Test aid: True forms the equilibrium node values directly (as the GPU kernels do)
+        instead of as differences of the reference's running sum; see orc_set_eq_node_mode."""
+        if self.L.orc_set_eq_node_mode(self.ctx, 1 if direct else 0):
+            raise RuntimeError("oracle: cannot set the equilibrium node mode")
 
     def close(self):
         if getattr(self, "ctx", None):

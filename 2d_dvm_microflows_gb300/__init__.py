@@ -446,34 +446,101 @@ class DVMServer:
         return {"completed": n.value, "peak_active": a.value, "peak_bytes": b.value}
 
 
-# Tecplot output of the moments, in the layout of write_properties
-# (input_output/visualization.f90:620-660, 1591-1660): a title, a variables line, and per
-# output time a zone of rows "time x y <properties>", cells ordered x outer, y inner.
-TECPLOT_FIELDS = (("Density", DVM_P_DENS), ("X-Velocity", DVM_P_U), ("Y-Velocity", DVM_P_V),
-                  ("Z-Velocity", DVM_P_W), ("Temperature", DVM_P_TEMP),
-                  ("Avg Speed", DVM_P_AVG_SPEED), ("Pressure", DVM_P_PRESSURE),
-                  ("Heat Flux X", DVM_P_QX), ("Heat Flux Y", DVM_P_QY),
-                  ("Heat Flux Z", DVM_P_QZ))
-TECPLOT_STRESS = (("xx", DVM_P_TXX), ("yy", DVM_P_TYY), ("zz", DVM_P_TZZ), ("xy", DVM_P_TXY),
-                  ("xz", DVM_P_TXZ), ("yz", DVM_P_TYZ))
+# Tecplot output: the reference's visualization module (input_output/visualization.f90),
+# written by the library's host code (dvm_vis_* in the C ABI) so that this host and the
+# C++ one write the same bytes.
+VIS_PROPERTY_KEYS = ("write_dens", "write_x_vel", "write_y_vel", "write_z_vel", "write_speed",
+                     "write_mach", "write_tr_temp", "write_rot_temp", "write_vib_temp",
+                     "write_tot_temp", "write_temp_x", "write_temp_y", "write_temp_z",
+                     "write_tr_energy", "write_rot_energy", "write_vib_energy",
+                     "write_tot_energy", "write_entropy", "write_heat_flux_x",
+                     "write_heat_flux_y", "write_heat_flux_z", "write_rot_dof",
+                     "write_vib_dof", "write_rot_temp_relax", "write_vib_temp_relax",
+                     "write_kin_temp_relax", "write_pressure")
 
 
-def write_properties_header(path):
-    names = ['"Time"', '"x-Location"', '"y-Location"'] + ['"%s"' % n for n, _ in TECPLOT_FIELDS]
-    names += ['"Tau %s"' % n for n, _ in TECPLOT_STRESS]
-    with open(path, "w") as fh:
-        fh.write('title = "Macroscopic Properties"\n')
-        fh.write("variables = " + ", ".join(names) + "\n")
+class TecplotOutput:
+    """The reference's output files for one monatomic species: `write_headers`, then
+    `write_properties` and `write_df` at each output time (write_vis_data,
+    visualization.f90:870-918, calls them at ntime % dump_freq == 0 and at the last step).
+
+    `properties` holds the deck's write_* flags by name (VIS_PROPERTY_KEYS, the order of the
+    reference's property_names); `stress` the stress_directions (11, 22, 33, 12, 13, 23);
+    `moments` the moment_numbers (written to the species file, zero in the mixture file);
+    `df_locations` the 1-based (x, y) cells of the distribution-function files."""
+
+    def __init__(self, nx_space, ny_space, dx, dy, mass=1.0, omega=0.5, end_time=0,
+                 properties_filename=None, properties=(), properties_dump_freq=1,
+                 stress=(), moments=(), df_filename=None, df_locations=(), df_dimension=1,
+                 enable_vel_df=True, rot_levels=0, vib_levels=0, pi_mode=DVM_PI_REFERENCE,
+                 right_wall_dens=1.0, cZr=0.0, cZv=0.0, right_wall_temp_rot=0.0,
+                 right_wall_temp_vib=0.0, lib=None):
+        self.lib = lib or load_library()
+        v = dvm_vis()
+        if properties_filename:
+            v.properties_filename = properties_filename.encode()
+            v.enable_properties = 1
+        for key in properties:
+            v.properties_to_output[VIS_PROPERTY_KEYS.index(key)] = 1
+        if len(stress) > 6:
+            raise ValueError("at most six stress components")
+        v.write_stress = len(stress)
+        for i, d in enumerate(stress):
+            v.stress_directions[i] = int(d)
+        if len(moments) > 6:
+            raise ValueError("at most six moment columns")
+        v.write_moment = len(moments)
+        for i, d in enumerate(moments):
+            v.moment_numbers[i] = int(d)
+        v.nx_space, v.ny_space, v.dx, v.dy = nx_space, ny_space, dx, dy
+        v.end_time, v.properties_dump_freq = int(end_time), int(properties_dump_freq)
+        if df_filename:
+            if not 1 <= len(df_locations) <= 16:
+                raise ValueError("1 to 16 distribution-function locations")
+            v.df_filename = df_filename.encode()
+            v.enable_vel_df = 1 if enable_vel_df else 0
+            v.enable_rot_df = 1 if rot_levels else 0
+            v.enable_vib_df = 1 if vib_levels else 0
+            v.df_dimension = int(df_dimension)
+            v.num_locations = len(df_locations)
+            for i, (x, y) in enumerate(df_locations):
+                v.x_locations[i], v.y_locations[i] = int(x), int(y)
+        v.rot_levels, v.vib_levels, v.pi_mode = int(rot_levels), int(vib_levels), int(pi_mode)
+        v.mass, v.omega, v.cZr, v.cZv = mass, omega, cZr, cZv
+        v.right_wall_dens = right_wall_dens
+        v.right_wall_temp_rot, v.right_wall_temp_vib = right_wall_temp_rot, right_wall_temp_vib
+        self.vis = v
+
+    def write_headers(self):
+        _check(self.lib.dvm_vis_write_headers(C.byref(self.vis)), "dvm_vis_write_headers")
+
+    def write_properties(self, time, props=None, f=None, grid=None):
+        """props[cells, DVM_NPROP] (device moments) and/or f[cells, Nv]; with f every column
+        is formed from it the way the reference forms it."""
+        pp = fp = None
+        keep = []
+        if props is not None:
+            props = np.ascontiguousarray(props, dtype=np.float64)
+            keep.append(props)
+            pp = _dptr(props)
+        vg = None
+        if f is not None:
+            f = np.ascontiguousarray(f, dtype=np.float64)
+            keep.append(f)
+            fp = _dptr(f)
+            vg = C.byref(make_vgrid(grid))
+        _check(self.lib.dvm_vis_write_properties(C.byref(self.vis), float(time), pp, fp, vg),
+               "dvm_vis_write_properties")
+
+    def write_df(self, time, f, grid):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        _check(self.lib.dvm_vis_write_df(C.byref(self.vis), float(time), _dptr(f),
+                                         C.byref(make_vgrid(grid))), "dvm_vis_write_df")
 
 
-def append_properties(path, time, props, nx_space, ny_space, dx, dy):
-    """One output time: props[cells, DVM_NPROP] with cell = cx + nx_space * cy."""
-    props = np.asarray(props).reshape(nx_space * ny_space, DVM_NPROP)
-    cols = [q for _, q in TECPLOT_FIELDS] + [q for _, q in TECPLOT_STRESS]
-    with open(path, "a") as fh:
-        fh.write("zone i=%5d\n" % (nx_space * ny_space))
-        for cx in range(nx_space):
-            for cy in range(ny_space):
-                p = props[cx + nx_space * cy]
-                row = [time, (cx + 0.5) * dx, (cy + 0.5) * dy] + [p[q] for q in cols]
-                fh.write("".join("%24.15e" % v for v in row) + "\n")
+def fortran_e(x, w, d, lib=None):
+    """One Ew.d field as the reference's format statements write it."""
+    lib = lib or load_library()
+    buf = C.create_string_buffer(w + 1)
+    _check(lib.dvm_vis_format_e(float(x), w, d, buf, w + 1), "dvm_vis_format_e")
+    return buf.value.decode()

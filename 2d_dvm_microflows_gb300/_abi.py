@@ -9,7 +9,7 @@ DVM_ABI_VERSION = 2
 
 # status codes
 DVM_OK, DVM_ERR_PARAM, DVM_ERR_OOM, DVM_ERR_CUDA, DVM_ERR_NUMERIC, DVM_ERR_TIMEOUT, \
-    DVM_ERR_NODEVICE, DVM_ERR_TOO_LARGE = range(8)
+    DVM_ERR_NODEVICE, DVM_ERR_TOO_LARGE, DVM_ERR_IO = range(9)
 
 # device error word bits
 DVM_EW_SEARCH, DVM_EW_REMAP, DVM_EW_NONFINITE, DVM_EW_NEGDENS, DVM_EW_WAIT = 1, 2, 4, 8, 16
@@ -75,6 +75,30 @@ class dvm_request_info(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+# Tecplot output settings (visualization.f90); see dvm_vis in the header
+DVM_VIS_NPROP = 27
+DVM_VIS_DF_1D, DVM_VIS_DF_2D, DVM_VIS_DF_3D = 1, 2, 3
+
+
+class dvm_vis(C.Structure):
+    _fields_ = [("properties_filename", C.c_char * 128), ("df_filename", C.c_char * 128),
+                ("enable_properties", C.c_int32),
+                ("properties_to_output", C.c_int32 * DVM_VIS_NPROP),
+                ("write_stress", C.c_int32), ("stress_directions", C.c_int32 * 6),
+                ("write_moment", C.c_int32), ("moment_numbers", C.c_int32 * 6),
+                ("nx_space", C.c_int32), ("ny_space", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double),
+                ("end_time", C.c_int32), ("properties_dump_freq", C.c_int32),
+                ("enable_vel_df", C.c_int32), ("enable_rot_df", C.c_int32),
+                ("enable_vib_df", C.c_int32), ("df_dimension", C.c_int32),
+                ("num_locations", C.c_int32), ("x_locations", C.c_int32 * 16),
+                ("y_locations", C.c_int32 * 16), ("rot_levels", C.c_int32),
+                ("vib_levels", C.c_int32), ("pi_mode", C.c_int32),
+                ("mass", C.c_double), ("omega", C.c_double),
+                ("cZr", C.c_double), ("cZv", C.c_double), ("right_wall_dens", C.c_double),
+                ("right_wall_temp_rot", C.c_double), ("right_wall_temp_vib", C.c_double)]
+
+
 # Entry points declared in include/dvm_gpu.h: name -> (restype, argtypes)
 _P = C.c_void_p
 ENTRY_POINTS = {
@@ -134,6 +158,13 @@ ENTRY_POINTS = {
     "dvm_server_set_preemption": (C.c_int, [_P, C.c_int32]),
     "dvm_collide_noalloc": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), _P, _P,
                                       C.c_int, C.c_uint64, _P, C.POINTER(C.c_int64)]),
+    "dvm_vis_write_headers": (C.c_int, [C.POINTER(dvm_vis)]),
+    "dvm_vis_write_properties": (C.c_int, [C.POINTER(dvm_vis), C.c_double,
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                           C.POINTER(dvm_vgrid)]),
+    "dvm_vis_write_df": (C.c_int, [C.POINTER(dvm_vis), C.c_double, C.POINTER(C.c_double),
+                                   C.POINTER(dvm_vgrid)]),
+    "dvm_vis_format_e": (C.c_int, [C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int]),
 }
 
 

@@ -20,7 +20,10 @@ HOST = os.path.join(HERE, "dvm_host")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
-SOURCES = ["dvm_kernels.cu", "dvm_api.cu", "dvm_noalloc.cu", "dvm_server.cu"]
+SOURCES = ["dvm_kernels.cu", "dvm_api.cu", "dvm_noalloc.cu", "dvm_server.cu", "dvm_vis.cpp"]
+# the output writer restates the reference's FP64 sums operation by operation: no contraction
+# into fused multiply-adds (the host compiler's default on aarch64)
+EXTRA = {"dvm_vis.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc():
@@ -35,7 +38,7 @@ def nvcc():
 
 def _compile(src):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc()] + ARCH + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc()] + ARCH + NVFLAGS + EXTRA.get(src, []) + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
@@ -60,7 +63,9 @@ def build(verbose=False):
     if os.path.exists(host_src):
         cxx = shutil.which("g++") or "g++"
         cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
-        cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(REPO, "include"), "-I", cuda_inc,
+        # the initial states restate the reference's FP64 operations: no fused multiply-adds
+        cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
+               "-I", cuda_inc,
                host_src, "-o", HOST, "-L", HERE, "-ldvm_gpu", "-Wl,-rpath,$ORIGIN", "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -401,6 +401,7 @@ const char* dvm_strerror(int status) {
     case DVM_ERR_TIMEOUT: return "device wait timed out";
     case DVM_ERR_NODEVICE: return "no CUDA device";
     case DVM_ERR_TOO_LARGE: return "problem exceeds the 32 MiB no-allocation scratch array";
+    case DVM_ERR_IO: return "an output file could not be opened or written";
     default: return "unknown status";
   }
 }

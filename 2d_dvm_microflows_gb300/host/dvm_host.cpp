@@ -3,18 +3,27 @@
 // running through the C ABI of include/dvm_gpu.h.
 //
 //   dvm_host <input deck> [--check] [--steps N] [--dump-f FILE] [--dump-props FILE]
+//            [--restart-in FILE] [--restart-out FILE]
 //
 // The deck is the reference's `key = value` format (input_output/read_input_2D.f90:75-777;
 // e.g. trunk/bin/velocity_refined.inp): [sections] and `#` comments are skipped, values may
-// be quoted and may use Fortran exponents (1.0d0). Keys read: Kn, species_codes,
-// csection_method, csection_coeff, delta_x, delta_y, nx_space, ny_space, deltat, ntstep,
-// num_points_{x,y,z}, {x,y,z}v_{min,max}, InitC, InitDF, dens_init, {x,y,z}_vel_init,
-// tr_temp_init, {dens,x_vel,y_vel,z_vel,tr_temp}_{LW,RW,BW,TW}, {L,R,B,T}WallBC,
-// acc_coeff, iColl, cdf_tolerance, NRepl, ColnRMS, iConv, display_freq. Keys this build
-// adds: geometry, samples_per_step, seed, pi_mode, and for the initial states of the
-// benchmark configurations InitC = 6 (two drifting Maxwellians: bimodal_T_ratio,
-// bimodal_drift) and InitC = 7 (Rankine-Hugoniot shock joined by a tanh profile:
-// mach_number, shock_width).
+// be quoted and may use Fortran exponents (1.0d0); a key holding several entries (one per
+// species or zone, '11 11') gives its first, as the reference's per-species reads do for
+// species 1. Keys read: Kn, species_codes, csection_method, csection_coeff, delta_x,
+// delta_y, nx_space, ny_space, deltat, ntstep, num_points_{x,y,z}, {x,y,z}v_{min,max},
+// InitC, InitDF, spatial_middle, dens_init, {x,y,z}_vel_init, tr_temp_init,
+// {x,y,z}_delta_loc, {dens,x_vel,y_vel,z_vel,tr_temp}_{LW,RW,BW,TW}, {L,R,B,T}WallBC,
+// acc_coeff, iColl, cdf_tolerance, NRepl, ColnRMS, iConv, display_freq, and the output keys
+// of the [vis] section (enable_properties_vis, properties_vis_filename,
+// properties_vis_dump_freq, write_* of each property, write_stress, stress_directions,
+// write_moment, moment_numbers, enable_{vel,rot,vib}_df_vis, df_vis_filename,
+// df_vis_dump_freq, num_output_locations, {x,y}_output_locations, df_output_dimension,
+// num_rot_levels, num_vib_levels). Decks of the earlier GRVY reader name the cell count
+// nspace; it is read as nx_space when nx_space is absent, and num_zones > 1 (per-zone
+// velocity grids) is refused. Keys this build adds: geometry, samples_per_step, seed,
+// pi_mode, and for the initial states of the benchmark configurations InitC = 6 (two
+// drifting Maxwellians: bimodal_T_ratio, bimodal_drift) and InitC = 7 (Rankine-Hugoniot
+// shock joined by a tanh profile: mach_number, shock_width).
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -82,6 +91,16 @@ struct Deck {
     std::string v = str(k, "");
     return v.empty() ? def : std::strtoll(v.c_str(), nullptr, 10);
   }
+  // every entry of a vector key (x_output_locations = '1 4')
+  std::vector<long long> integers(const std::string& k) const {
+    std::vector<long long> out;
+    auto it = kv.find(k);
+    if (it == kv.end()) return out;
+    std::istringstream ss(it->second);
+    std::string tok;
+    while (ss >> tok) out.push_back(std::strtoll(tok.c_str(), nullptr, 10));
+    return out;
+  }
 };
 
 // gamma_calculator (utils/math_utils.f90:79-135): Lanczos, g = 7, the nine published
@@ -126,7 +145,14 @@ class Host {
   // read_input_grvy + set_molecule_constants + create_velocity_grid (host side)
   bool read_input(const Deck& d, std::string& err) {
     std::memset(&p, 0, sizeof(p));
-    p.nx_space = static_cast<int>(d.integer("nx_space", 1));
+    if (d.integer("num_zones", 1) > 1) {
+      err = "num_zones = " + d.str("num_zones", "") +
+            ": per-zone velocity grids are not supported (one grid for every cell)";
+      return false;
+    }
+    // the earlier reader's name for the cell count
+    p.nx_space = static_cast<int>(d.has("nx_space") ? d.integer("nx_space", 1)
+                                                    : d.integer("nspace", 1));
     p.ny_space = static_cast<int>(d.integer("ny_space", 1));
     const int geo_default = (p.nx_space == 1 && p.ny_space == 1) ? DVM_GEOM_0D
                             : (p.ny_space == 1 ? DVM_GEOM_1D : DVM_GEOM_2D);
@@ -193,52 +219,106 @@ class Host {
     return true;
   }
 
-  // Discrete Maxwellian times the node volume, renormalised to n
-  // (conditions/initial_conditions.f90:480-617).
-  void maxwellian(double* out, double n, double u, double v, double w, double T) const {
-    const double pi = p.pi_mode == DVM_PI_EXACT ? kPiExact : kPiReference;
-    auto beta = [](const std::vector<double>& a, size_t i) {
-      const size_t N = a.size();
-      if (i == 0) return a[1] - a[0];
-      if (i == N - 1) return a[N - 1] - a[N - 2];
-      return (a[i + 1] - a[i]) / 2.0 + (a[i] - a[i - 1]) / 2.0;
-    };
-    const double opt = p.mass / (pi * T);
-    const double coeff = n * std::sqrt(opt * opt * opt);
-    double sum = 0.0;
-    size_t l = 0;
-    for (size_t k = 0; k < z.size(); ++k)
-      for (size_t j = 0; j < y.size(); ++j)
-        for (size_t i = 0; i < x.size(); ++i, ++l) {
-          const double c2 = (x[i] - u) * (x[i] - u) + (y[j] - v) * (y[j] - v) + (z[k] - w) * (z[k] - w);
-          out[l] = coeff * std::exp(-c2 * p.mass / T) * beta(x, i) * beta(y, j) * beta(z, k);
-          sum += out[l];
-        }
-    if (sum > 0.0)
-      for (size_t q = 0; q < l; ++q) out[q] = (n / sum) * out[q];
+  // compute_beta (grid/velocity_grid.f90:486-540)
+  static double beta(const std::vector<double>& a, size_t i) {
+    const size_t N = a.size();
+    if (i == 0) return a[1] - a[0];
+    if (i == N - 1) return a[N - 1] - a[N - 2];
+    return (a[i + 1] - a[i]) / 2.0 + (a[i] - a[i - 1]) / 2.0;
   }
 
-  // initialize_dist_func (conditions/initial_conditions.f90:212-650), Maxwellian states.
+  // One cell of initialize_dist_func (conditions/initial_conditions.f90:465-617): the
+  // velocity distribution InitDF (1 Maxwellian, 2 BKW at K = 3/5, 3 a delta function at
+  // {x,y,z}_delta_loc, 4 the Maxwellian integrated exactly over each node's cell) of the
+  // local state, times the node volume, then scaled so that its sum is the density. A zero
+  // density leaves the cell empty (:456-469).
+  void fill_cell(double* out, int initdf, double n, double u, double v, double w, double T,
+                 const double delta[3]) const {
+    const size_t nv = x.size() * y.size() * z.size();
+    if (n == 0.0) {
+      for (size_t l = 0; l < nv; ++l) out[l] = 0.0;
+      return;
+    }
+    const double pi = p.pi_mode == DVM_PI_EXACT ? kPiExact : kPiReference;
+    const double mass = p.mass;
+    const double opt = mass / (pi * T);
+    const double maxwell_coeff = n * std::sqrt(opt * opt * opt);
+    const double bkw_xk = 1.0 - 0.4 * std::exp(-0.0 / 6.0);
+    const double bkw_norm = 0.5 * n * std::sqrt(opt * opt * opt) * std::pow(bkw_xk, -2.5);
+    double calculated = 0.0;
+    size_t l = 0;
+    for (size_t k = 0; k < z.size(); ++k) {
+      const double bz = beta(z, k);
+      const double z1 = k > 0 ? z[k - 1] : z[k] - bz, z2 = k + 1 < z.size() ? z[k + 1] : z[k] + bz;
+      for (size_t j = 0; j < y.size(); ++j) {
+        const double by = beta(y, j);
+        const double y1 = j > 0 ? y[j - 1] : y[j] - by, y2 = j + 1 < y.size() ? y[j + 1] : y[j] + by;
+        for (size_t i = 0; i < x.size(); ++i, ++l) {
+          const double bx = beta(x, i);
+          const double b3 = bx * by * bz;
+          double cxsq = (x[i] - u);
+          cxsq = cxsq * cxsq;
+          double cysq = (y[j] - v);
+          cysq = cysq * cysq;
+          double czsq = (z[k] - w);
+          czsq = czsq * czsq;
+          const double csq = cxsq + cysq + czsq;
+          double df = 0.0;
+          if (initdf == 1) {  // compute_maxwellian (dist_funcs/dist_func.f90:317-343)
+            df = maxwell_coeff * std::exp(-csq * mass / T);
+          } else if (initdf == 2) {  // compute_bkw (:374-401)
+            df = bkw_norm * (5.0 * bkw_xk - 3.0 + 2.0 * (1.0 - bkw_xk) * csq * mass / (bkw_xk * T)) *
+                 std::exp(-csq * mass / (bkw_xk * T));
+          } else if (initdf == 3) {
+            df = (std::fabs(delta[0] - x[i]) < 1.0e-13 && std::fabs(delta[1] - y[j]) < 1.0e-13 &&
+                  std::fabs(delta[2] - z[k]) < 1.0e-13) ? n / b3 : 0.0;
+          } else {  // compute_exact_gaussian (:345-372)
+            const double x1 = i > 0 ? x[i - 1] : x[i] - bx, x2 = i + 1 < x.size() ? x[i + 1] : x[i] + bx;
+            const double C2 = mass / T, sq = std::sqrt(C2);
+            const double xl = sq * (x1 + 0.5 * (x[i] - x1) - u), xr = sq * (x[i] + 0.5 * (x2 - x[i]) - u);
+            const double yl = sq * (y1 + 0.5 * (y[j] - y1) - v), yr = sq * (y[j] + 0.5 * (y2 - y[j]) - v);
+            const double zl = sq * (z1 + 0.5 * (z[k] - z1) - w), zr = sq * (z[k] + 0.5 * (z2 - z[k]) - w);
+            const double Cx = std::erf(xr) - std::erf(xl);
+            const double Cy = std::erf(yl) - std::erf(yr);
+            const double Cz = std::erf(zl) - std::erf(zr);
+            df = 0.125 * maxwell_coeff * std::pow(pi / C2, 1.5) * Cx * Cy * Cz;
+          }
+          out[l] = df * b3;
+          calculated = calculated + out[l];
+        }
+      }
+    }
+    const double ratio = n / calculated;
+    for (size_t q = 0; q < l; ++q) out[q] = ratio * out[q];
+  }
+
+  // initialize_dist_func (conditions/initial_conditions.f90:212-650). InitC: 1 every cell in
+  // the left wall's state, 2 in the right wall's, 3 the left wall's up to spatial_middle and
+  // the right wall's beyond, 5 the *_init state; this build's 6 and 7 are described at the
+  // top of the file. A state that comes out non-finite is refused.
   bool initial_state(const Deck& d, std::string& err) {
     f.assign(static_cast<size_t>(ncells) * nv, 0.0);
-    if (d.integer("InitDF", 1) != 1) { err = "only InitDF = 1 (Maxwellian) is supported"; return false; }
+    const int initdf = static_cast<int>(d.integer("InitDF", 1));
+    if (initdf < 1 || initdf > 4) { err = "InitDF " + std::to_string(initdf) + " not supported"; return false; }
     const int initc = static_cast<int>(d.integer("InitC", 5));
+    const double delta[3] = {d.num("x_delta_loc", 0.0), d.num("y_delta_loc", 0.0), d.num("z_delta_loc", 0.0)};
+    const long long space_mid = d.integer("spatial_middle", p.nx_space / 2);
     std::vector<double> tmp(nv);
     for (int c = 0; c < ncells; ++c) {
       double* fc = f.data() + static_cast<size_t>(c) * nv;
       const int cx = c % p.nx_space;
       if (initc == 1 || initc == 2 || initc == 3) {
-        const int w = (initc == 1 || (initc == 3 && cx < p.nx_space / 2)) ? 0 : 1;
-        maxwellian(fc, p.wall[w][0], p.wall[w][1], p.wall[w][2], p.wall[w][3], p.wall[w][4]);
+        const int w = (initc == 1 || (initc == 3 && cx + 1 <= space_mid)) ? 0 : 1;
+        fill_cell(fc, initdf, p.wall[w][0], p.wall[w][1], p.wall[w][2], p.wall[w][3], p.wall[w][4], delta);
       } else if (initc == 5) {
-        maxwellian(fc, d.num("dens_init", 1.0), d.num("x_vel_init", 0.0), d.num("y_vel_init", 0.0),
-                   d.num("z_vel_init", 0.0), d.num("tr_temp_init", 1.0));
-      } else if (initc == 6) {
+        fill_cell(fc, initdf, d.num("dens_init", 1.0), d.num("x_vel_init", 0.0), d.num("y_vel_init", 0.0),
+                  d.num("z_vel_init", 0.0), d.num("tr_temp_init", 1.0), delta);
+      } else if (initc == 6 && initdf == 1) {
         const double Tr = d.num("bimodal_T_ratio", 3.0), u = d.num("bimodal_drift", 1.0);
-        maxwellian(fc, 1.0, u, 0.0, 0.0, 1.0);
-        maxwellian(tmp.data(), 1.0, -u, 0.0, 0.0, Tr);
+        fill_cell(fc, 1, 1.0, u, 0.0, 0.0, 1.0, delta);
+        fill_cell(tmp.data(), 1, 1.0, -u, 0.0, 0.0, Tr, delta);
         for (int l = 0; l < nv; ++l) fc[l] = 0.5 * fc[l] + 0.5 * tmp[l];
-      } else if (initc == 7) {
+      } else if (initc == 7 && initdf == 1) {
         // stationary shock, flow in -x (conditions/shock_conditions.f90:54-171)
         const double M = d.num("mach_number", 1.5), width = d.num("shock_width", 10.0);
         const double g = 5.0 / 3.0, Tu = 1.0, nu = 1.0;
@@ -249,17 +329,28 @@ class Host {
         const double Md = std::sqrt((1.0 + 0.5 * (g - 1.0) * M * M) / (g * M * M - 0.5 * (g - 1.0)));
         const double Td = Tr * Tu, nd = nr * nu, ud = -std::sqrt(g * Td / (2.0 * p.mass)) * Md;
         const double xc = (cx + 0.5) * p.dx, x0 = 0.5 * p.nx_space * p.dx;
-        const double s = 0.5 * (1.0 + std::tanh((xc - x0) / width));
-        maxwellian(fc, nd + (nu - nd) * s, ud + (u_up - ud) * s, 0.0, 0.0, Td + (Tu - Td) * s);
+        const double sh = 0.5 * (1.0 + std::tanh((xc - x0) / width));
+        fill_cell(fc, 1, nd + (nu - nd) * sh, ud + (u_up - ud) * sh, 0.0, 0.0, Td + (Tu - Td) * sh, delta);
         if (c == 0) {  // inflow states of both ends
           const double L[5] = {nd, ud, 0.0, 0.0, Td}, R[5] = {nu, u_up, 0.0, 0.0, Tu};
           for (int q = 0; q < 5; ++q) { p.wall[0][q] = L[q]; p.wall[1][q] = R[q]; }
         }
+      } else if (initc == 4) {
+        err = "InitC 4 (the reference's linear Rankine-Hugoniot ramp) is not supported; "
+              "InitC 7 builds the shock joined by a tanh profile";
+        return false;
       } else {
-        err = "InitC " + std::to_string(initc) + " not supported";
+        err = "InitC " + std::to_string(initc) + " with InitDF " + std::to_string(initdf) +
+              " not supported";
         return false;
       }
     }
+    for (double v : f)
+      if (!std::isfinite(v)) {
+        err = "the initial state is not finite (InitC " + std::to_string(initc) +
+              ": check the density and temperature it takes)";
+        return false;
+      }
     return true;
   }
 
@@ -282,46 +373,112 @@ class Host {
                 static_cast<long long>(colls));
   }
 
-  // solve (solver/dvm_solver.f90:231-369)
-  // Tecplot output of the moments in the layout of write_properties
-  // (input_output/visualization.f90:620-660, 1591-1660).
-  const char* props_dat = nullptr;
-  long long props_every = 1;
+  // Output (input_output/visualization.f90): the deck's [vis] settings, written through
+  // dvm_vis_* from f downloaded at each output time.
+  dvm_vis vis{};
+  bool vis_props = false, vis_df = false;
+  long long props_freq = 1, df_freq = 1;
 
-  void write_props_header() const {
-    FILE* fp = std::fopen(props_dat, "w");
-    if (!fp) return;
-    std::fprintf(fp, "title = \"Macroscopic Properties\"\n");
-    std::fprintf(fp, "variables = \"Time\", \"x-Location\", \"y-Location\", \"Density\", "
-                     "\"X-Velocity\", \"Y-Velocity\", \"Z-Velocity\", \"Temperature\", "
-                     "\"Avg Speed\", \"Pressure\", \"Heat Flux X\", \"Heat Flux Y\", "
-                     "\"Heat Flux Z\", \"Tau xx\", \"Tau yy\", \"Tau zz\", \"Tau xy\", "
-                     "\"Tau xz\", \"Tau yz\"\n");
-    std::fclose(fp);
+  bool read_vis(const Deck& d, std::string& err) {
+    std::memset(&vis, 0, sizeof(vis));
+    static const char* keys[DVM_VIS_NPROP] = {
+        "write_dens", "write_x_vel", "write_y_vel", "write_z_vel", "write_speed", "write_mach",
+        "write_tr_temp", "write_rot_temp", "write_vib_temp", "write_tot_temp", "write_temp_x",
+        "write_temp_y", "write_temp_z", "write_tr_energy", "write_rot_energy",
+        "write_vib_energy", "write_tot_energy", "write_entropy", "write_heat_flux_x",
+        "write_heat_flux_y", "write_heat_flux_z", "write_rot_dof", "write_vib_dof",
+        "write_rot_temp_relax", "write_vib_temp_relax", "write_kin_temp_relax",
+        "write_pressure"};
+    vis_props = d.integer("enable_properties_vis", 0) != 0;
+    vis_df = d.integer("enable_vel_df_vis", 0) != 0 || d.integer("enable_rot_df_vis", 0) != 0 ||
+             d.integer("enable_vib_df_vis", 0) != 0;
+    auto name = [&](const char* key, const char* def, char* out) {
+      const std::string v = d.str(key, def);
+      if (v.size() >= 128) return false;
+      std::memcpy(out, v.c_str(), v.size() + 1);
+      return true;
+    };
+    if (!name("properties_vis_filename", "properties", vis.properties_filename) ||
+        !name("df_vis_filename", "dist_func", vis.df_filename)) {
+      err = "output file name longer than 127 characters";
+      return false;
+    }
+    vis.enable_properties = vis_props ? 1 : 0;
+    for (int i = 0; i < DVM_VIS_NPROP; ++i)
+      vis.properties_to_output[i] = d.integer(keys[i], 0) != 0 ? 1 : 0;
+    const std::vector<long long> sd = d.integers("stress_directions");
+    vis.write_stress = static_cast<int32_t>(d.integer("write_stress", 0));
+    if (vis.write_stress < 0 || vis.write_stress > 6 ||
+        static_cast<long long>(sd.size()) < vis.write_stress) {
+      err = "write_stress needs that many stress_directions (at most 6)";
+      return false;
+    }
+    for (int i = 0; i < vis.write_stress; ++i) vis.stress_directions[i] = static_cast<int32_t>(sd[i]);
+    const std::vector<long long> mn = d.integers("moment_numbers");
+    vis.write_moment = static_cast<int32_t>(d.integer("write_moment", 0));
+    if (vis.write_moment < 0 || vis.write_moment > 6 ||
+        static_cast<long long>(mn.size()) < vis.write_moment) {
+      err = "write_moment needs that many moment_numbers (at most 6)";
+      return false;
+    }
+    for (int i = 0; i < vis.write_moment; ++i) vis.moment_numbers[i] = static_cast<int32_t>(mn[i]);
+    vis.nx_space = p.nx_space;
+    vis.ny_space = p.ny_space;
+    vis.dx = p.dx;
+    vis.dy = p.dy;
+    vis.end_time = static_cast<int32_t>(ntstep);
+    props_freq = std::max(1LL, d.integer("properties_vis_dump_freq", 1));
+    df_freq = std::max(1LL, d.integer("df_vis_dump_freq", 1));
+    vis.properties_dump_freq = static_cast<int32_t>(props_freq);
+    vis.enable_vel_df = d.integer("enable_vel_df_vis", 0) != 0;
+    vis.enable_rot_df = d.integer("enable_rot_df_vis", 0) != 0;
+    vis.enable_vib_df = d.integer("enable_vib_df_vis", 0) != 0;
+    vis.df_dimension = static_cast<int32_t>(d.integer("df_output_dimension", DVM_VIS_DF_1D));
+    const std::vector<long long> xl = d.integers("x_output_locations"),
+                                 yl = d.integers("y_output_locations");
+    vis.num_locations = static_cast<int32_t>(d.integer("num_output_locations", 0));
+    if (vis_df && (vis.num_locations < 1 || vis.num_locations > 16 ||
+                   static_cast<long long>(xl.size()) < vis.num_locations ||
+                   static_cast<long long>(yl.size()) < vis.num_locations)) {
+      err = "distribution-function output needs 1 to 16 x/y_output_locations";
+      return false;
+    }
+    for (int i = 0; i < vis.num_locations && i < 16; ++i) {
+      vis.x_locations[i] = static_cast<int32_t>(xl[i]);
+      vis.y_locations[i] = static_cast<int32_t>(yl[i]);
+    }
+    vis.rot_levels = static_cast<int32_t>(d.integer("num_rot_levels", 0));
+    vis.vib_levels = static_cast<int32_t>(d.integer("num_vib_levels", 0));
+    vis.pi_mode = p.pi_mode;
+    vis.mass = p.mass;
+    vis.omega = p.omega;
+    vis.right_wall_dens = p.wall[DVM_WALL_RIGHT][DVM_WP_DENS];
+    vis.right_wall_temp_rot = d.num("rot_temp_RW", 0.0);
+    vis.right_wall_temp_vib = d.num("vib_temp_RW", 0.0);
+    return true;
   }
 
-  int write_props(long long ntime) const {
-    std::vector<double> pr(static_cast<size_t>(ncells) * DVM_NPROP);
-    int st = dvm_get_properties(ctx, pr.data());
-    if (st) return st;
-    FILE* fp = std::fopen(props_dat, "a");
-    if (!fp) return DVM_ERR_PARAM;
-    static const int cols[] = {DVM_P_DENS, DVM_P_U, DVM_P_V, DVM_P_W, DVM_P_TEMP, DVM_P_AVG_SPEED,
-                               DVM_P_PRESSURE, DVM_P_QX, DVM_P_QY, DVM_P_QZ, DVM_P_TXX, DVM_P_TYY,
-                               DVM_P_TZZ, DVM_P_TXY, DVM_P_TXZ, DVM_P_TYZ};
-    std::fprintf(fp, "zone i=%5d\n", ncells);
+  // write_vis_data (visualization.f90:870-918): at ntime = 0, every dump_freq steps and at
+  // the last step, time = ntime * deltat
+  int write_vis(long long ntime, bool headers) {
+    if (!vis_props && !vis_df) return DVM_OK;
+    int st = DVM_OK;
+    if (headers && (st = dvm_vis_write_headers(&vis))) return st;
+    const bool last = ntime % std::max(1LL, ntstep) == 0;
+    const bool want_props = vis_props && (last || ntime % props_freq == 0);
+    const bool want_df = vis_df && (last || ntime % df_freq == 0);
+    if (!want_props && !want_df) return DVM_OK;
+    std::vector<double> fh(static_cast<size_t>(ncells) * nv);
+    if ((st = dvm_download_f(ctx, fh.data()))) return st;
+    dvm_vgrid vg{static_cast<int32_t>(x.size()), static_cast<int32_t>(y.size()),
+                 static_cast<int32_t>(z.size()), x.data(), y.data(), z.data()};
     const double time = static_cast<double>(ntime) * p.dt;
-    for (int cx = 0; cx < p.nx_space; ++cx)
-      for (int cy = 0; cy < p.ny_space; ++cy) {
-        const double* q = pr.data() + static_cast<size_t>(cx + p.nx_space * cy) * DVM_NPROP;
-        std::fprintf(fp, "%24.15e%24.15e%24.15e", time, (cx + 0.5) * p.dx, (cy + 0.5) * p.dy);
-        for (int c : cols) std::fprintf(fp, "%24.15e", q[c]);
-        std::fprintf(fp, "\n");
-      }
-    std::fclose(fp);
+    if (want_df && (st = dvm_vis_write_df(&vis, time, fh.data(), &vg))) return st;
+    if (want_props && (st = dvm_vis_write_properties(&vis, time, nullptr, fh.data(), &vg))) return st;
     return DVM_OK;
   }
 
+  // solve (solver/dvm_solver.f90:231-369)
   int solve(long long nsteps, long long first = 0) {
     std::printf("%8s %12s %18s %18s %18s %12s\n", "ntime", "time", "dens", "x_vel", "temp", "colls");
     for (long long ntime = first + 1; ntime <= first + nsteps; ++ntime) {
@@ -330,10 +487,7 @@ class Host {
       if (!st) st = dvm_calculate_physical_properties(ctx);
       if (st) return st;
       if (ntime % display_freq == 0 || ntime == first + nsteps) print_update(ntime);
-      if (props_dat && (ntime % props_every == 0 || ntime == first + nsteps)) {
-        st = write_props(ntime);
-        if (st) return st;
-      }
+      if ((st = write_vis(ntime, false))) return st;
     }
     uint32_t word = 0;
     dvm_get_error_word(ctx, &word);
@@ -371,25 +525,21 @@ bool write_doubles(const char* path, const std::vector<double>& v) {
 int main(int argc, char** argv) {
   if (argc < 2) {
     std::fprintf(stderr, "usage: %s <input deck> [--check] [--steps N] [--dump-f FILE] "
-                         "[--dump-props FILE] [--props-dat FILE] [--props-every N] "
-                         "[--restart-in FILE] [--restart-out FILE]\n", argv[0]);
+                         "[--dump-props FILE] [--restart-in FILE] [--restart-out FILE]\n",
+                 argv[0]);
     return 1;
   }
   bool check = false;
   long long steps = -1;
   const char* dump_f = nullptr;
   const char* dump_props = nullptr;
-  const char* props_dat = nullptr;
   const char* restart_in = nullptr;
   const char* restart_out = nullptr;
-  long long props_every = 1;
   for (int a = 2; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--check")) check = true;
     else if (!std::strcmp(argv[a], "--steps") && a + 1 < argc) steps = std::atoll(argv[++a]);
     else if (!std::strcmp(argv[a], "--dump-f") && a + 1 < argc) dump_f = argv[++a];
     else if (!std::strcmp(argv[a], "--dump-props") && a + 1 < argc) dump_props = argv[++a];
-    else if (!std::strcmp(argv[a], "--props-dat") && a + 1 < argc) props_dat = argv[++a];
-    else if (!std::strcmp(argv[a], "--props-every") && a + 1 < argc) props_every = std::atoll(argv[++a]);
     else if (!std::strcmp(argv[a], "--restart-in") && a + 1 < argc) restart_in = argv[++a];
     else if (!std::strcmp(argv[a], "--restart-out") && a + 1 < argc) restart_out = argv[++a];
   }
@@ -397,7 +547,7 @@ int main(int argc, char** argv) {
   if (!deck.load(argv[1])) { std::fprintf(stderr, "Error: cannot read %s\n", argv[1]); return 1; }
   Host h;
   std::string err;
-  if (!h.read_input(deck, err) || !h.initial_state(deck, err)) {
+  if (!h.read_input(deck, err) || !h.initial_state(deck, err) || !h.read_vis(deck, err)) {
     std::fprintf(stderr, "Error: %s\n", err.c_str());
     return 1;
   }
@@ -410,6 +560,12 @@ int main(int argc, char** argv) {
                 h.p.geometry, h.ncells, h.nv, h.p.coll_method, h.p.conv_method, h.p.sigma,
                 h.p.omega, h.p.alpha, h.p.dt, h.p.Kn, h.p.samples_mode,
                 static_cast<long long>(h.p.samples_per_step), steps, mass);
+    if (mass == 0.0)
+      std::fprintf(stderr, "warning: the initial state is empty (the density InitC takes is 0)\n");
+    if (dump_f && !write_doubles(dump_f, h.f)) {  // the initial state, no device needed
+      std::fprintf(stderr, "Error: cannot write %s\n", dump_f);
+      return 1;
+    }
     return 0;
   }
   int st = h.initialize_solver();
@@ -421,12 +577,7 @@ int main(int argc, char** argv) {
     if (!st) st = dvm_checkpoint_load(h.ctx, buf.data(), buf.size(), &nt);
     first = static_cast<long long>(nt);
   }
-  h.props_dat = props_dat;
-  h.props_every = props_every > 0 ? props_every : 1;
-  if (!st && props_dat) {
-    h.write_props_header();
-    st = h.write_props(first);
-  }
+  if (!st) st = h.write_vis(first, true);
   if (!st) st = h.solve(steps, first);
   if (!st && restart_out) {
     uint64_t n = 0;

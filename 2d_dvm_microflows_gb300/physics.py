@@ -153,6 +153,34 @@ def maxwellian(grid, dens, u, v, w, temp, mass=1.0, pi_mode=0, renormalise=True)
     return f
 
 
+def bkw_xk(time):
+    """The BKW shape parameter K at time t (collision times of a Maxwell gas), from 3/5 at
+    t = 0 to 1: generate_bkw (conditions/initial_conditions.f90:693-695)."""
+    return 1.0 - 0.4 * math.exp(-time / 6.0)
+
+
+def bkw(grid, dens, temp, time=0.0, mass=1.0, u=0.0, v=0.0, w=0.0, pi_mode=0,
+        renormalise=True):
+    """Discrete Bobylev-Krook-Wu distribution times the node volume (compute_bkw,
+    dist_funcs/dist_func.f90:374-401, as generate_bkw uses it): with K = bkw_xk(time),
+    n/2 (m/(pi T))^{3/2} K^{-5/2} (5K - 3 + 2(1-K) m|c-u|^2/(K T)) exp(-m|c-u|^2/(K T)),
+    scaled so that sum(f) = n. The exact solution of the isotropic Maxwell-molecule
+    Boltzmann equation with time in units of the inverse collision frequency."""
+    pi = pi_value(pi_mode)
+    X, Y, Z, B3 = grid.mesh()
+    xk = bkw_xk(time)
+    opt = mass / (pi * temp)
+    norm = 0.5 * dens * math.sqrt(opt * opt * opt) * xk ** (-2.5)
+    csq = (X - u) ** 2 + (Y - v) ** 2 + (Z - w) ** 2
+    f = norm * (5.0 * xk - 3.0 + 2.0 * (1.0 - xk) * csq * mass / (xk * temp)) * \
+        np.exp(-csq * mass / (xk * temp)) * B3
+    if renormalise:
+        s = f.sum()
+        if s != 0:
+            f = (dens / s) * f
+    return f
+
+
 def bimodal(grid, w1=0.5, T1=1.0, u1=1.0, w2=0.5, T2=3.0, u2=-1.0, mass=1.0, pi_mode=0):
     """Sum of two renormalised Maxwellians with x-drifts (the 0-D relaxation state)."""
     return (w1 * maxwellian(grid, 1.0, u1, 0.0, 0.0, T1, mass, pi_mode) +

@@ -716,17 +716,24 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded R-H tanh shock state)", "config": config_record("gpu"),
         "cell_updates_per_s": NCELLS * args.steps * ws / (t_max * 1e-3),
-        "roofline": {"bound": "hbm", "kernel": "collide", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_sample": BYTES_PER_SAMPLE},
-        "roofline_atomic": {"kernel": "collide", "achieved": atom_achieved, "peak": atom_peak,
-                            "unit": "FP64 atomic adds/s", "frac": atom_achieved / atom_peak,
-                            "atomics_per_sample": atom_per_sample,
-                            "atomics_per_sample_source": "counted by the collide kernel",
-                            "atomics_per_sample_nominal": ATOMICS_PER_SAMPLE,
-                            "peak_source": "measured in this run (dvm_atomic_rate, pseudo-"
-                                           "random adds over a window the size of f)"},
+        # the collide kernel's read-modify-writes stay in L2 (its DRAM traffic is about 1 %
+        # of the bytes it moves), so the roofline that bounds it is the L2 FP64 atomic rate;
+        # the HBM view is kept beside it with the measured traffic
+        "roofline": {"bound": "l2_atomic", "kernel": "collide", "achieved": atom_achieved,
+                     "peak": atom_peak, "unit": "FP64 atomic adds/s",
+                     "frac": atom_achieved / atom_peak, "traffic": traffic,
+                     "atomics_per_sample": atom_per_sample,
+                     "atomics_per_sample_source": "counted by the collide kernel",
+                     "atomics_per_sample_nominal": ATOMICS_PER_SAMPLE,
+                     "peak_source": "measured in this run (dvm_atomic_rate, pseudo-random "
+                                    "FP64 adds over a window the size of f)"},
+        "roofline_hbm": {"bound": "hbm", "kernel": "collide", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": traffic,
+                         "traffic_over_algorithmic": (traffic / (samples_per_launch *
+                                                                 BYTES_PER_SAMPLE)
+                                                      if traffic else None),
+                         "algorithmic_bytes_per_sample": BYTES_PER_SAMPLE},
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "collisions/s",
                 "h2d_bytes_per_step": NCELLS * nv * 8, "d2h_bytes_per_step": NCELLS * nv * 8},

@@ -40,7 +40,8 @@ enum {
   DVM_ERR_NUMERIC = 4,    /* device error word set (see dvm_get_error_word)          */
   DVM_ERR_TIMEOUT = 5,    /* a bounded device wait ran out                           */
   DVM_ERR_NODEVICE = 6,   /* no CUDA device                                          */
-  DVM_ERR_TOO_LARGE = 7   /* problem exceeds a fixed scratch or a server's budget     */
+  DVM_ERR_TOO_LARGE = 7,  /* problem exceeds a fixed scratch or a server's budget     */
+  DVM_ERR_IO = 8          /* an output file could not be opened or written            */
 };
 
 /* Bits of the device error word. */
@@ -312,6 +313,54 @@ int dvm_atomic_rate(dvm_ctx* ctx, uint64_t window_bytes, double* per_s);
  * and sets DVM_EW_WAIT in the error word (read it with dvm_get_error_word); the context
  * stays usable. */
 int dvm_wait_selftest(dvm_ctx* ctx);
+
+/* ---- Tecplot output (input_output/visualization.f90) --------------------------------- */
+/* The reference's output files for one monatomic species, written on the host from data the
+ * caller downloaded; no device work. Replaces write_headers (visualization.f90:514-762),
+ * write_properties (:1591-1716, with get_data_to_output :2296-2633) and write_df
+ * (:920-1230). Given f, every property is formed from it on the host with the reference's
+ * formulas and summation order (physical_props.f90:285-485, 1779-2071), so an f equal to
+ * the reference's gives the same bytes; without f (props only) the device moments are
+ * written and the columns formed from phi (Temp. X/Y/Z, Entropy) are refused. */
+enum { DVM_VIS_NPROP = 27 };  /* property_names(1:27), visualization.f90:314-340        */
+enum { DVM_VIS_DF_1D = 1, DVM_VIS_DF_2D = 2, DVM_VIS_DF_3D = 3 };  /* df_output_dimension */
+typedef struct dvm_vis {
+  char properties_filename[128]; /* properties_vis_filename: <name>.dat (mixture) and
+                                    <name>_1.dat (the species)                            */
+  char df_filename[128];         /* df_vis_filename: <name>_1_<x>_<y>.dat per location    */
+  int32_t enable_properties;     /* enable_properties_vis                                 */
+  int32_t properties_to_output[DVM_VIS_NPROP]; /* write_dens ... write_pressure, in the
+                                    order of property_names                               */
+  int32_t write_stress;          /* stress columns written (0..6)                         */
+  int32_t stress_directions[6];  /* 11, 22, 33, 12, 13 or 23 each                         */
+  int32_t write_moment;          /* moment columns of the species file (0..6)             */
+  int32_t moment_numbers[6];     /* moment_numbers: orders of compute_moment              */
+  int32_t nx_space, ny_space;
+  double dx, dy;                 /* delta_x, delta_y                                      */
+  int32_t end_time;              /* ntstep (zone count of a one-cell run)                 */
+  int32_t properties_dump_freq;  /* properties_vis_dump_freq                              */
+  int32_t enable_vel_df, enable_rot_df, enable_vib_df;
+  int32_t df_dimension;          /* DVM_VIS_DF_*                                          */
+  int32_t num_locations;         /* df output cells (1..16), 1-based like the reference  */
+  int32_t x_locations[16], y_locations[16];
+  int32_t rot_levels, vib_levels;/* num_rot_levels, num_vib_levels (columns of zeros)     */
+  int32_t pi_mode;               /* DVM_PI_* of the Maxwellian in the deviation column    */
+  double mass, omega;            /* molecule mass and viscosity exponent                  */
+  double cZr, cZv;               /* collision numbers of the analytic relaxation columns  */
+  double right_wall_dens;        /* gamma and molecular mass of the Mach column           */
+  double right_wall_temp_rot, right_wall_temp_vib;
+} dvm_vis;
+/* Creates (truncates) the files and writes their title, variables and, for a one-cell run,
+ * zone lines. */
+int dvm_vis_write_headers(const dvm_vis* vis);
+/* Appends one output time: props[cells][DVM_NPROP] and/or f[cells][Nv] (either may be NULL,
+ * not both; grid is needed with f). */
+int dvm_vis_write_properties(const dvm_vis* vis, double time, const double* props,
+                             const double* f, const dvm_vgrid* grid);
+/* Appends one output time of the distribution function at the chosen cells. */
+int dvm_vis_write_df(const dvm_vis* vis, double time, const double* f, const dvm_vgrid* grid);
+/* One Ew.d field as the reference's format statements write it (for checking the format). */
+int dvm_vis_format_e(double x, int w, int d, char* out, int out_len);
 
 /* ---- collisions without device allocation ------------------------------------------ */
 /* No counterpart in the reference. The collision integral of dvm_compute_collision_integral

@@ -612,3 +612,14 @@ def test_full_steps_stretched_grid(gpulib, pkg, oracle, geometry):
         assert rel_err(gpu.phi(), cpu.phi()) <= REL
     assert props_err(gpu.properties(), cpu.properties()) <= 1e-10
     assert gpu.error_word() == 0
+
+
+def test_bkw_relaxation(gpulib, pkg):
+    """Physical known answer on the GPU: the BKW state of a pseudo-Maxwell gas relaxes along
+    the exact BKW solution of the Boltzmann equation (fourth moment within 2e-3 over six
+    collision times; 20^3 grid, 1e5 samples per step)."""
+    from test_oracle_pins import bkw_fourth_moments
+
+    m = bkw_fourth_moments(pkg, pkg.DVMSolver, 20, 100000, 60, 0.1, seed=7)
+    assert np.abs(m[:, 0] / m[:, 1] - 1.0).max() < 2e-3
+    assert m[-1, 0] > m[0, 0]  # towards the Maxwellian's 3.75

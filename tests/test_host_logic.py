@@ -120,25 +120,3 @@ def test_oracle_cavity_conserves_mass_with_diffuse_walls(pkg, oracle):
     for _ in range(4):
         s.compute_convection()
     assert abs(s.phi().sum() - m0) < 1e-12 * m0
-
-
-def test_tecplot_properties_layout(pkg, tmp_path):
-    """The moments file of write_properties: title, variables, one zone per output time
-    with rows time, x, y, properties (cells ordered x outer, y inner)."""
-    path = str(tmp_path / "props.dat")
-    nx, ny = 3, 2
-    props = np.arange(nx * ny * pkg.DVM_NPROP, dtype=float).reshape(nx * ny, pkg.DVM_NPROP)
-    pkg.write_properties_header(path)
-    pkg.append_properties(path, 0.0, props, nx, ny, 0.5, 0.25)
-    pkg.append_properties(path, 0.1, props + 1.0, nx, ny, 0.5, 0.25)
-    lines = open(path).read().splitlines()
-    assert lines[0] == 'title = "Macroscopic Properties"'
-    names = lines[1].split("=", 1)[1].split(",")
-    assert len(names) == 3 + len(pkg.TECPLOT_FIELDS) + len(pkg.TECPLOT_STRESS)
-    assert lines[2].strip() == "zone i=    6" and lines[9].strip() == "zone i=    6"
-    row = [float(v) for v in lines[3].split()]
-    assert row[:3] == [0.0, 0.25, 0.125]  # cell (0, 0)
-    row = [float(v) for v in lines[4].split()]
-    assert row[1:3] == [0.25, 0.375]      # cell (0, 1): y varies fastest
-    assert row[3] == props[0 + nx * 1, pkg.DVM_P_DENS]
-    assert len(row) == len(names)

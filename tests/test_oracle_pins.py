@@ -144,3 +144,46 @@ def test_scatter_count(oracle, pkg):
     cpu.compute_collision_integral(0, pkg.PairList([sub, empty, empty]))
     sc = cpu.scatter_count()
     assert 10 * n <= sc <= 16 * n
+
+
+def bkw_fourth_moments(pkg, solver_cls, n, samples, steps, dtau, seed, threads=None):
+    """A 0-D pseudo-Maxwell gas (csection_method = 2: omega = 1, so g^(2-2 omega) = 1)
+    started from the BKW state at t = 0 (K = 3/5): the fourth moment <|c|^4> after each
+    step, and the analytic BKW one at the same time. The time unit of compute_bkw is the
+    inverse collision frequency; for the reference's collision operator (loss rate
+    sigma/Kn * sum f g^(2-2 omega), variance_reduction.f90:679 with factor_coeff = dt/(2 Kn))
+    that frequency is sigma n / Kn."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(n, -5.0, 5.0)
+    X, Y, Z, _ = g.mesh()
+    c4 = (X * X + Y * Y + Z * Z) ** 2
+    sigma, Kn, dens = 1.0, 1.0, 1.0
+    dt = dtau * Kn / (sigma * dens)
+    cfg = pkg.DVMConfig(iColl=pkg.DVM_COLL_VR, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                        samples_per_step=samples, deltat=dt, Kn=Kn, omega=1.0, alpha=1.0,
+                        sigma=sigma, seed=seed)
+    s = solver_cls(cfg, g) if threads is None else solver_cls(cfg, g, threads=threads)
+    s.initialize_dist_func(ph.bkw(g, dens, 1.0, 0.0))
+    out = []
+    for k in range(1, steps + 1):
+        s.solve(1)
+        f = s.phi()[0]
+        fa = ph.bkw(g, dens, 1.0, k * dtau)
+        out.append(((f * c4).sum() / f.sum(), (fa * c4).sum() / fa.sum()))
+    return np.array(out)
+
+
+def test_bkw_relaxation_restatement(pkg, oracle):
+    """Physical pin of the restatement: the Monte Carlo collision integral relaxes the BKW
+    state along the exact BKW solution (the fourth moment within 3e-3 over six collision
+    times, 16^3 grid, 2e4 samples per step), and not along a solution twice as fast or
+    slow -- the normalisation of the collision operator is the Boltzmann equation's."""
+    m = bkw_fourth_moments(pkg, oracle.OracleSolver, 16, 20000, 60, 0.1, seed=3, threads=4)
+    assert np.abs(m[:, 0] / m[:, 1] - 1.0).max() < 3e-3
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(16, -5.0, 5.0)
+    X, Y, Z, _ = g.mesh()
+    c4 = (X * X + Y * Y + Z * Z) ** 2
+    for scale in (0.5, 2.0):
+        fa = ph.bkw(g, 1.0, 1.0, scale * 3.0)
+        assert abs(m[29, 0] / ((fa * c4).sum() / fa.sum()) - 1.0) > 5e-3

@@ -155,3 +155,38 @@ def test_preemption_off_by_default(gpulib, pkg):
     reqs = _requests(pkg, pkg.DVM_PREC_FP64)[:3]
     res, _ = _serve(pkg, reqs, max_active=1)
     assert all(info["preempted"] == 0 for info, _, _ in res)
+
+
+def test_served_mix_ensemble_accuracy(gpulib, pkg):
+    """The accuracy bar of the served precision form, at matched ensembles: a mix of shock
+    and cavity requests served in FP32 (continuous batching, several in flight) under 8
+    independent seeds, against the same requests run plainly in FP64 under 8 other seeds.
+    After 12 steps the ensemble means of every moment field agree within 1e-3 of the field's
+    scale in every cell."""
+    import dataclasses
+
+    ph = pkg.physics
+    kinds = [lambda prec, seed: _shock(pkg, ph, 24, 14, 2.0, seed, prec),
+             lambda prec, seed: _cavity(pkg, ph, 8, 12, 0.1, seed, prec)]
+    K, steps = 8, 12
+    for make in kinds:
+        reqs = [(make(pkg.DVM_PREC_FP32, 100 + k), steps) for k in range(K)]
+        reqs = [((dataclasses.replace(c, samples_per_step=40000), g, f0), n)
+                for (c, g, f0), n in reqs]
+        res, _ = _serve(pkg, reqs, max_active=4)
+        served = np.array([props[:, :17] for _, props, _ in res])
+        plain = []
+        for k in range(K):
+            c, g, f0 = make(pkg.DVM_PREC_FP64, 500 + k)
+            s = pkg.DVMSolver(dataclasses.replace(c, samples_per_step=40000), g)
+            s.initialize_dist_func(f0)
+            s.solve(steps)
+            plain.append(s.properties()[:, :17])
+            s.close()
+        plain = np.array(plain)
+        m32, m64 = served.mean(0), plain.mean(0)
+        n, T = np.abs(m64[:, 0]).max(), np.abs(m64[:, 4]).max()
+        pr = 0.5 * n * T
+        sc = np.array([n, T ** 0.5, T ** 0.5, T ** 0.5, T, T, T ** 0.5, pr] +
+                      [n * T ** 1.5] * 3 + [pr] * 6)
+        assert (np.abs(m32 - m64).max(0) / sc).max() <= 1e-3

@@ -278,6 +278,32 @@ def moment_error(p_test, p_ref):
                  "qy", "qz", "txx", "tyy", "tzz", "txy", "txz", "tyz"], e)}}
 
 
+ENS_SEEDS = 4  # independent seeds per precision in the ensemble accuracy comparisons
+
+
+def ensemble_error(pkg, make, steps, seeds=ENS_SEEDS):
+    """Accuracy of the precision form as the benchmark spec states it, at matched ensembles:
+    `make(precision, seed)` returns a stepped-ready solver (or batch); after `steps` steps the
+    means over `seeds` independent seeds of each precision are compared per moment field
+    (moment_error), beside the FP64 ensemble's own standard error on the same scale."""
+    ens = {}
+    for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+        runs = []
+        for k in range(seeds):
+            s = make(prec, SEED + 7919 * (k + 1))
+            s.step(steps) if hasattr(s, "upload_f") else s.solve(steps)
+            runs.append(s.properties())
+            s.close()
+        ens[prec] = np.array(runs)
+    m64 = ens[pkg.DVM_PREC_FP64].mean(0)
+    se = ens[pkg.DVM_PREC_FP64].std(0, ddof=1) / np.sqrt(seeds)
+    out = moment_error(ens[pkg.DVM_PREC_FP32].mean(0), m64)
+    out["fp64_ensemble_standard_error_max"] = moment_error(m64 + se, m64)["max"]
+    out["seeds"] = seeds
+    out["steps"] = steps
+    return out
+
+
 def cavity_config(pkg):
     """2-D microcavity: 64 x 64 cells (unit side), 24^3 grid on [-5, 5], hard sphere,
     Kn = 0.1, three diffuse walls at T = 1, lid diffuse at T = 1 moving at u = 0.3,
@@ -303,6 +329,11 @@ def run_forms(pkg, args, fp64_value):
     import dataclasses
     out = {}
     cfg, g, f0 = workload_config(pkg, args.cells)
+
+    def make(prec, seed):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec, seed=seed), g)
+        s.initialize_dist_func(f0)
+        return s
     res = {}
     for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
         s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec), g)
@@ -315,8 +346,7 @@ def run_forms(pkg, args, fp64_value):
         "ms_per_step": res[pkg.DVM_PREC_FP32][1],
         "fp64_value_same_run": res[pkg.DVM_PREC_FP64][0],
         "speedup_vs_fp64": res[pkg.DVM_PREC_FP32][0] / res[pkg.DVM_PREC_FP64][0],
-        "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
-        "steps_compared": args.steps + args.warmup}
+        "moment_err_ensemble_vs_fp64": ensemble_error(pkg, make, 8)}
     out["cavity"] = run_cavity(pkg, args)
     return out
 
@@ -356,6 +386,11 @@ def run_cavity(pkg, args):
         s.close()
     cells = cfg.nx_space * cfg.ny_space
     one_step = one_step_error(pkg, cfg, g, f0)
+
+    def make(prec, seed):
+        s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec, seed=seed), g)
+        s.initialize_dist_func(f0)
+        return s
     return {
         "one_step_moment_err_fp32_vs_fp64": one_step,
         "workload": "2-D microcavity 64x64 cells, 24^3 on [-5,5], hard sphere, Kn=0.1, "
@@ -370,8 +405,7 @@ def run_cavity(pkg, args):
                  "ms_per_step": res[pkg.DVM_PREC_FP64][1],
                  "cell_updates_per_s": cells / (res[pkg.DVM_PREC_FP64][1] * 1e-3),
                  "ms_per_launch": kern[pkg.DVM_PREC_FP64]},
-        "moment_err_vs_fp64": moment_error(res[pkg.DVM_PREC_FP32][2], res[pkg.DVM_PREC_FP64][2]),
-        "steps_compared": args.steps + args.warmup}
+        "moment_err_ensemble_vs_fp64": ensemble_error(pkg, make, 8)}
 
 
 BATCH_GRIDS = (16, 24, 32, 40)
@@ -427,8 +461,13 @@ def run_batch(pkg, args):
                      "wall_collisions_per_s": per_step * args.steps / wall,
                      "instance_updates_per_s": len(gid) * args.steps / wall}
         b.close()
-    out["moment_err_fp32_vs_fp64"] = moment_error(props["fp32_batched"], props["fp64_batched"])
-    out["steps_compared"] = 2 * args.steps + args.warmup
+    def make(prec, seed):
+        b = pkg.DVMBatch(dataclasses.replace(cfg, precision=prec, seed=seed), grids, gid, samples)
+        for i, f in enumerate(f0):
+            b.upload_f(i, f)
+        return b
+    out["moment_err_ensemble_fp32_vs_fp64"] = ensemble_error(pkg, make, 2 * args.steps +
+                                                             args.warmup, seeds=3)
     one = []
     for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
         b = pkg.DVMBatch(dataclasses.replace(cfg, precision=prec), grids, gid, samples)
@@ -438,9 +477,9 @@ def run_batch(pkg, args):
         one.append(b.properties())
         b.close()
     out["one_step_moment_err_fp32_vs_fp64"] = moment_error(one[1], one[0])
-    out["note"] = ("moment_err_fp32_vs_fp64 compares two Monte Carlo realisations after "
-                   "steps_compared steps (they decorrelate); one_step_* isolates the FP32 "
-                   "rounding: one step of each form from the same state and Philox words")
+    out["note"] = ("moment_err_ensemble_* compares ensemble means over independent seeds; "
+                   "one_step_* isolates the FP32 rounding: one step of each form from the "
+                   "same state and Philox words")
     # plain FP64: one context per instance, stepped one after another
     solvers = []
     for i, f in enumerate(f0):
@@ -472,7 +511,7 @@ def run_batch(pkg, args):
     return out
 
 
-SERVE_REQUESTS = 40
+SERVE_REQUESTS = 200
 SERVE_RATE = 50.0        # Poisson arrivals per second
 SERVE_MAX_STEPS = 40
 SERVE_TOL = 1e-6
@@ -481,12 +520,17 @@ SERVE_SLOTS = 6   # concurrent requests (measured: 4.98e9 collisions/s at 6, 4.8
 SERVE_QUANTUM = 8    # steps per graph replay; the residual is checked between replays
                      # (measured: 4.7e9 collisions/s at 8 against 4.5e9 at 2)
 SERVE_PREEMPT = 0    # turns before a request yields its slot to a waiting one (0: never)
+SERVE_ENS = 4        # seeds per precision in the ensemble accuracy comparison
+SERVE_ENS_REQ = 3    # requests of each kind in that comparison
 
 
 def serving_workload(pkg, nreq=SERVE_REQUESTS, seed=SEED):
     """Poisson arrivals (50 req/s) of mixed requests: 60% 1-D shocks (Mach ~U[1.2,4],
     100-400 cells, 24^3-32^3 grids, 2e4 samples per cell-step), 40% 2-D lid-driven cavities
-    (Kn ~logU[0.01,1], 32x32-96x96 cells, 16^3-24^3 grids, 4e3 samples per cell-step).
+    (Kn ~logU[0.01,1], 32x32-96x96 cells, 16^3-24^3 grids, 4e3 x max(1, 0.1/Kn) samples per
+    cell-step: the weight of one sample grows as dt/Kn, and at Kn = 0.015 with 4e3 samples the
+    Monte Carlo noise drives f negative and the state non-finite within 90 steps, so the count
+    grows with 1/Kn as the reference's own formula makes it, compute_num_coll_pairs).
     Returns [(arrival_s, config, grid, f0, kind)] in arrival order."""
     ph = pkg.physics
     rng = np.random.default_rng(seed)
@@ -523,7 +567,8 @@ def serving_workload(pkg, nreq=SERVE_REQUESTS, seed=SEED):
             cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_2D, nx_space=side, ny_space=side,
                                 dx=1.0 / side, dy=1.0 / side, deltat=0.9 / (side * 5.0 * 2.0),
                                 Kn=kn, iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
-                                samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=4000,
+                                samples_mode=pkg.DVM_SAMPLES_FIXED,
+                                samples_per_step=int(round(4000 * max(1.0, 0.1 / kn))),
                                 walls=walls, seed=seed + i)
             kind = "cavity Kn=%.3f %dx%d %d^3" % (kn, side, side, n)
         out.append((t, cfg, g, f0, kind))
@@ -552,35 +597,48 @@ def run_serving(pkg, args):
                 time.sleep(dt)
             ids.append(sv.submit(dataclasses.replace(cfg, precision=pkg.DVM_PREC_FP32), g, f0,
                                  SERVE_MAX_STEPS, SERVE_TOL))
-        for rid in ids:
+        failed = []
+        for rid, req in zip(ids, reqs):
             info = sv.wait(rid)
-            props, _ = sv.result(rid)
-            served.append((info, props))
+            try:
+                props, _ = sv.result(rid)
+            except pkg.DVMError as e:  # reported in the line, kept out of the statistics
+                failed.append({"request": req[4], "error": str(e)})
+                continue
+            served.append((info, props, req))
         t_end = time.perf_counter()
         stats = sv.stats()
     window = t_end - t0
-    colls = sum(i["collisions"] for i, _ in served)
-    cells = sum((c.nx_space * c.ny_space) * i["steps"] for (_, c, _, _, _), (i, _) in
-                zip(reqs, served))
-    lat = [i["latency_ms"] for i, _ in served]
+    colls = sum(i["collisions"] for i, _, _ in served)
+    cells = sum((r[1].nx_space * r[1].ny_space) * i["steps"] for i, _, r in served)
+    lat = [i["latency_ms"] for i, _, _ in served]
     out = {"workload": "%d requests, Poisson %.0f req/s: 60%% 1-D shocks (Mach U[1.2,4], "
                        "100-400 cells, 24^3-32^3, 2e4 samples/cell-step), 40%% 2-D cavities "
-                       "(Kn logU[0.01,1], 32^2-96^2 cells, 16^3-24^3, 4e3 samples/cell-step); "
+                       "(Kn logU[0.01,1], 32^2-96^2 cells, 16^3-24^3, 4e3 x max(1, 0.1/Kn) "
+                       "samples/cell-step); "
                        "each to residual %g or %d steps" % (len(reqs), SERVE_RATE, SERVE_TOL,
                                                             SERVE_MAX_STEPS),
            "served_fp32": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
                            "collisions_per_s": colls / window,
                            "cell_updates_per_s": cells / window,
                            "requests_per_s": len(reqs) / window,
-                           "converged": sum(i["converged"] for i, _ in served),
+                           "converged": sum(i["converged"] for i, _, _ in served),
+                           "failed": failed,
                            "peak_active": stats["peak_active"],
                            "peak_bytes": stats["peak_bytes"], "budget_bytes": SERVE_BUDGET,
-                           "statuses": sorted(set(i["status"] for i, _ in served))}}
-    # plain FP64: one solve at a time, per-step residual check
-    finish, lat_p, colls_p, cells_p, err, plain_props = 0.0, [], 0, 0, [], []
-    first = reqs[0][0]
-    for (t, cfg, g, f0, _), (info, props32) in zip(reqs, served):
-        ts = time.perf_counter()
+                           "statuses": sorted(set(i["status"] for i, _, _ in served))}}
+    out["served_fp32"]["final_residual"] = {
+        "median": _pct([i["residual"] for i, _, _ in served], 50),
+        "max": max(i["residual"] for i, _, _ in served)}
+    # plain FP64 under the same arrival clock: one solve at a time in arrival order, each
+    # started when it has arrived and the previous one has finished; latency = finish -
+    # arrival on the wall clock
+    lat_p, colls_p, cells_p, resid_p, failed_p = [], 0, 0, [], 0
+    t0 = time.perf_counter()
+    for t, cfg, g, f0, _ in reqs:
+        wait = t0 + t - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
         s = pkg.DVMSolver(cfg, g)
         s.initialize_dist_func(f0)
         steps = 0
@@ -590,37 +648,52 @@ def run_serving(pkg, args):
             colls_p += s.collision_count()
             if s.residual() <= SERVE_TOL:
                 break
-        props64 = s.properties()
-        plain_props.append(props64)
+        resid_p.append(s.residual())
+        failed_p += int(s.error_word() != 0)
         s.close()
-        service = time.perf_counter() - ts
-        finish = max(finish, t) + service
-        lat_p.append((finish - t) * 1e3)
+        lat_p.append((time.perf_counter() - (t0 + t)) * 1e3)
         cells_p += cfg.nx_space * cfg.ny_space * steps
-        err.append(moment_error(props32, props64))
-    # the yardstick for the served-vs-plain difference: plain FP64 against itself with
-    # other seeds (two independent realisations of each request)
-    spread = []
-    for (t, cfg, g, f0, _), (info, _) in zip(reqs, served):
-        s = pkg.DVMSolver(dataclasses.replace(cfg, seed=cfg.seed + 7919), g)
-        s.initialize_dist_func(f0)
-        s.solve(info["steps"])
-        spread.append(moment_error(s.properties(), plain_props[len(spread)]))
-        s.close()
-    span = finish - min(first, 0.0)
+    span = time.perf_counter() - t0
     out["plain_fp64"] = {"p50_ms": _pct(lat_p, 50), "p99_ms": _pct(lat_p, 99),
                          "collisions_per_s": colls_p / span, "cell_updates_per_s": cells_p / span,
-                         "requests_per_s": len(reqs) / span}
-    fields = err[0]["per_field"].keys()
-    out["moment_err_served_fp32_vs_plain_fp64"] = {
-        "max": max(e["max"] for e in err),
-        "per_field": {k: max(e["per_field"][k] for e in err) for k in fields}}
-    out["moment_err_plain_fp64_seed_to_seed"] = {
-        "max": max(e["max"] for e in spread),
-        "per_field": {k: max(e["per_field"][k] for e in spread) for k in fields}}
-    out["note"] = ("served FP32 and plain FP64 runs of a request are two Monte Carlo "
-                   "realisations; their difference is compared with the FP64 seed-to-seed "
-                   "difference of the same requests")
+                         "requests_per_s": len(reqs) / span,
+                         "converged": sum(1 for r in resid_p if r <= SERVE_TOL),
+                         "failed": failed_p,
+                         "final_residual": {"median": _pct(resid_p, 50), "max": max(resid_p)}}
+    # accuracy at matched ensembles: the precision form the server runs (a request's result
+    # depends only on its parameters, seed and steps) against FP64, SERVE_ENS seeds each, on
+    # the first requests of each kind; errors are of the ensemble means, with the FP64
+    # ensemble's own standard error beside them
+    subset = ([r for r in reqs if r[4].startswith("shock")][:SERVE_ENS_REQ] +
+              [r for r in reqs if r[4].startswith("cavity")][:SERVE_ENS_REQ])
+    errs, ses = [], []
+    for t, cfg, g, f0, _ in subset:
+        ens = {}
+        for prec in (pkg.DVM_PREC_FP64, pkg.DVM_PREC_FP32):
+            runs = []
+            for k in range(SERVE_ENS):
+                s = pkg.DVMSolver(dataclasses.replace(cfg, precision=prec,
+                                                      seed=cfg.seed + 7919 * (k + 1)), g)
+                s.initialize_dist_func(f0)
+                s.solve(SERVE_MAX_STEPS)
+                runs.append(s.properties())
+                s.close()
+            ens[prec] = np.array(runs)
+        m64 = ens[pkg.DVM_PREC_FP64].mean(0)
+        errs.append(moment_error(ens[pkg.DVM_PREC_FP32].mean(0), m64))
+        se = ens[pkg.DVM_PREC_FP64].std(0, ddof=1) / np.sqrt(SERVE_ENS)
+        ses.append(moment_error(m64 + se, m64))
+    fields = errs[0]["per_field"].keys()
+    out["moment_err_ensemble_fp32_vs_fp64"] = {
+        "max": max(e["max"] for e in errs),
+        "per_field": {k: max(e["per_field"][k] for e in errs) for k in fields},
+        "fp64_ensemble_standard_error_max": max(e["max"] for e in ses),
+        "requests": len(subset), "seeds": SERVE_ENS, "steps": SERVE_MAX_STEPS}
+    out["note"] = ("each request runs to the residual or the step cap; the per-step residual "
+                   "of a Monte Carlo step settles at the noise of the collision integral "
+                   "(final_residual), far above 1e-6 at these sample counts. Accuracy is "
+                   "compared between ensemble means of the precision form and of FP64 over "
+                   "independent seeds, with the FP64 ensemble's standard error beside it")
     out["speedup_collisions"] = (out["served_fp32"]["collisions_per_s"] /
                                  out["plain_fp64"]["collisions_per_s"])
     out["speedup_cell_updates"] = (out["served_fp32"]["cell_updates_per_s"] /

@@ -368,6 +368,14 @@ class DVMBatch:
                "dvm_batch_time_steps")
         return ms.value, n.value
 
+    def launch_shape(self):
+        """The autotuned shape: CDF threads per CTA, collision CTAs per SM, launches per step."""
+        t, b, n = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.dvm_batch_launch_shape(self.b, C.byref(t), C.byref(b), C.byref(n)),
+               "dvm_batch_launch_shape")
+        return {"cdf_threads": t.value, "collide_ctas_per_sm": b.value,
+                "launches_per_step": n.value}
+
 
 def footprint_bytes(config, grid, lib=None):
     """Device bytes a context for (config, grid) allocates (dvm_footprint_bytes)."""

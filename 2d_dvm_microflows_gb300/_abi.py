@@ -143,6 +143,8 @@ ENTRY_POINTS = {
     "dvm_batch_get_properties": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "dvm_batch_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double),
                                        C.POINTER(C.c_int64)]),
+    "dvm_batch_launch_shape": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]),
     "dvm_footprint_bytes": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid),
                                       C.POINTER(C.c_uint64)]),
     "dvm_server_create": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(_P)]),

@@ -1004,6 +1004,11 @@ struct dvm_batch {
   uint32_t* d_step = nullptr;
   bool props_stale = true;
   int64_t collisions_per_step = 0;
+  // launch shape of the grouped kernels, chosen by the autotuner
+  int cdf_threads = 256;
+  int collide_bps = 0;   // persistent collide CTAs per SM (0: not tuned yet)
+  std::vector<double> group_cost;  // collide time of each group alone (ms): the CTA shares
+  std::vector<double> tune_log;  // (cdf threads | collide CTAs/SM, ms) pairs, in tuning order
 };
 
 namespace {
@@ -1018,54 +1023,210 @@ void batch_release(dvm_batch* b) {
   delete b;
 }
 
-// Launch-shape autotuner: for each group, time the persistent collision kernel at 1..4
-// CTAs per SM (bounded by occupancy) on a saved copy of the state, keep the fastest, and
-// restore the state.
-int autotune(dvm_batch* b) {
-  for (dvm_ctx* c : b->groups) {
-    const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
-    // 0-D contexts never use f_conv: it holds the saved f
-    int st = cuda_status(cudaMemcpyAsync(c->d_fconv, c->d_f, bytes, cudaMemcpyDeviceToDevice,
-                                         c->stream));
-    std::vector<double> cache(static_cast<size_t>(c->ncells) * kEqCache);
-    if (!st && c->d_eq_cache)
-      st = cuda_status(cudaMemcpyAsync(cache.data(), c->d_eq_cache, cache.size() * sizeof(double),
-                                       cudaMemcpyDeviceToHost, c->stream));
-    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
-    if (st) return st;
-    const bool fp32 = (c->p.precision == DVM_PREC_FP32);
-    const int max_bps = fp32 ? collide_f32_blocks_per_sm(c->g, c->tabs)
-                             : collide_blocks_per_sm(collide_smem_bytes(c->g, c->tabs));
-    int best = c->num_sms * max_bps;
-    float best_ms = 1e30f;
-    for (int bps = 1; bps <= std::min(4, max_bps); ++bps) {
-      const int grid = c->num_sms * bps;
-      if (fp32) c->collide_f32_grid = grid; else c->collide_grid = grid;
-      cudaEvent_t e0 = take_event(c), e1 = take_event(c);
-      float ms = 0.f;
-      for (int rep = 0; rep < 2; ++rep) {  // first pass warms up
-        cudaMemcpyAsync(c->d_f, c->d_fconv, bytes, cudaMemcpyDeviceToDevice, c->stream);
-        cudaEventRecord(e0, c->stream);
-        st = dvm_compute_collision_integral(c, 0, nullptr);
-        cudaEventRecord(e1, c->stream);
-        if (st) return st;
-        cudaEventSynchronize(e1);
-        cudaEventElapsedTime(&ms, e0, e1);
-      }
-      c->ev_pool.push_back(e0);
-      c->ev_pool.push_back(e1);
-      if (ms < best_ms) { best_ms = ms; best = grid; }
+// CTAs of a persistent launch dealt to the groups in proportion to their samples per step,
+// at least one each: first[g] is group g's first CTA.
+void partition_ctas(int total, const std::vector<double>& work, int* first) {
+  const int ng = static_cast<int>(work.size());
+  double W = 0.0;
+  for (double w : work) W += w;
+  total = std::max(total, ng);
+  std::vector<int> n(ng, 1);
+  int used = ng;
+  std::vector<std::pair<double, int>> rem;
+  for (int g = 0; g < ng; ++g) {
+    const double share = W > 0.0 ? work[g] / W * total : static_cast<double>(total) / ng;
+    const int extra = std::max(0, static_cast<int>(share) - 1);
+    n[g] += extra;
+    used += extra;
+    rem.push_back({share - static_cast<double>(n[g]), g});
+  }
+  std::sort(rem.begin(), rem.end(), [](const std::pair<double, int>& x,
+                                       const std::pair<double, int>& y) {
+    return x.first > y.first || (x.first == y.first && x.second < y.second);
+  });
+  for (size_t k = 0; used < total && k < rem.size(); ++k, ++used) ++n[rem[k].second];
+  first[0] = 0;
+  for (int g = 0; g < ng; ++g) first[g + 1] = first[g] + n[g];
+}
+
+// The grouped launch records of groups [g0, g0 + ng) of a batch.
+struct GroupedStep {
+  GroupedCdf cdf;
+  GroupedPlan plan;
+  GroupedCollide col;
+  GroupedProject proj;
+  GroupedMoments mom;
+  bool fp32;
+};
+
+void grouped_records(const dvm_batch* b, int g0, int ng, int bps, GroupedStep& gs) {
+  std::memset(&gs, 0, sizeof(gs));
+  gs.cdf.ngroups = gs.plan.ngroups = gs.col.ngroups = gs.proj.ngroups = gs.mom.ngroups = ng;
+  gs.fp32 = (b->groups[g0]->p.precision == DVM_PREC_FP32);
+  std::vector<double> work(ng);
+  int cells = 0;
+  for (int k = 0; k < ng; ++k) {
+    const dvm_ctx* c = b->groups[g0 + k];
+    gs.cdf.first[k] = gs.proj.first[k] = gs.mom.first[k] = cells;
+    cells += c->ncells;
+    CdfArgs& ca = gs.cdf.a[k];
+    ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
+    ca.f = c->d_f; ca.props = c->d_props; ca.eq_cache = c->d_eq_cache;
+    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
+    ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan; ca.err = c->d_err;
+    gs.plan.ncells[k] = c->ncells;
+    gs.plan.plan[k] = c->d_plan;
+    gs.plan.chunk_off[k] = c->d_chunk_off;
+    gs.plan.total[k] = c->d_total_samples;
+    CollideArgs a{};
+    a.g = c->g; a.cp = coll_params(c); a.t = c->tabs; a.ncells = c->ncells;
+    a.step_dev = c->step_dev;
+    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
+    a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
+    a.chunk_off = c->d_chunk_off; a.err = c->d_err;
+    gs.col.a[k] = collide_consts(a);
+    gs.col.tf[k] = c->tabs_f;
+    gs.col.df[k] = c->d_df;
+    gs.proj.a[k] = ProjectArgs{c->g, c->ncells, c->d_f, c->d_df, c->d_props};
+    gs.mom.a[k] = MomentArgs{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, nullptr};
+    work[k] = b->group_cost.size() == b->groups.size()
+                  ? b->group_cost[g0 + k]
+                  : static_cast<double>(c->ncells) * static_cast<double>(c->p.samples_per_step);
+  }
+  gs.cdf.first[ng] = gs.proj.first[ng] = gs.mom.first[ng] = cells;
+  partition_ctas(b->groups[g0]->num_sms * bps, work, gs.col.first);
+}
+
+// CTAs per SM the grouped collide launch of groups [g0, g0 + ng) can hold.
+int grouped_max_bps(const dvm_batch* b, int g0, int ng) {
+  GroupedStep gs;
+  grouped_records(b, g0, ng, 1, gs);
+  return std::min(4, collide_grouped_blocks_per_sm(gs.col, gs.fp32));
+}
+
+// One step of every instance: per block of up to kMaxGroups grids, one launch each of the
+// CDF build, the plan, the persistent collision kernel (the precision form adds the
+// projection) and the moments.
+int batch_issue(dvm_batch* b, bool cdf = true, bool plan = true, bool collide = true,
+                bool moments = true) {
+  const int G = static_cast<int>(b->groups.size());
+  for (int g0 = 0; g0 < G; g0 += kMaxGroups) {
+    const int ng = std::min(kMaxGroups, G - g0);
+    const int bps = std::min(b->collide_bps > 0 ? b->collide_bps : 4, grouped_max_bps(b, g0, ng));
+    GroupedStep gs;
+    grouped_records(b, g0, ng, bps, gs);
+    int st = DVM_OK;
+    if (cdf) st = cuda_status(launch_cdf_grouped(gs.cdf, b->cdf_threads, b->stream));
+    if (!st && plan) st = cuda_status(launch_plan_grouped(gs.plan, b->stream));
+    if (!st && collide) {
+      st = cuda_status(launch_collide_grouped(gs.col, gs.fp32, b->stream));
+      if (!st && gs.fp32) st = cuda_status(launch_project_grouped(gs.proj, b->stream));
     }
-    if (fp32) c->collide_f32_grid = best; else c->collide_grid = best;
-    st = cuda_status(cudaMemcpyAsync(c->d_f, c->d_fconv, bytes, cudaMemcpyDeviceToDevice,
-                                     c->stream));
-    if (!st && c->d_eq_cache)
-      st = cuda_status(cudaMemcpyAsync(c->d_eq_cache, cache.data(), cache.size() * sizeof(double),
-                                       cudaMemcpyHostToDevice, c->stream));
-    if (!st) st = cuda_status(cudaStreamSynchronize(c->stream));
+    if (!st && moments) st = cuda_status(launch_moments_grouped(gs.mom, b->stream));
     if (st) return st;
   }
   return DVM_OK;
+}
+
+// Launch-shape autotuner for the grouped step: the CDF CTA width (256, 512, 1024 threads)
+// and the persistent collide CTAs per SM (1..4, bounded by occupancy), each timed on the
+// batch's own state, which is saved first (f into f_conv, unused by 0-D contexts; the
+// equilibrium caches to the host) and restored afterwards.
+int autotune(dvm_batch* b) {
+  b->tune_log.clear();
+  std::vector<std::vector<double>> caches(b->groups.size());
+  int st = DVM_OK;
+  for (size_t k = 0; k < b->groups.size() && !st; ++k) {
+    dvm_ctx* c = b->groups[k];
+    const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+    st = cuda_status(cudaMemcpyAsync(c->d_fconv, c->d_f, bytes, cudaMemcpyDeviceToDevice,
+                                     b->stream));
+    caches[k].resize(static_cast<size_t>(c->ncells) * kEqCache);
+    if (!st && c->d_eq_cache)
+      st = cuda_status(cudaMemcpyAsync(caches[k].data(), c->d_eq_cache,
+                                       caches[k].size() * sizeof(double),
+                                       cudaMemcpyDeviceToHost, b->stream));
+  }
+  if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
+  if (st) return st;
+  auto restore_f = [&]() {
+    for (dvm_ctx* c : b->groups) {
+      const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+      cudaMemcpyAsync(c->d_f, c->d_fconv, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    }
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto timed = [&](bool cdf, bool collide, float& ms) -> int {
+    for (int rep = 0; rep < 2; ++rep) {  // the first pass warms up
+      if (collide) restore_f();
+      cudaEventRecord(e0, b->stream);
+      const int s2 = batch_issue(b, cdf, false, collide, false);
+      cudaEventRecord(e1, b->stream);
+      if (s2) return s2;
+      const int s3 = cuda_status(cudaEventSynchronize(e1));
+      if (s3) return s3;
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    return DVM_OK;
+  };
+  float best = 1e30f, ms = 0.f;
+  int best_t = 256;
+  for (int t : {256, 512, 1024}) {
+    b->cdf_threads = t;
+    st = timed(true, false, ms);
+    if (st) break;
+    b->tune_log.push_back(t);
+    b->tune_log.push_back(ms);
+    if (ms < best) { best = ms; best_t = t; }
+  }
+  b->cdf_threads = best_t;
+  if (!st) st = batch_issue(b, true, true, false, false);  // the plan the collide walks
+  // each group's collide alone on the whole GPU: its time sets the group's share of CTAs
+  b->group_cost.clear();
+  for (size_t g = 0; g < b->groups.size() && !st; ++g) {
+    GroupedStep gs;
+    grouped_records(b, static_cast<int>(g), 1, grouped_max_bps(b, static_cast<int>(g), 1), gs);
+    for (int rep = 0; rep < 2 && !st; ++rep) {
+      restore_f();
+      cudaEventRecord(e0, b->stream);
+      st = cuda_status(launch_collide_grouped(gs.col, gs.fp32, b->stream));
+      cudaEventRecord(e1, b->stream);
+      if (!st) st = cuda_status(cudaEventSynchronize(e1));
+      if (!st) cudaEventElapsedTime(&ms, e0, e1);
+    }
+    b->group_cost.push_back(std::max(static_cast<double>(ms), 1e-6));
+  }
+  if (st) b->group_cost.clear();
+  int max_bps = 4;
+  for (size_t g0 = 0; g0 < b->groups.size(); g0 += kMaxGroups)
+    max_bps = std::min(max_bps, grouped_max_bps(b, static_cast<int>(g0),
+                                                std::min<int>(kMaxGroups, b->groups.size() - g0)));
+  best = 1e30f;
+  int best_b = max_bps;
+  for (int bps = 1; bps <= max_bps && !st; ++bps) {
+    b->collide_bps = bps;
+    st = timed(false, true, ms);
+    if (st) break;
+    b->tune_log.push_back(bps);
+    b->tune_log.push_back(ms);
+    if (ms < best) { best = ms; best_b = bps; }
+  }
+  b->collide_bps = best_b;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  restore_f();
+  for (size_t k = 0; k < b->groups.size() && !st; ++k) {
+    dvm_ctx* c = b->groups[k];
+    if (c->d_eq_cache)
+      st = cuda_status(cudaMemcpyAsync(c->d_eq_cache, caches[k].data(),
+                                       caches[k].size() * sizeof(double),
+                                       cudaMemcpyHostToDevice, b->stream));
+  }
+  if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
+  return st;
 }
 
 int batch_prepare(dvm_batch* b) {
@@ -1085,11 +1246,7 @@ int batch_prepare(dvm_batch* b) {
   cudaGraph_t graph = nullptr;
   st = cuda_status(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
   if (st) return st;
-  for (dvm_ctx* c : b->groups) {
-    st = dvm_compute_collision_integral(c, 0, nullptr);
-    if (!st) st = dvm_calculate_physical_properties(c);
-    if (st) break;
-  }
+  st = batch_issue(b);
   if (!st) st = cuda_status(launch_step_end(b->d_step, nullptr, nullptr, b->stream));
   const int st2 = cuda_status(cudaStreamEndCapture(b->stream, &graph));
   if (st || st2) {
@@ -1253,6 +1410,19 @@ int dvm_batch_get_properties(dvm_batch* b, double* props) {
                                 DVM_NPROP * sizeof(double), cudaMemcpyDeviceToHost));
     if (st) return st;
   }
+  return DVM_OK;
+}
+
+int dvm_batch_launch_shape(dvm_batch* b, int* cdf_threads, int* collide_ctas_per_sm,
+                           int* launches_per_step) {
+  if (!b || !cdf_threads || !collide_ctas_per_sm || !launches_per_step) return DVM_ERR_PARAM;
+  const bool tuned = b->exec != nullptr;
+  const int blocks = (static_cast<int>(b->groups.size()) + kMaxGroups - 1) / kMaxGroups;
+  const bool fp32 = !b->groups.empty() && b->groups[0]->p.precision == DVM_PREC_FP32;
+  *cdf_threads = tuned ? b->cdf_threads : 0;
+  *collide_ctas_per_sm = tuned ? b->collide_bps : 0;
+  // per block of grids: CDF, plan, collide (+ projection), moments; then the step counter
+  *launches_per_step = tuned ? blocks * (fp32 ? 5 : 4) + 1 : 0;
   return DVM_OK;
 }
 

@@ -195,6 +195,45 @@ struct MomentArgs {
   unsigned long long* residual;
 };
 
+// Grouped launches: the instances of a batch on up to kMaxGroups velocity grids advance in
+// one launch of each kernel. Each group keeps its own arguments; a CTA finds its group from
+// its index (groups own consecutive CTAs) and runs that group's code path.
+constexpr int kMaxGroups = 8;
+
+struct GroupedCdf {
+  int ngroups;
+  int first[kMaxGroups + 1];   // first CTA (= instance) of each group; first[ngroups] = grid
+  CdfArgs a[kMaxGroups];
+};
+
+struct GroupedPlan {  // one CTA per group
+  int ngroups;
+  int ncells[kMaxGroups];
+  const CellPlan* plan[kMaxGroups];
+  long long* chunk_off[kMaxGroups];
+  long long* total[kMaxGroups];
+};
+
+struct GroupedCollide {  // persistent: group g owns CTAs first[g] .. first[g+1] - 1
+  int ngroups;
+  int first[kMaxGroups + 1];
+  CollideArgs a[kMaxGroups];
+  CollTablesF tf[kMaxGroups];  // precision form
+  float* df[kMaxGroups];
+};
+
+struct GroupedProject {
+  int ngroups;
+  int first[kMaxGroups + 1];
+  ProjectArgs a[kMaxGroups];
+};
+
+struct GroupedMoments {
+  int ngroups;
+  int first[kMaxGroups + 1];
+  MomentArgs a[kMaxGroups];
+};
+
 // Launch wrappers (dvm_kernels.cu). Each returns the cudaGetLastError of its launch.
 cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s);
 cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
@@ -218,6 +257,17 @@ cudaError_t launch_atomic_probe(double* buf, size_t n, int blocks, int per_threa
                                 cudaStream_t s);
 int collide_blocks_per_sm(size_t smem);
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t);
+
+// Grouped launches (batches). cdf_threads: 256, 512 or 1024 threads per CDF CTA.
+cudaError_t launch_cdf_grouped(const GroupedCdf& m, int cdf_threads, cudaStream_t s);
+cudaError_t launch_plan_grouped(const GroupedPlan& m, cudaStream_t s);
+// m.a[g] carry the FP32 grid constants (collide_consts); the grid is m.first[m.ngroups]
+cudaError_t launch_collide_grouped(const GroupedCollide& m, bool fp32, cudaStream_t s);
+cudaError_t launch_project_grouped(const GroupedProject& m, cudaStream_t s);
+cudaError_t launch_moments_grouped(const GroupedMoments& m, cudaStream_t s);
+// CTAs per SM of the grouped collide launch (the largest group's shared memory decides)
+int collide_grouped_blocks_per_sm(const GroupedCollide& m, bool fp32);
+CollideArgs collide_consts(const CollideArgs& a);
 
 }  // namespace dvm
 

@@ -179,7 +179,7 @@ __device__ __forceinline__ void block_scan2_i64(long long& a, long long& b, long
 // T threads per CTA (256, or 512 / 1024 for launches of few cells: the per-cell scan then
 // walks fewer, wider chunks).
 template <int T>
-__global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
+__device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
   constexpr int kCdfThreads = T;
   constexpr int kCdfChunk = T * kCdfPer;  // nodes per scan chunk
   __shared__ long long s_scan[2][128];
@@ -196,7 +196,6 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
   long long* tr_d = tr_e + 32 * kCdfPitch;
   float* tr_k = reinterpret_cast<float*>(tr_d + 32 * kCdfPitch);
   const GridInfo& g = a.g;
-  const int cell = blockIdx.x;
   const int nv = g.nv;
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
   const double* f = a.f + static_cast<size_t>(cell) * nv;
@@ -517,6 +516,11 @@ __global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
 }
 
 template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_cdf(CdfArgs a) {
+  cdf_cta<T>(a, blockIdx.x);
+}
+
+template <int T>
 static cudaError_t launch_cdf_t(const CdfArgs& a, cudaStream_t s) {
   constexpr int smem = (T / 32) * kCdfTrWarp * static_cast<int>(sizeof(long long));
   const cudaError_t e = cudaFuncSetAttribute(k_cdf<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -536,8 +540,8 @@ cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
 
 // ----------------------------------------------------------------------------------------
 // k_plan: chunk offsets of every (cell, sub-integral) for the persistent collide kernel.
-__global__ void __launch_bounds__(1024) k_plan(int ncells, const CellPlan* plan,
-                                               long long* chunk_off, long long* total_samples) {
+__device__ __forceinline__ void plan_cta(int ncells, const CellPlan* plan, long long* chunk_off,
+                                         long long* total_samples) {
   __shared__ long long s_w[32];
   __shared__ long long s_carry, s_samples;
   const int n = 3 * ncells;
@@ -580,6 +584,11 @@ __global__ void __launch_bounds__(1024) k_plan(int ncells, const CellPlan* plan,
     __syncthreads();
   }
   if (threadIdx.x == 0) { chunk_off[n] = s_carry; *total_samples = s_samples; }
+}
+
+__global__ void __launch_bounds__(1024) k_plan(int ncells, const CellPlan* plan,
+                                               long long* chunk_off, long long* total_samples) {
+  plan_cta(ncells, plan, chunk_off, total_samples);
 }
 
 cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
@@ -938,7 +947,8 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   return L;
 }
 
-__global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
+// One CTA of the persistent collide launch: CTA bid of the nblk that walk this grid's chunks.
+__device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
   const CollideSmem L = collide_smem_layout(g, a.t);
@@ -1012,8 +1022,8 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   // 0..total-1), so the warps in flight at any moment work on many cells and their FP64
   // atomics spread over many f slabs instead of piling onto the busiest nodes of one cell
   const int wpb = blockDim.x >> 5;
-  const long long pos0 = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
-  const long long stride = static_cast<long long>(gridDim.x) * wpb;
+  const long long pos0 = static_cast<long long>(bid) * wpb + (threadIdx.x >> 5);
+  const long long stride = static_cast<long long>(nblk) * wpb;
   ChunkWalk walk(pos0, stride, total);
   for (long long pos = pos0; pos < total; pos += stride) {
     const long long chunk = walk.next(total);
@@ -1191,6 +1201,10 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   add_scatter_count(a.scatter_count, nat);
 }
 
+__global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
+  collide_cta(a, blockIdx.x, gridDim.x);
+}
+
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
   return collide_smem_layout(g, t).total;
 }
@@ -1220,6 +1234,8 @@ static CollideArgs with_collide_consts(const CollideArgs& a) {
   b.rnxy = 1.f / static_cast<float>(a.g.nx * a.g.ny);
   return b;
 }
+
+CollideArgs collide_consts(const CollideArgs& a) { return with_collide_consts(a); }
 
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s) {
   const size_t smem = collide_smem_bytes(a.g, a.t);
@@ -1623,8 +1639,9 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   }
 }
 
-__global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a, CollTablesF tf,
-                                                                float* __restrict__ dfs) {
+// One CTA of the persistent FP32 collide launch (as collide_cta).
+__device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const CollTablesF& tf,
+                                                float* __restrict__ dfs, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const F32Ctx c = load_f32_tables(a, tf, s_raw);
   __syncthreads();
@@ -1634,8 +1651,8 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   uint32_t bad = 0;
   uint32_t nat = 0;  // FP32 adds into df by this thread
   const int wpb = blockDim.x >> 5;
-  const long long pos0 = static_cast<long long>(blockIdx.x) * wpb + (threadIdx.x >> 5);
-  const long long stride = static_cast<long long>(gridDim.x) * wpb;
+  const long long pos0 = static_cast<long long>(bid) * wpb + (threadIdx.x >> 5);
+  const long long stride = static_cast<long long>(nblk) * wpb;
   ChunkWalk walk(pos0, stride, total);
   for (long long pos = pos0; pos < total; pos += stride) {
     const long long chunk = walk.next(total);
@@ -1653,6 +1670,11 @@ __global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a,
   }
   if (bad) atomicOr(a.err, bad);
   add_scatter_count(a.scatter_count, nat);
+}
+
+__global__ void __launch_bounds__(kCollideChunk, 4) k_collide_f32(CollideArgs a, CollTablesF tf,
+                                                                float* __restrict__ dfs) {
+  collide_f32_cta(a, tf, dfs, blockIdx.x, gridDim.x);
 }
 
 int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
@@ -2616,4 +2638,145 @@ cudaError_t launch_flush(double* buf, size_t n, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ----------------------------------------------------------------------------------------
+// Grouped launches: one launch of each kernel advances every instance of a batch, whatever
+// its velocity grid. Groups own consecutive CTAs; a CTA looks its group up in the launch
+// parameters (first[g] <= blockIdx.x < first[g+1]) and runs that group's code path with
+// the group's own arguments, so the instances of all grids share the SMs in one launch.
+__device__ __forceinline__ int group_of(const int* first, int ngroups, int x) {
+  int gi = 0;
+  while (gi + 1 < ngroups && x >= first[gi + 1]) ++gi;
+  return gi;
+}
+
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) k_cdf_grouped(const __grid_constant__ GroupedCdf m) {
+  const int gi = group_of(m.first, m.ngroups, static_cast<int>(blockIdx.x));
+  cdf_cta<T>(m.a[gi], static_cast<int>(blockIdx.x) - m.first[gi]);
+}
+
+template <int T>
+static cudaError_t launch_cdf_grouped_t(const GroupedCdf& m, cudaStream_t s) {
+  constexpr int smem = (T / 32) * kCdfTrWarp * static_cast<int>(sizeof(long long));
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_cdf_grouped<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_cdf_grouped<T><<<m.first[m.ngroups], T, smem, s>>>(m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cdf_grouped(const GroupedCdf& m, int cdf_threads, cudaStream_t s) {
+  if (m.ngroups < 1 || m.ngroups > kMaxGroups || m.first[m.ngroups] < 1) return cudaErrorInvalidValue;
+  if (cdf_threads >= 1024) return launch_cdf_grouped_t<1024>(m, s);
+  if (cdf_threads >= 512) return launch_cdf_grouped_t<512>(m, s);
+  return launch_cdf_grouped_t<256>(m, s);
+}
+
+__global__ void __launch_bounds__(1024) k_plan_grouped(const __grid_constant__ GroupedPlan m) {
+  const int gi = static_cast<int>(blockIdx.x);
+  plan_cta(m.ncells[gi], m.plan[gi], m.chunk_off[gi], m.total[gi]);
+}
+
+cudaError_t launch_plan_grouped(const GroupedPlan& m, cudaStream_t s) {
+  if (m.ngroups < 1 || m.ngroups > kMaxGroups) return cudaErrorInvalidValue;
+  k_plan_grouped<<<m.ngroups, 1024, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+// Groups own consecutive CTAs (first[g] <= blockIdx.x < first[g+1]). Three CTAs per SM:
+// the per-group arguments are read by index and need the registers that 80 per thread
+// leave (at 64 the FP64 kernel spills three times as much and runs 25 % slower).
+__global__ void __launch_bounds__(kCollideChunk, 3) k_collide_grouped(const __grid_constant__ GroupedCollide m) {
+  const int b = static_cast<int>(blockIdx.x);
+  const int gi = group_of(m.first, m.ngroups, b);
+  collide_cta(m.a[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+}
+
+__global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32_grouped(const __grid_constant__ GroupedCollide m) {
+  const int b = static_cast<int>(blockIdx.x);
+  const int gi = group_of(m.first, m.ngroups, b);
+  collide_f32_cta(m.a[gi], m.tf[gi], m.df[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+}
+
+static size_t collide_grouped_smem(const GroupedCollide& m, bool fp32) {
+  size_t smem = 0;
+  for (int gi = 0; gi < m.ngroups; ++gi) {
+    const size_t b = fp32 ? collide_f32_smem_layout(m.a[gi].g, m.a[gi].t, m.tf[gi].gtab_smem).total
+                          : collide_smem_bytes(m.a[gi].g, m.a[gi].t);
+    smem = b > smem ? b : smem;
+  }
+  return smem;
+}
+
+int collide_grouped_blocks_per_sm(const GroupedCollide& m, bool fp32) {
+  const size_t smem = collide_grouped_smem(m, fp32);
+  const void* fn = fp32 ? reinterpret_cast<const void*>(k_collide_f32_grouped)
+                        : reinterpret_cast<const void*>(k_collide_grouped);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kCollideChunk, smem) != cudaSuccess)
+    n = 1;
+  cudaGetLastError();
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_collide_grouped(const GroupedCollide& m, bool fp32, cudaStream_t s) {
+  if (m.ngroups < 1 || m.ngroups > kMaxGroups) return cudaErrorInvalidValue;
+  if (m.first[0] != 0) return cudaErrorInvalidValue;
+  for (int gi = 0; gi < m.ngroups; ++gi)
+    if (m.first[gi + 1] <= m.first[gi]) return cudaErrorInvalidValue;  // every group owns a CTA
+  const size_t smem = collide_grouped_smem(m, fp32);
+  const void* fn = fp32 ? reinterpret_cast<const void*>(k_collide_f32_grouped)
+                        : reinterpret_cast<const void*>(k_collide_grouped);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned grid = static_cast<unsigned>(m.first[m.ngroups]);
+  if (fp32) k_collide_f32_grouped<<<grid, kCollideChunk, smem, s>>>(m);
+  else k_collide_grouped<<<grid, kCollideChunk, smem, s>>>(m);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(kProjThreads, 3) k_project_grouped(const __grid_constant__ GroupedProject m) {
+  const int gi = group_of(m.first, m.ngroups, static_cast<int>(blockIdx.x));
+  const ProjectArgs& a = m.a[gi];
+  const int cell = static_cast<int>(blockIdx.x) - m.first[gi];
+  const size_t off = static_cast<size_t>(cell) * a.g.nv;
+  project_cell(a.g, a.df + off, true, a.f + off, a.props + static_cast<size_t>(cell) * DVM_NPROP);
+}
+
+cudaError_t launch_project_grouped(const GroupedProject& m, cudaStream_t s) {
+  if (m.ngroups < 1 || m.ngroups > kMaxGroups || m.first[m.ngroups] < 1) return cudaErrorInvalidValue;
+  int threads = 32;
+  for (int gi = 0; gi < m.ngroups; ++gi) {
+    const int t = column_threads(m.a[gi].g, kProjThreads);
+    threads = t > threads ? t : threads;
+  }
+  k_project_grouped<<<m.first[m.ngroups], threads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(kMomThreads, 3) k_moments_grouped(const __grid_constant__ GroupedMoments m) {
+  const int gi = group_of(m.first, m.ngroups, static_cast<int>(blockIdx.x));
+  const MomentArgs& a = m.a[gi];
+  const int cell = static_cast<int>(blockIdx.x) - m.first[gi];
+  MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
+  moments_of_cell<false>(a, cell, src);
+}
+
+cudaError_t launch_moments_grouped(const GroupedMoments& m, cudaStream_t s) {
+  if (m.ngroups < 1 || m.ngroups > kMaxGroups || m.first[m.ngroups] < 1) return cudaErrorInvalidValue;
+  int threads = 32;
+  for (int gi = 0; gi < m.ngroups; ++gi) {
+    const int t = column_threads(m.a[gi].g, kMomThreads);
+    threads = t > threads ? t : threads;
+  }
+  k_moments_grouped<<<m.first[m.ngroups], threads, 0, s>>>(m);
+  return cudaGetLastError();
+}
+
 }  // namespace dvm
+

@@ -459,8 +459,10 @@ def run_batch(pkg, args):
         out[name] = {"value": colls / (ms_dev * 1e-3), "unit": "collisions/s",
                      "ms_per_step": ms_dev / args.steps,
                      "wall_collisions_per_s": per_step * args.steps / wall,
-                     "instance_updates_per_s": len(gid) * args.steps / wall}
+                     "instance_updates_per_s": len(gid) * args.steps / wall,
+                     "launch_shape": b.launch_shape()}
         b.close()
+
     def make(prec, seed):
         b = pkg.DVMBatch(dataclasses.replace(cfg, precision=prec, seed=seed), grids, gid, samples)
         for i, f in enumerate(f0):
@@ -506,8 +508,9 @@ def run_batch(pkg, args):
         s.close()
     out["speedup_fp32_batched_vs_fp64_plain"] = (out["fp32_batched"]["wall_collisions_per_s"] /
                                                  out["fp64_plain"]["value"])
-    out["timing"] = ("batched value: CUDA events around graph replays; wall_*: host clock "
-                     "around the same replays; fp64_plain: host clock; working set > L2")
+    out["timing"] = ("batched value: CUDA events around graph replays (one grouped launch of "
+                     "each kernel per step, launch_shape); wall_*: host clock around the same "
+                     "replays; fp64_plain: host clock; working set > L2")
     return out
 
 

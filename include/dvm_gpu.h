@@ -216,12 +216,15 @@ int dvm_checkpoint_load(dvm_ctx* ctx, const void* buf, uint64_t bytes, uint64_t*
 /* ---- batched homogeneous instances --------------------------------------------------- */
 /* Many independent 0-D relaxations (the reference's homogeneous case, nx_space = ny_space =
  * 1, run for many initial states and grids at once). No reference counterpart. Instances on
- * the same velocity grid form one group (one context whose cells are the instances); every
- * group shares one stream, and one step of all groups is captured into a single CUDA graph
- * on the first dvm_batch_step and replayed after. The persistent collision launch of each
- * group is sized by a timing autotuner at that point. params gives the common settings
- * (collision method, dt, Kn, species, precision, seed); samples_per_grid[g] is the fixed
- * sample count per instance-step on grid g. */
+ * the same velocity grid form one group (one context whose cells are the instances). One
+ * step of every instance is one launch each of the CDF build, the sample plan, the
+ * persistent collision kernel (the precision form adds the projection) and the moments, over
+ * all groups at once (up to 8 grids per launch; each CTA runs its own group's grid), and that
+ * step is captured into a single CUDA graph on the first dvm_batch_step and replayed after.
+ * A timing autotuner picks the CDF CTA width and the collision kernel's CTAs per SM at that
+ * point; the collision CTAs are dealt to the groups in proportion to their samples.
+ * params gives the common settings (collision method, dt, Kn, species, precision, seed);
+ * samples_per_grid[g] is the fixed sample count per instance-step on grid g. */
 typedef struct dvm_batch dvm_batch;
 int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrids,
                      const int32_t* instance_grid, int ninstances,
@@ -235,6 +238,10 @@ int dvm_batch_step(dvm_batch* b, int nsteps);
 int dvm_batch_get_properties(dvm_batch* b, double* props);
 /* Device time of nsteps graph replays (ms) and the samples they drew. */
 int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisions);
+/* The launch shape the autotuner chose (after the first step; 0 before it): threads per CDF
+ * CTA and collision CTAs per SM; launches per step of the graph. */
+int dvm_batch_launch_shape(dvm_batch* b, int* cdf_threads, int* collide_ctas_per_sm,
+                           int* launches_per_step);
 
 /* ---- request server ------------------------------------------------------------------ */
 /* Device bytes a context for (params, vgrid) allocates; the server admits by this figure.

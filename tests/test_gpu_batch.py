@@ -122,3 +122,81 @@ def test_batch_rejects_bad_instances(gpulib, pkg):
     ptr = f.ctypes.data_as(pkg._abi.C.POINTER(pkg._abi.C.c_double))
     assert b.lib.dvm_batch_upload_f(b.b, 2, ptr) == pkg.DVM_ERR_PARAM
     assert b.lib.dvm_batch_step(b.b, -1) == pkg.DVM_ERR_PARAM
+
+
+def test_batch_one_launch_per_kernel_over_grids(gpulib, pkg):
+    """Instances on ten velocity grids (more than one grouped launch holds) step exactly as
+    plain multi-cell contexts of each grid's instances do, with one launch of each kernel per
+    block of up to eight grids: CDF, plan, collide and moments, then the step counter."""
+    ph = pkg.physics
+    sizes = list(range(6, 16))
+    grids = [ph.VelocityGrid.uniform(n, -4.5, 4.5) for n in sizes]
+    samples = [3000 + 500 * q for q in range(len(grids))]
+    rng = np.random.default_rng(3)
+    gid = np.concatenate([np.arange(len(grids)), rng.integers(0, len(grids), 8)]).astype(np.int32)
+    f0 = []
+    for i in range(len(gid)):
+        g = grids[gid[i]]
+        u = rng.uniform(0.0, 1.0)
+        f0.append(0.5 * ph.maxwellian(g, 1.0, u, 0.0, 0.0, 1.0) +
+                  0.5 * ph.maxwellian(g, 1.0, -u, 0.0, 0.0, 2.0))
+    batch = pkg.DVMBatch(_cfg(pkg, pkg.DVM_PREC_FP64), grids, gid, samples)
+    for i, f in enumerate(f0):
+        batch.upload_f(i, f)
+    batch.step(2)
+    shape = batch.launch_shape()
+    assert shape["launches_per_step"] == 2 * 4 + 1, shape
+    assert shape["cdf_threads"] in (256, 512, 1024) and 1 <= shape["collide_ctas_per_sm"] <= 4
+    pb = batch.properties()
+    for q, g in enumerate(grids):
+        members = np.flatnonzero(gid == q)
+        cfg = _cfg(pkg, pkg.DVM_PREC_FP64)
+        cfg.nx_space = len(members)
+        cfg.samples_mode = pkg.DVM_SAMPLES_FIXED
+        cfg.samples_per_step = samples[q]
+        s = pkg.DVMSolver(cfg, g)
+        s.initialize_dist_func(np.stack([f0[i] for i in members]))
+        s.solve(2)
+        ps, fs = s.properties(), s.phi()
+        s.close()
+        for c, i in enumerate(members):
+            fb = batch.download_f(i)
+            assert np.abs(fb - fs[c]).max() <= 1e-12 * np.abs(fs[c]).max(), (q, i)
+            assert np.abs(pb[i, :17] - ps[c, :17]).max() <= 1e-11 * max(1.0, np.abs(ps[c]).max())
+    batch.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_batch_configuration4_grids_single_grouped_launch(gpulib, pkg, prec):
+    """The four grids of configuration 4 (16^3, 24^3, 32^3, 40^3: the two largest read their
+    velocity table through L1, the others stage it in shared memory) advance in one grouped
+    launch of each kernel; FP64 equals the per-grid contexts to 1e-12 after two steps."""
+    ph = pkg.physics
+    prec = pkg.DVM_PREC_FP64 if prec == "fp64" else pkg.DVM_PREC_FP32
+    grids = [ph.VelocityGrid.uniform(n, -5.0, 5.0) for n in (16, 24, 32, 40)]
+    samples = [int(2e4 * (n / 24.0) ** 3) for n in (16, 24, 32, 40)]
+    gid, f0 = _instances(ph, grids, 10, 4)
+    batch = pkg.DVMBatch(_cfg(pkg, prec), grids, gid, samples)
+    for i, f in enumerate(f0):
+        batch.upload_f(i, f)
+    nsteps = 2 if prec == pkg.DVM_PREC_FP64 else 1
+    batch.step(nsteps)
+    assert batch.launch_shape()["launches_per_step"] == (4 if prec == pkg.DVM_PREC_FP64 else 5) + 1
+    for q, g in enumerate(grids):
+        members = np.flatnonzero(gid == q)
+        if len(members) == 0:
+            continue
+        cfg = _cfg(pkg, prec)
+        cfg.nx_space = len(members)
+        cfg.samples_mode = pkg.DVM_SAMPLES_FIXED
+        cfg.samples_per_step = samples[q]
+        s = pkg.DVMSolver(cfg, g)
+        s.initialize_dist_func(np.stack([f0[i] for i in members]))
+        s.solve(nsteps)
+        fs = s.phi()
+        s.close()
+        ftol = 1e-12 if prec == pkg.DVM_PREC_FP64 else 1e-5
+        for c, i in enumerate(members):
+            fb = batch.download_f(i)
+            assert np.abs(fb - fs[c]).max() <= ftol * np.abs(fs[c]).max(), (q, i)
+    batch.close()

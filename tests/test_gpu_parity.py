@@ -89,6 +89,44 @@ def test_moments_cluster_split(gpulib, pkg, oracle, ncells):
     assert gpu.error_word() == 0
 
 
+@pytest.mark.parametrize("grid", [("uniform", 24), ("uniform", 33), ("stretched", 14)])
+def test_moments_independent_of_previous_properties(gpulib, pkg, oracle, grid):
+    """The moments are summed about the previous step's velocity (for accuracy) but must not
+    depend on it or on the rest of the stored properties: with near-zero and negative node
+    values in the mix, the first call (no previous properties), the next, and calls after the
+    stored density was set 1e-9 and 100 times its value all match the restatement."""
+    ph = pkg.physics
+    kind, n = grid
+    if kind == "uniform":
+        g = ph.VelocityGrid.uniform(n, -6.0, 6.0)
+    else:
+        g = ph.VelocityGrid(_stretched_axis(n, 5.0), _stretched_axis(n + 1, 5.0, 1.3),
+                            _stretched_axis(n + 2, 5.5, 1.4))
+    rng = np.random.default_rng(n)
+    f0 = np.stack([ph.bimodal(g, u1=0.6 + 0.3 * c, T2=1.5 + c) * (1 + 0.02 * rng.random(g.nv))
+                   for c in range(5)])
+    f0[2] *= -0.01 * rng.random(g.nv) + 1.0  # a little of everything: some nodes near zero
+    f0[3, :: 7] *= -1e-3                     # and some negative values
+    gpu, cpu = pair_solvers(pkg, oracle, g, f0, nx_space=5, iColl=pkg.DVM_COLL_NONE)
+    pc = cpu.properties()
+    sc = prop_scales(pc)
+
+    def check(pg):
+        for q in range(17):
+            assert np.abs(pg[:, q] - pc[:, q]).max() <= 1e-12 * sc[q], pkg.PROP_NAMES[q]
+
+    check(gpu.properties())
+    gpu.calculate_physical_properties()
+    check(gpu.properties())
+    for factor in (1e-9, 100.0):
+        p = gpu.properties().copy()
+        p[:, 0] *= factor
+        gpu.set_properties(p)
+        gpu.calculate_physical_properties()
+        check(gpu.properties())
+    assert gpu.error_word() == 0
+
+
 @pytest.mark.parametrize("nodes", [True, False])
 @pytest.mark.parametrize("grid_n", [8, 12, 24])
 def test_vr_pairlist_step(gpulib, pkg, oracle, nodes, grid_n):

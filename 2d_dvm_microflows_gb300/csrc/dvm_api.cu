@@ -681,7 +681,9 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
   }
   if (!st)
     st = launch(c, DVM_K_PLAN, [&] {
-      return launch_plan(c->ncells, c->d_plan, c->d_chunk_off, c->d_total_samples, c->stream);
+      const int grid = (c->p.precision == DVM_PREC_FP32) ? c->collide_f32_grid : c->collide_grid;
+      return launch_plan(c->ncells, c->d_plan, c->d_chunk_off, c->d_total_samples,
+                         static_cast<long long>(grid) * (kCollideChunk / 32), c->stream);
     });
   if (!st) {
     CollideArgs a{};
@@ -1095,6 +1097,9 @@ void grouped_records(const dvm_batch* b, int g0, int ng, int bps, GroupedStep& g
   }
   gs.cdf.first[ng] = gs.proj.first[ng] = gs.mom.first[ng] = cells;
   partition_ctas(b->groups[g0]->num_sms * bps, work, gs.col.first);
+  for (int k = 0; k < ng; ++k)
+    gs.plan.warps[k] = static_cast<long long>(gs.col.first[k + 1] - gs.col.first[k]) *
+                       (kCollideChunk / 32);
 }
 
 // CTAs per SM the grouped collide launch of groups [g0, g0 + ng) can hold.

@@ -9,6 +9,19 @@ namespace dvm {
 
 constexpr int kCollideChunk = 256;  // threads per collide CTA
 constexpr int kChunkSamples = 32;   // samples per chunk of one (cell, sub-integral): a warp
+// A warp takes a run of consecutive chunks of one (cell, sub-integral) per visit: the runs
+// are visited in a scattered order and a warp walks its run's chunks in turn, one lookup of
+// the run's (cell, sub-integral) per run. Measured on the benchmark shock at fixed run
+// lengths of 1, 2, 4, 8, 16, 32, 64 chunks: FP64 collide 5.44, 5.46, 5.45, 5.34, 5.25,
+// 5.32, 5.58 ms; FP32 3.58, 3.58, 3.40, 3.33, 3.28, 3.31, 3.47 ms. Launches with few
+// samples per warp need short runs (the cavity's FP32 collide went from 0.28 to 0.35 ms at
+// 16), so k_plan picks the length per launch: as many chunks as leave each warp of the
+// collide launch about kRunsPerWarp runs, between 1 and kRunChunks. It is stored in the top
+// bits of the last chunk offset (chunk_off[3C] = runs | length << kRunShift).
+constexpr int kRunChunks = 16;
+constexpr long long kRunsPerWarp = 16;
+constexpr int kRunShift = 56;
+constexpr long long kRunMask = (1ll << kRunShift) - 1;
 
 // Samples and depletion factor of each sub-integral of one cell-step
 // (variance_reduction.f90:669-683, 822-835, 967-981; full_mc.f90:330-331).
@@ -136,7 +149,7 @@ struct CollideArgs {
   const int2* ref_eq;
   const int2* ref_dev;
   const CellPlan* plan;
-  const long long* chunk_off;  // [3*C + 1]
+  const long long* chunk_off;  // [3*C + 1]: run offsets; [3C] = runs | run length << kRunShift
   PairDev pairs;
   uint32_t* err;
   unsigned long long* scatter_count;  // if set, the adds into f (df) are counted here
@@ -209,6 +222,7 @@ struct GroupedCdf {
 struct GroupedPlan {  // one CTA per group
   int ngroups;
   int ncells[kMaxGroups];
+  long long warps[kMaxGroups];  // warps of the group's share of the collide launch
   const CellPlan* plan[kMaxGroups];
   long long* chunk_off[kMaxGroups];
   long long* total[kMaxGroups];
@@ -236,8 +250,9 @@ struct GroupedMoments {
 
 // Launch wrappers (dvm_kernels.cu). Each returns the cudaGetLastError of its launch.
 cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s);
+// warps: the warps of the collide launch that walks this plan (sets the run length)
 cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
-                        long long* total_samples, cudaStream_t s);
+                        long long* total_samples, long long warps, cudaStream_t s);
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s);
 cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, float* df, int grid,
                                cudaStream_t s);

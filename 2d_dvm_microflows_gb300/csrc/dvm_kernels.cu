@@ -541,18 +541,32 @@ cudaError_t launch_cdf(const CdfArgs& a, cudaStream_t s) {
 // ----------------------------------------------------------------------------------------
 // k_plan: chunk offsets of every (cell, sub-integral) for the persistent collide kernel.
 __device__ __forceinline__ void plan_cta(int ncells, const CellPlan* plan, long long* chunk_off,
-                                         long long* total_samples) {
+                                         long long* total_samples, long long warps) {
   __shared__ long long s_w[32];
-  __shared__ long long s_carry, s_samples;
+  __shared__ long long s_carry, s_samples, s_chunks;
   const int n = 3 * ncells;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) { s_carry = 0; s_samples = 0; }
+  if (threadIdx.x == 0) { s_carry = 0; s_samples = 0; s_chunks = 0; }
   __syncthreads();
+  // the run length: as many chunks per run as leave every warp of the collide launch about
+  // kRunsPerWarp runs (at least 1 chunk, at most kRunChunks)
+  {
+    long long c = 0;
+    for (int e = threadIdx.x; e < n; e += blockDim.x)
+      c += (plan[e / 3].num[e % 3] + kChunkSamples - 1) / kChunkSamples;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0 && c > 0)
+      atomicAdd(reinterpret_cast<unsigned long long*>(&s_chunks), static_cast<unsigned long long>(c));
+  }
+  __syncthreads();
+  const long long want = (warps > 0 ? warps : 1) * kRunsPerWarp;
+  const long long runlen = max(1ll, min(static_cast<long long>(kRunChunks), s_chunks / want));
   for (int base = 0; base < n; base += 1024) {
     const int e = base + threadIdx.x;
     long long num = 0;
     if (e < n) num = plan[e / 3].num[e % 3];
-    long long ch = (num + kChunkSamples - 1) / kChunkSamples;
+    long long ch = (num + kChunkSamples * runlen - 1) / (kChunkSamples * runlen);
     long long v = ch;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -583,17 +597,21 @@ __device__ __forceinline__ void plan_cta(int ncells, const CellPlan* plan, long 
     if (threadIdx.x == 0) s_carry += s_w[31];
     __syncthreads();
   }
-  if (threadIdx.x == 0) { chunk_off[n] = s_carry; *total_samples = s_samples; }
+  if (threadIdx.x == 0) {
+    chunk_off[n] = s_carry | (runlen << kRunShift);
+    *total_samples = s_samples;
+  }
 }
 
 __global__ void __launch_bounds__(1024) k_plan(int ncells, const CellPlan* plan,
-                                               long long* chunk_off, long long* total_samples) {
-  plan_cta(ncells, plan, chunk_off, total_samples);
+                                               long long* chunk_off, long long* total_samples,
+                                               long long warps) {
+  plan_cta(ncells, plan, chunk_off, total_samples, warps);
 }
 
 cudaError_t launch_plan(int ncells, const CellPlan* plan, long long* chunk_off,
-                        long long* total_samples, cudaStream_t s) {
-  k_plan<<<1, 1024, 0, s>>>(ncells, plan, chunk_off, total_samples);
+                        long long* total_samples, long long warps, cudaStream_t s) {
+  k_plan<<<1, 1024, 0, s>>>(ncells, plan, chunk_off, total_samples, warps);
   return cudaGetLastError();
 }
 
@@ -1007,7 +1025,8 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
 
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const int nent = 3 * a.ncells;
-  const long long total = a.chunk_off[nent];
+  const long long total = a.chunk_off[nent] & kRunMask;
+  const int runlen = static_cast<int>(a.chunk_off[nent] >> kRunShift);
   const bool vr = (a.cp.method == DVM_COLL_VR);
   const int NR = a.cp.num_repl;
   const double vhs = 2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega));
@@ -1034,11 +1053,15 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     }
     const int cell = lo / 3, q = lo - 3 * (lo / 3);
     const CellPlan& pl = a.plan[cell];
-    const long long i = (chunk - a.chunk_off[lo]) * kChunkSamples + (threadIdx.x & 31);
-    if (i >= pl.num[q]) continue;
     const double factor = pl.factor[q];
     const size_t cs = static_cast<size_t>(cell) * (nv + 1);
     double* f = a.f + static_cast<size_t>(cell) * nv;
+    // the run's chunks of 32 samples, one after another
+    const long long i0 =
+        (chunk - a.chunk_off[lo]) * (kChunkSamples * runlen) + (threadIdx.x & 31);
+    for (int rr = 0; rr < runlen; ++rr) {
+    const long long i = i0 + rr * kChunkSamples;
+    if (i >= pl.num[q]) break;
 
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
     unsigned long long mA = 0, mB = 0;
@@ -1196,6 +1219,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
     }
+    }  // the run's chunks
   }
   if (bad) atomicOr(a.err, bad);
   add_scatter_count(a.scatter_count, nat);
@@ -1647,7 +1671,8 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
   __syncthreads();
   const int nv = a.g.nv;
   const int nent = 3 * a.ncells;
-  const long long total = a.chunk_off[nent];
+  const long long total = a.chunk_off[nent] & kRunMask;
+  const int runlen = static_cast<int>(a.chunk_off[nent] >> kRunShift);
   uint32_t bad = 0;
   uint32_t nat = 0;  // FP32 adds into df by this thread
   const int wpb = blockDim.x >> 5;
@@ -1663,10 +1688,14 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
     }
     const int cell = lo / 3, q = lo - 3 * (lo / 3);
     const CellPlan& pl = a.plan[cell];
-    const long long i = (chunk - a.chunk_off[lo]) * kChunkSamples + (threadIdx.x & 31);
-    if (i >= pl.num[q]) continue;
-    collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
-                       dfs + static_cast<size_t>(cell) * nv, bad, nat);
+    const long long i0 =
+        (chunk - a.chunk_off[lo]) * (kChunkSamples * runlen) + (threadIdx.x & 31);
+    for (int rr = 0; rr < runlen; ++rr) {
+      const long long i = i0 + rr * kChunkSamples;
+      if (i >= pl.num[q]) break;
+      collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
+                         dfs + static_cast<size_t>(cell) * nv, bad, nat);
+    }
   }
   if (bad) atomicOr(a.err, bad);
   add_scatter_count(a.scatter_count, nat);
@@ -2674,7 +2703,7 @@ cudaError_t launch_cdf_grouped(const GroupedCdf& m, int cdf_threads, cudaStream_
 
 __global__ void __launch_bounds__(1024) k_plan_grouped(const __grid_constant__ GroupedPlan m) {
   const int gi = static_cast<int>(blockIdx.x);
-  plan_cta(m.ncells[gi], m.plan[gi], m.chunk_off[gi], m.total[gi]);
+  plan_cta(m.ncells[gi], m.plan[gi], m.chunk_off[gi], m.total[gi], m.warps[gi]);
 }
 
 cudaError_t launch_plan_grouped(const GroupedPlan& m, cudaStream_t s) {

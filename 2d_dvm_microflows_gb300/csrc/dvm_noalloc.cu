@@ -289,7 +289,11 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   if ((e = launch_cdf(ca, s)) != cudaSuccess) return status_of(e);
   long long* d_chunk = reinterpret_cast<long long*>(base + L.chunk_off);
   long long* d_total = reinterpret_cast<long long*>(base + L.total);
-  if ((e = launch_plan(ncells, ca.plan, d_chunk, d_total, s)) != cudaSuccess) return status_of(e);
+  // (the collide launch below has up to 4 CTAs per SM)
+  if ((e = launch_plan(ncells, ca.plan, d_chunk, d_total,
+                       static_cast<long long>(grid_blocks) * 4 * (kCollideChunk / 32), s)) !=
+      cudaSuccess)
+    return status_of(e);
 
   CollideArgs a{};
   a.g = g; a.cp = cp; a.ncells = ncells; a.step = static_cast<uint32_t>(step);

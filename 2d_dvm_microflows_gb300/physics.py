@@ -11,6 +11,7 @@ import numpy as np
 
 PI_REFERENCE = 3.1459265358979323  # utils/constants.f90:30 (sic)
 PI_EXACT = math.pi
+KB_REFERENCE = 1.3805e-23           # utils/constants.f90:31, Boltzmann's constant [J/K]
 
 
 def pi_value(pi_mode):
@@ -115,6 +116,23 @@ def molecule(species="Ar", csection_method=CSECTION_HS, ref_species=None):
         alpha = 1.0
     return dict(mass=s["mass"] / ref["mass"], diam=s["diam"] / ref["diam"],
                 omega=omega, alpha=alpha)
+
+
+def reference_values(dens, temp, species="Ar", Kn=1.0, pi_mode=0):
+    """The dimensional reference values of a run (set_scaling_parameters,
+    solver/scaling.f90:118-148, and the derived ones of write_reference_values_to_file
+    :203-237): reference speed sqrt(2 kb T/m), cross-section pi d^2, length 1/(Kn n sigma),
+    time L/c, pressure 2 kb n T, heat flux m c^3, energy m c^2 (SI units), for the reference
+    species' single-precision mass and diameter."""
+    s = SPECIES[species]
+    m, d = s["mass"], s["diam"]
+    c = math.sqrt(2.0 * KB_REFERENCE * temp / m)
+    sigma = pi_value(pi_mode) * d * d
+    L = 1.0 / (Kn * dens * sigma)
+    return {"Mass": m, "Diameter": d, "Cross-section": sigma, "Density": dens,
+            "Temperature": temp, "Speed": c, "Pressure": 2.0 * KB_REFERENCE * dens * temp,
+            "Heat Flux": m * c * c * c, "Energy": m * c * c, "Flow Knudsen number": Kn,
+            "Characteristic length scale": L, "Time scale": L / c}
 
 
 def cross_section(mol, csection_coeff=CSECTION_BIRD, pi_mode=0, viscosity=None,

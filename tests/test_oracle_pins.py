@@ -187,3 +187,45 @@ def test_bkw_relaxation_restatement(pkg, oracle):
     for scale in (0.5, 2.0):
         fa = ph.bkw(g, 1.0, 1.0, scale * 3.0)
         assert abs(m[29, 0] / ((fa * c4).sum() / fa.sum()) - 1.0) > 5e-3
+
+
+def _reference_pins():
+    import json
+    return json.load(open(os.path.join(HERE, "golden", "reference_pins.json")))
+
+
+def test_reference_values_file(pkg):
+    """The reference's own reference_values.txt (trunk/bin; written by
+    write_reference_values_to_file, solver/scaling.f90:203-237, for argon at 1e20 m^-3,
+    273 K, Kn 1.091): every value agrees to the 9 significant digits the file prints. This
+    pins the constants kb and the reference's pi (3.14592...), the single-precision argon
+    constants and the scaling formulas."""
+    want = _reference_pins()["reference_values"]
+    got = pkg.physics.reference_values(want["Density"], want["Temperature"], "Ar",
+                                       Kn=want["Flow Knudsen number"])
+    for k, v in want.items():
+        assert abs(got[k] - v) <= 6e-9 * abs(v), (k, got[k], v)
+
+
+def test_normal_shock_against_shock_calculator(pkg):
+    """The reference's shock calculator output (software/shock_calculator/
+    normal_shock_parameters.txt: 3 % Xe / 97 % He, stationary shock, Mach 3.9, upstream at
+    the reference temperature): the end states of the Rankine-Hugoniot relations used for
+    the shock initial state agree to the 10 decimals the file prints. The calculator's
+    specific-heat ratio comes from the last species' c_p alone (its mixture sum assigns
+    rather than adds, normal_shock.f90:88), gamma = 0.97 (5/2) / (0.97 (5/2) - 1); the
+    mixture mass in reference units is 0.03 + 0.97 m_He/m_Xe."""
+    s = _reference_pins()["normal_shock"]
+    x_he = s["He fraction"]
+    cp = x_he * 2.5
+    gamma = cp / (cp - 1.0)
+    assert abs(gamma - s["Specific heat ratio"]) <= 5e-6
+    mass = s["Xe fraction"] + x_he * s["He mass ratio"]
+    up, dn = pkg.physics.normal_shock(s["Mach"], gamma=gamma, T_up=s["T_up"], n_up=s["n_up"],
+                                      mass=mass)
+    assert abs(dn["n"] - s["n_down"]) <= 1e-9
+    assert abs(dn["T"] - s["T_down"]) <= 1e-9
+    assert abs(abs(up["u"]) - s["u_up"]) <= 1e-9
+    assert abs(abs(dn["u"]) - s["u_down"]) <= 1e-9
+    p_ratio = dn["n"] * dn["T"] / (up["n"] * up["T"])
+    assert abs(p_ratio - s["Pressure ratio (P2/P1)"]) <= 1e-9

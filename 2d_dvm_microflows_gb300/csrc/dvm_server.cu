@@ -3,12 +3,16 @@
 // Continuous batching: queued requests are admitted in arrival order whenever the sum of
 // the admitted requests' device footprints stays within the budget and a slot is free;
 // every admitted request keeps its f, CDFs and moments resident in its own context on its
-// own stream and advances in turns of a few steps, each turn one replay of a CUDA graph
-// captured for that request. The turns of different requests run on different streams, so
-// their kernels overlap on the device. After every turn the request's convergence residual
-// comes back by an asynchronous 8-byte copy to pinned memory, polled with an event; the
-// request is retired once the residual reaches its tolerance or its step limit is reached,
-// its memory going back to the stream-ordered pool. Three host threads share the work so
+// own stream and advances in turns of up to steps_per_turn steps, each turn one launch of a
+// CUDA graph captured for that request. The graph is a device-side loop: a conditional
+// while node whose body is one step (two where convection swaps f and f_conv) followed by
+// a one-thread kernel that reads the step's convergence residual and continues the loop
+// only while the residual is above the request's tolerance and the turn has steps left, so
+// a request stops on the device at the step that converged. The turns of different
+// requests run on different streams, so their kernels overlap on the device. After every
+// turn the residual and the device step counter come back by asynchronous copies to pinned
+// memory, polled with an event; the request is retired once the residual reaches its
+// tolerance or its step limit is reached, its memory going back to the stream-ordered pool. Three host threads share the work so
 // that the one issuing turns never waits on the others: a preparer admits requests (context,
 // upload, graph capture), the worker polls and issues turns, a retirer downloads results and
 // releases contexts. A request's result depends only on its own parameters,
@@ -61,12 +65,13 @@ struct Request {
   cudaStream_t stream = nullptr;
   uint32_t* d_step = nullptr;
   long long* d_acc = nullptr;
+  int* d_left = nullptr;    // steps the current turn may still take (the graph's loop)
   cudaGraphExec_t exec = nullptr;
   int quantum = 0;
+  int body = 1;             // steps per pass of the graph's loop
   cudaEvent_t ev = nullptr;
   int slot = -1;
   bool inflight = false;
-  int steps_issued = 0;
   int steps_done = 0;
   bool eager_tail = false;  // an odd last step was issued outside the graph
   int turns = 0;            // turns completed since the last admission
@@ -119,6 +124,8 @@ struct dvm_server {
   int live = 0;               // requests holding a slot (admission to retirement or parking)
   std::thread worker, preparer, retirer;
   double* h_slots = nullptr;  // pinned, one residual per slot
+  uint32_t* h_steps = nullptr;  // pinned, the device step counter per slot
+  int* h_left = nullptr;        // pinned, the turn length per slot (copied to d_left)
   std::vector<int> free_slots;
   uint64_t used = 0;
   // every thread ends once destruction was asked for and no request is left
@@ -142,15 +149,49 @@ int eager_step(Request& r) {
   return st;
 }
 
-int capture_quantum(Request& r) {
+// The loop's test after each pass: the turn's remaining steps go down by the pass, and the
+// loop goes on while a whole pass still fits and the residual of the last step is above
+// the tolerance (a NaN residual stops it too).
+__global__ void k_turn_check(cudaGraphConditionalHandle h, const unsigned long long* residual,
+                             double tol, int* left, int body) {
+  const int l = *left - body;
+  *left = l;
+  const double res = __longlong_as_double(static_cast<long long>(*residual));
+  cudaGraphSetConditional(h, (l >= body && res > tol) ? 1u : 0u);
+}
+
+// A turn as one graph: a conditional while node (its handle set to 1 at every launch)
+// whose body, captured from the request's own stream, is r.body steps and the check.
+int capture_turn(Request& r) {
   cudaGraph_t graph = nullptr;
-  int st = cuda_st(cudaStreamBeginCapture(r.stream, cudaStreamCaptureModeRelaxed));
+  int st = cuda_st(cudaGraphCreate(&graph, 0));
   if (st) return st;
-  for (int s = 0; s < r.quantum && !st; ++s) st = eager_step(r);
-  const int st2 = cuda_st(cudaStreamEndCapture(r.stream, &graph));
-  if (!st) st = st2;
+  cudaGraphConditionalHandle h;
+  st = cuda_st(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (!st) st = cuda_st(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np));
+  if (!st) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    st = cuda_st(cudaStreamBeginCaptureToGraph(r.stream, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeRelaxed));
+    if (!st) {
+      for (int s = 0; s < r.body && !st; ++s) st = eager_step(r);
+      if (!st) {
+        k_turn_check<<<1, 1, 0, r.stream>>>(h, dvm::ctx_residual(r.ctx), r.tol, r.d_left, r.body);
+        st = cuda_st(cudaGetLastError());
+      }
+      cudaGraph_t out = nullptr;
+      const int st2 = cuda_st(cudaStreamEndCapture(r.stream, &out));
+      if (!st) st = st2;
+    }
+  }
   if (!st) st = cuda_st(cudaGraphInstantiate(&r.exec, graph, 0));
-  if (graph) cudaGraphDestroy(graph);
+  cudaGraphDestroy(graph);
   return st;
 }
 
@@ -163,6 +204,8 @@ int admit(dvm_server* sv, Request& r) {
   st = cuda_st(cudaMallocAsync(reinterpret_cast<void**>(&r.d_step), sizeof(uint32_t), r.stream));
   if (!st)
     st = cuda_st(cudaMallocAsync(reinterpret_cast<void**>(&r.d_acc), sizeof(long long), r.stream));
+  if (!st)
+    st = cuda_st(cudaMallocAsync(reinterpret_cast<void**>(&r.d_left), sizeof(int), r.stream));
   if (st) return st;
   cudaMemsetAsync(r.d_step, 0, sizeof(uint32_t), r.stream);
   cudaMemsetAsync(r.d_acc, 0, sizeof(long long), r.stream);
@@ -189,37 +232,39 @@ int admit(dvm_server* sv, Request& r) {
     std::vector<double>().swap(r.f0);
   }
   r.turns = 0;
-  // an even number of steps per graph when convection swaps f and f_conv
-  r.quantum = sv->quantum;
-  if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) ++r.quantum;
-  r.quantum = std::min(r.quantum, std::max(1, r.max_steps - r.steps_done));
-  if (r.p.conv_method != DVM_CONV_NONE && (r.quantum & 1)) r.quantum = 0;  // eager only
-  if (r.quantum > 0) st = capture_quantum(r);
+  // two steps per pass of the loop when convection swaps f and f_conv (the graph then
+  // leaves them where it found them); a turn is a whole number of passes
+  r.body = (r.p.conv_method != DVM_CONV_NONE) ? 2 : 1;
+  r.quantum = std::max(r.body, sv->quantum - sv->quantum % r.body);
+  if (r.max_steps - r.steps_done < r.body) r.quantum = 0;  // eager steps only
+  if (r.quantum > 0) st = capture_turn(r);
   if (!st) st = cuda_st(cudaEventCreateWithFlags(&r.ev, cudaEventDisableTiming));
   return st;
 }
 
-// Issues the next turn of a request: one graph replay, or single eager steps for a tail
-// shorter than the graph (after which the graph is not replayed again).
+// Issues the next turn of a request: one launch of its graph (up to a turn's whole passes,
+// fewer if the residual reaches the tolerance on the way), or a single eager step for a
+// tail shorter than a pass (after which the graph is not launched again).
 int issue(dvm_server* sv, Request& r) {
-  const int left = r.max_steps - r.steps_issued;
-  int n = 0, st = DVM_OK;
-  if (r.quantum > 0 && !r.eager_tail && left >= r.quantum) {
-    st = cuda_st(cudaGraphLaunch(r.exec, r.stream));
-    n = r.quantum;
+  const int left = r.max_steps - r.steps_done;
+  int st = DVM_OK;
+  if (r.quantum > 0 && !r.eager_tail && left >= r.body) {
+    sv->h_left[r.slot] = std::min(r.quantum, left - left % r.body);
+    st = cuda_st(cudaMemcpyAsync(r.d_left, sv->h_left + r.slot, sizeof(int),
+                                 cudaMemcpyHostToDevice, r.stream));
+    if (!st) st = cuda_st(cudaGraphLaunch(r.exec, r.stream));
   } else {
     r.eager_tail = true;
     st = eager_step(r);
-    n = 1;
   }
   if (!st)
     st = cuda_st(cudaMemcpyAsync(sv->h_slots + r.slot, dvm::ctx_residual(r.ctx), sizeof(double),
                                  cudaMemcpyDeviceToHost, r.stream));
+  if (!st)
+    st = cuda_st(cudaMemcpyAsync(sv->h_steps + r.slot, r.d_step, sizeof(uint32_t),
+                                 cudaMemcpyDeviceToHost, r.stream));
   if (!st) st = cuda_st(cudaEventRecord(r.ev, r.stream));
-  if (!st) {
-    r.steps_issued += n;
-    r.inflight = true;
-  }
+  if (!st) r.inflight = true;
   return st;
 }
 
@@ -230,11 +275,13 @@ void release_device(Request& r) {
   if (r.ev) cudaEventDestroy(r.ev);
   if (r.d_step) cudaFreeAsync(r.d_step, r.stream);
   if (r.d_acc) cudaFreeAsync(r.d_acc, r.stream);
+  if (r.d_left) cudaFreeAsync(r.d_left, r.stream);
   dvm::ctx_destroy(r.ctx);
   r.exec = nullptr;
   r.ev = nullptr;
   r.d_step = nullptr;
   r.d_acc = nullptr;
+  r.d_left = nullptr;
   r.ctx = nullptr;
 }
 
@@ -390,10 +437,10 @@ void worker_loop(dvm_server* sv) {
         if (q == cudaErrorNotReady) continue;
         r.inflight = false;
         progress = true;
-        r.steps_done = r.steps_issued;
         if (q != cudaSuccess) {
           r.status = DVM_ERR_CUDA;
         } else {
+          r.steps_done = static_cast<int>(sv->h_steps[r.slot]);
           r.residual = sv->h_slots[r.slot];
           if (r.residual <= r.tol) r.converged = 1;
         }
@@ -455,7 +502,13 @@ int dvm_server_create(uint64_t hbm_budget_bytes, int max_active, int steps_per_t
   sv->quantum = steps_per_turn;
   cudaGetDevice(&sv->device);
   if (cudaHostAlloc(reinterpret_cast<void**>(&sv->h_slots), sizeof(double) * max_active,
+                    cudaHostAllocDefault) != cudaSuccess ||
+      cudaHostAlloc(reinterpret_cast<void**>(&sv->h_steps), sizeof(uint32_t) * max_active,
+                    cudaHostAllocDefault) != cudaSuccess ||
+      cudaHostAlloc(reinterpret_cast<void**>(&sv->h_left), sizeof(int) * max_active,
                     cudaHostAllocDefault) != cudaSuccess) {
+    if (sv->h_slots) cudaFreeHost(sv->h_slots);
+    if (sv->h_steps) cudaFreeHost(sv->h_steps);
     delete sv;
     return DVM_ERR_OOM;
   }
@@ -486,6 +539,8 @@ int dvm_server_destroy(dvm_server* sv) {
   if (sv->preparer.joinable()) sv->preparer.join();
   if (sv->retirer.joinable()) sv->retirer.join();
   cudaFreeHost(sv->h_slots);
+  cudaFreeHost(sv->h_steps);
+  cudaFreeHost(sv->h_left);
   delete sv;
   return DVM_OK;
 }

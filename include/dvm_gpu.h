@@ -252,10 +252,12 @@ int dvm_footprint_bytes(const dvm_params* params, const dvm_vgrid* vgrid, uint64
  * batching. No reference counterpart: the reference runs one solve per process. Native
  * host threads admit submitted requests in arrival order while the admitted footprints fit in
  * hbm_budget_bytes and fewer than max_active run; each admitted request keeps its state on
- * the device in its own context and stream and advances steps_per_turn steps per turn (one
- * CUDA-graph replay), so the turns of different requests overlap on the device. A request
- * ends when the convergence residual (dvm_get_residual) is <= residual_tol or after
- * max_steps steps. Its result depends only on its own parameters, seed and step count. */
+ * the device in its own context and stream and advances up to steps_per_turn steps per turn
+ * (one launch of a CUDA graph whose conditional while loop tests the residual on the device
+ * after every step, or every two steps with convection, and stops there), so the turns of
+ * different requests overlap on the device. A request ends when the convergence residual
+ * (dvm_get_residual) is <= residual_tol or after max_steps steps. Its result depends only
+ * on its own parameters, seed and step count. */
 typedef struct dvm_server dvm_server;
 typedef struct dvm_request_info {
   int32_t status;         /* DVM_OK or the status that ended the request               */

@@ -307,9 +307,10 @@ class DVMSolver:
 
 
 class DVMBatch:
-    """Many independent 0-D relaxations stepped together (dvm_batch_*): instances on the same
-    velocity grid share one context, one step of all of them is one CUDA-graph replay, and
-    the persistent collision launch of each grid is sized by a timing autotuner."""
+    """Many independent solves stepped together (dvm_batch_*): 0-D relaxations, or 1-D
+    instances of config.nx_space cells sharing the config's end conditions. Instances on the
+    same velocity grid share one context, one step of all of them is one CUDA-graph replay
+    (one launch of each kernel over all grids), and the launch shape is autotuned."""
 
     def __init__(self, config, grids, instance_grid, samples_per_grid, lib=None):
         self.lib = lib or load_library()
@@ -330,6 +331,7 @@ class DVMBatch:
             self.samples.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(b)), "dvm_batch_create")
         self.b = b
         self.ninstances = len(self.instance_grid)
+        self.cells = config.nx_space if config.geometry == DVM_GEOM_1D else 1
 
     def close(self):
         if getattr(self, "b", None):
@@ -344,12 +346,13 @@ class DVMBatch:
 
     def upload_f(self, instance, f):
         g = self.grids[self.instance_grid[instance]]
-        f = np.ascontiguousarray(f, dtype=np.float64).reshape(g.nv)
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.cells * g.nv)
         _check(self.lib.dvm_batch_upload_f(self.b, int(instance), _dptr(f)), "dvm_batch_upload_f")
 
     def download_f(self, instance):
+        """f of one instance: [nv] (0-D) or [cells, nv] (1-D)."""
         g = self.grids[self.instance_grid[instance]]
-        out = np.empty(g.nv)
+        out = np.empty((self.cells, g.nv)) if self.cells > 1 else np.empty(g.nv)
         _check(self.lib.dvm_batch_download_f(self.b, int(instance), _dptr(out)),
                "dvm_batch_download_f")
         return out
@@ -358,9 +361,10 @@ class DVMBatch:
         _check(self.lib.dvm_batch_step(self.b, int(nsteps)), "dvm_batch_step")
 
     def properties(self):
-        out = np.empty((self.ninstances, DVM_NPROP))
+        """[instances, DVM_NPROP] (0-D) or [instances, cells, DVM_NPROP] (1-D)."""
+        out = np.empty((self.ninstances, self.cells, DVM_NPROP))
         _check(self.lib.dvm_batch_get_properties(self.b, _dptr(out)), "dvm_batch_get_properties")
-        return out
+        return out if self.cells > 1 else out[:, 0, :]
 
     def time_steps(self, nsteps):
         ms, n = C.c_double(), C.c_int64()

@@ -229,7 +229,9 @@ int validate(const dvm_params* p, const dvm_vgrid* vg) {
       if (p->nx_space < 2 || p->ny_space < 2 || !(p->dx > 0.0) || !(p->dy > 0.0))
         return DVM_ERR_PARAM;
     } else if (p->geometry == DVM_GEOM_1D) {
-      if (p->nx_space < 3 || p->ny_space != 1 || !(p->dx > 0.0)) return DVM_ERR_PARAM;
+      // ny_space > 1: that many independent rows of nx_space cells (a batch of 1-D
+      // instances), each with both end conditions
+      if (p->nx_space < 3 || p->ny_space < 1 || !(p->dx > 0.0)) return DVM_ERR_PARAM;
       for (int e = 0; e < 2; ++e)
         if (p->bc[e] < DVM_BC1D_SPECULAR || p->bc[e] > DVM_BC1D_ZEROGRAD) return DVM_ERR_PARAM;
     } else {
@@ -741,7 +743,7 @@ int dvm_compute_convection(dvm_ctx* c) {
     }
   } else {
     Convect1DArgs a{};
-    a.g = c->g; a.nxs = c->p.nx_space;
+    a.g = c->g; a.nxs = c->p.nx_space; a.rows = c->p.ny_space;
     a.bc[0] = c->p.bc[DVM_WALL_LEFT]; a.bc[1] = c->p.bc[DVM_WALL_RIGHT];
     a.factor = c->p.dt / c->p.dx;
     a.acc = c->p.acc_coeff; a.mass = c->p.mass; a.pi = c->pi;
@@ -1002,7 +1004,13 @@ struct dvm_batch {
   std::vector<int> group_grid;          // grid index of each group
   std::vector<int> inst_group, inst_cell;
   cudaStream_t stream = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  // one step of every instance as a graph; 1-D instances swap f and f_conv every step, so
+  // they take two graphs, one for each placement of f (exec[parity])
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  int parity = 0;
+  bool swaps = false;        // 1-D instances with convection
+  int cells_per_inst = 1;    // 0-D: 1; 1-D: the cells of one instance (a row)
+  int conv_launches = 0;     // convection launches of one step (all groups)
   uint32_t* d_step = nullptr;
   bool props_stale = true;
   int64_t collisions_per_step = 0;
@@ -1018,7 +1026,8 @@ namespace {
 void batch_release(dvm_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (cudaGraphExec_t& e : b->exec)
+    if (e) cudaGraphExecDestroy(e);
   for (dvm_ctx* c : b->groups) release(c);
   if (b->d_step) cudaFree(b->d_step);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -1126,6 +1135,12 @@ int batch_issue(dvm_batch* b, bool cdf = true, bool plan = true, bool collide = 
     if (!st && collide) {
       st = cuda_status(launch_collide_grouped(gs.col, gs.fp32, b->stream));
       if (!st && gs.fp32) st = cuda_status(launch_project_grouped(gs.proj, b->stream));
+    }
+    if (!st && moments && b->swaps) {
+      // 1-D rows: convection and ends per group (each swaps its f and f_conv), then the
+      // moments of the new f
+      for (int k = 0; k < ng && !st; ++k) st = dvm_compute_convection(b->groups[g0 + k]);
+      if (!st) grouped_records(b, g0, ng, bps, gs);
     }
     if (!st && moments) st = cuda_status(launch_moments_grouped(gs.mom, b->stream));
     if (st) return st;
@@ -1244,23 +1259,34 @@ int batch_prepare(dvm_batch* b) {
     if (st) return st;
     b->props_stale = false;
   }
-  if (b->exec) return DVM_OK;
+  if (b->exec[0]) return DVM_OK;
   int st = autotune(b);
   if (st) return st;
-  // one step of every group, then the step counter, captured into one graph
-  cudaGraph_t graph = nullptr;
-  st = cuda_status(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
-  if (st) return st;
-  st = batch_issue(b);
-  if (!st) st = cuda_status(launch_step_end(b->d_step, nullptr, nullptr, b->stream));
-  const int st2 = cuda_status(cudaStreamEndCapture(b->stream, &graph));
-  if (st || st2) {
+  // one step of every group, then the step counter, captured into one graph; with 1-D
+  // rows a second graph for the other placement of f (the capture of the first leaves the
+  // host's f and f_conv swapped, the second swaps them back)
+  b->parity = 0;
+  for (int e = 0; e < (b->swaps ? 2 : 1) && !st; ++e) {
+    cudaGraph_t graph = nullptr;
+    st = cuda_status(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed));
+    if (st) return st;
+    st = batch_issue(b);
+    if (!st) st = cuda_status(launch_step_end(b->d_step, nullptr, nullptr, b->stream));
+    const int st2 = cuda_status(cudaStreamEndCapture(b->stream, &graph));
+    if (!st) st = st2;
+    if (!st) st = cuda_status(cudaGraphInstantiate(&b->exec[e], graph, 0));
     if (graph) cudaGraphDestroy(graph);
-    return st ? st : st2;
   }
-  st = cuda_status(cudaGraphInstantiate(&b->exec, graph, 0));
-  cudaGraphDestroy(graph);
   return st;
+}
+
+// Launches one step's graph and keeps the host's view of each 1-D group's f in step.
+int batch_launch(dvm_batch* b) {
+  const int st = cuda_status(cudaGraphLaunch(b->exec[b->parity], b->stream));
+  if (st || !b->swaps) return st;
+  for (dvm_ctx* c : b->groups) std::swap(c->d_f, c->d_fconv);
+  b->parity ^= 1;
+  return DVM_OK;
 }
 
 }  // namespace
@@ -1327,11 +1353,18 @@ int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrid
       ninstances < 1)
     return DVM_ERR_PARAM;
   if (params->coll_method == DVM_COLL_NONE) return DVM_ERR_PARAM;
+  // 0-D instances, or 1-D instances of nx_space cells (ny_space is set per grid)
+  if (params->geometry == DVM_GEOM_2D) return DVM_ERR_PARAM;
+  if (params->geometry == DVM_GEOM_1D && params->nx_space < 3) return DVM_ERR_PARAM;
   *out = nullptr;
   for (int i = 0; i < ninstances; ++i)
     if (instance_grid[i] < 0 || instance_grid[i] >= ngrids) return DVM_ERR_PARAM;
   dvm_batch* b = new (std::nothrow) dvm_batch();
   if (!b) return DVM_ERR_OOM;
+  if (params->geometry == DVM_GEOM_1D) {
+    b->cells_per_inst = params->nx_space;
+    b->swaps = (params->conv_method != DVM_CONV_NONE);
+  }
   int st = cuda_status(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   if (!st) st = dalloc(&b->d_step, 1);
   if (!st) st = cuda_status(cudaMemset(b->d_step, 0, sizeof(uint32_t)));
@@ -1347,10 +1380,15 @@ int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrid
       }
     if (count == 0) continue;
     dvm_params p = *params;
-    p.geometry = DVM_GEOM_0D;
-    p.nx_space = count;
-    p.ny_space = 1;
-    p.conv_method = DVM_CONV_NONE;
+    if (params->geometry == DVM_GEOM_1D) {
+      // one row of nx_space cells per instance, each with the ends of params
+      p.ny_space = count;
+    } else {
+      p.geometry = DVM_GEOM_0D;
+      p.nx_space = count;
+      p.ny_space = 1;
+      p.conv_method = DVM_CONV_NONE;
+    }
     p.samples_mode = DVM_SAMPLES_FIXED;
     p.samples_per_step = samples_per_grid[gidx];
     dvm_ctx* c = nullptr;
@@ -1359,7 +1397,17 @@ int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrid
     c->step_dev = b->d_step;
     b->groups.push_back(c);
     b->group_grid.push_back(gidx);
-    b->collisions_per_step += static_cast<int64_t>(count) * samples_per_grid[gidx];
+    b->collisions_per_step +=
+        static_cast<int64_t>(count) * b->cells_per_inst * samples_per_grid[gidx];
+    if (b->swaps) {
+      // the convection of a step: the interior sweep, then the node-local and the diffuse
+      // end launches its end conditions need
+      const bool nodes = p.bc[DVM_WALL_LEFT] != DVM_BC1D_DIFFUSE ||
+                         p.bc[DVM_WALL_RIGHT] != DVM_BC1D_DIFFUSE;
+      const bool diffuse = p.bc[DVM_WALL_LEFT] == DVM_BC1D_DIFFUSE ||
+                           p.bc[DVM_WALL_RIGHT] == DVM_BC1D_DIFFUSE;
+      b->conv_launches += 1 + (nodes ? 1 : 0) + (diffuse ? 1 : 0);
+    }
   }
   *out = b;
   return DVM_OK;
@@ -1375,9 +1423,9 @@ int dvm_batch_upload_f(dvm_batch* b, int instance, const double* f) {
   if (!b || !f || instance < 0 || instance >= static_cast<int>(b->inst_group.size()))
     return DVM_ERR_PARAM;
   dvm_ctx* c = b->groups[b->inst_group[instance]];
-  const size_t nv = c->g.nv;
-  int st = cuda_status(cudaMemcpyAsync(c->d_f + b->inst_cell[instance] * nv, f,
-                                       nv * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  const size_t n = static_cast<size_t>(b->cells_per_inst) * c->g.nv;
+  int st = cuda_status(cudaMemcpyAsync(c->d_f + b->inst_cell[instance] * n, f,
+                                       n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
   if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
   b->props_stale = true;
   return st;
@@ -1387,9 +1435,9 @@ int dvm_batch_download_f(dvm_batch* b, int instance, double* f) {
   if (!b || !f || instance < 0 || instance >= static_cast<int>(b->inst_group.size()))
     return DVM_ERR_PARAM;
   dvm_ctx* c = b->groups[b->inst_group[instance]];
-  const size_t nv = c->g.nv;
-  int st = cuda_status(cudaMemcpyAsync(f, c->d_f + b->inst_cell[instance] * nv,
-                                       nv * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  const size_t n = static_cast<size_t>(b->cells_per_inst) * c->g.nv;
+  int st = cuda_status(cudaMemcpyAsync(f, c->d_f + b->inst_cell[instance] * n,
+                                       n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   if (!st) st = cuda_status(cudaStreamSynchronize(b->stream));
   return st;
 }
@@ -1399,7 +1447,7 @@ int dvm_batch_step(dvm_batch* b, int nsteps) {
   int st = batch_prepare(b);
   if (st) return st;
   for (int s = 0; s < nsteps; ++s) {
-    st = cuda_status(cudaGraphLaunch(b->exec, b->stream));
+    st = batch_launch(b);
     if (st) return st;
   }
   return DVM_OK;
@@ -1409,10 +1457,11 @@ int dvm_batch_get_properties(dvm_batch* b, double* props) {
   if (!b || !props) return DVM_ERR_PARAM;
   int st = cuda_status(cudaStreamSynchronize(b->stream));
   if (st) return st;
+  const size_t n = static_cast<size_t>(b->cells_per_inst) * DVM_NPROP;
   for (size_t i = 0; i < b->inst_group.size(); ++i) {
     dvm_ctx* c = b->groups[b->inst_group[i]];
-    st = cuda_status(cudaMemcpy(props + i * DVM_NPROP, c->d_props + b->inst_cell[i] * DVM_NPROP,
-                                DVM_NPROP * sizeof(double), cudaMemcpyDeviceToHost));
+    st = cuda_status(cudaMemcpy(props + i * n, c->d_props + b->inst_cell[i] * n,
+                                n * sizeof(double), cudaMemcpyDeviceToHost));
     if (st) return st;
   }
   return DVM_OK;
@@ -1421,13 +1470,14 @@ int dvm_batch_get_properties(dvm_batch* b, double* props) {
 int dvm_batch_launch_shape(dvm_batch* b, int* cdf_threads, int* collide_ctas_per_sm,
                            int* launches_per_step) {
   if (!b || !cdf_threads || !collide_ctas_per_sm || !launches_per_step) return DVM_ERR_PARAM;
-  const bool tuned = b->exec != nullptr;
+  const bool tuned = b->exec[0] != nullptr;
   const int blocks = (static_cast<int>(b->groups.size()) + kMaxGroups - 1) / kMaxGroups;
   const bool fp32 = !b->groups.empty() && b->groups[0]->p.precision == DVM_PREC_FP32;
   *cdf_threads = tuned ? b->cdf_threads : 0;
   *collide_ctas_per_sm = tuned ? b->collide_bps : 0;
-  // per block of grids: CDF, plan, collide (+ projection), moments; then the step counter
-  *launches_per_step = tuned ? blocks * (fp32 ? 5 : 4) + 1 : 0;
+  // per block of grids: CDF, plan, collide (+ projection), moments; the convection of 1-D
+  // rows, per grid; then the step counter
+  *launches_per_step = tuned ? blocks * (fp32 ? 5 : 4) + b->conv_launches + 1 : 0;
   return DVM_OK;
 }
 
@@ -1439,7 +1489,7 @@ int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisio
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, b->stream);
-  for (int s = 0; s < nsteps && !st; ++s) st = cuda_status(cudaGraphLaunch(b->exec, b->stream));
+  for (int s = 0; s < nsteps && !st; ++s) st = batch_launch(b);
   cudaEventRecord(e1, b->stream);
   if (!st) st = cuda_status(cudaEventSynchronize(e1));
   float t = 0.f;

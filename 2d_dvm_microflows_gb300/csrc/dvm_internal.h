@@ -186,7 +186,8 @@ struct Convect2DArgs {
 
 struct Convect1DArgs {
   GridInfo g;
-  int nxs;
+  int nxs;                  // cells of one row
+  int rows;                 // independent rows of nxs cells, each with both ends
   int bc[2];
   double factor;            // dt/dx
   double acc, mass, pi;

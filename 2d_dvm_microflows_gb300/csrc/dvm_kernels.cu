@@ -2221,8 +2221,9 @@ __global__ void __launch_bounds__(256) k_convect1d(Convect1DArgs a) {
   const int nv = g.nv;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= nv) return;
-  const int nx = blockIdx.y;
-  const size_t off = static_cast<size_t>(nx) * nv + l;
+  const int cell = blockIdx.y;  // row cell / nxs, position nx in it
+  const int nx = cell % a.nxs;
+  const size_t off = static_cast<size_t>(cell) * nv + l;
   const double p0 = a.f[off];
   if (nx == 0 || nx == a.nxs - 1) { a.fconv[off] = p0; return; }
   const int i = l % g.nx;
@@ -2233,23 +2234,24 @@ __global__ void __launch_bounds__(256) k_convect1d(Convect1DArgs a) {
 }
 
 cudaError_t launch_convect1d(const Convect1DArgs& a, cudaStream_t s) {
-  dim3 grid((a.g.nv + 255) / 256, a.nxs);
+  dim3 grid((a.g.nv + 255) / 256, a.nxs * a.rows);
   k_convect1d<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 // End conditions (grid_ref conditions/boundary_conditions.f90:319-1000). The node-local
 // ones (specular, inflow Maxwellian, zero gradient) run one thread per node over both
-// ends (blockIdx.y = end); the diffuse wall, which needs the incoming and outgoing flux
-// sums of its end first, runs one CTA per end.
+// ends of every row (blockIdx.y = 2 row + end); the diffuse wall, which needs the incoming
+// and outgoing flux sums of its end first, runs one CTA per end.
 __global__ void __launch_bounds__(256) k_bc1d_nodes(Convect1DArgs a) {
   const GridInfo& g = a.g;
-  const int e = blockIdx.y;  // 0 left, 1 right
+  const int e = blockIdx.y & 1;  // 0 left, 1 right
+  const int row0 = (blockIdx.y >> 1) * a.nxs;
   const int bc = a.bc[e];
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= nv) return;
-  const int nx = (e == 0) ? 0 : a.nxs - 1;
+  const int nx = row0 + ((e == 0) ? 0 : a.nxs - 1);
   const double* f = a.f + static_cast<size_t>(nx) * nv;
   double* fc = a.fconv + static_cast<size_t>(nx) * nv;
   const double* W = a.wall[e];
@@ -2265,13 +2267,13 @@ __global__ void __launch_bounds__(256) k_bc1d_nodes(Convect1DArgs a) {
     const double b3 = g.bx[i] * g.by[j] * g.bz[k];
     fc[l] = maxwellian(g.x[i], g.y[j], g.z[k], mc, a.mass, u, 0.0, 0.0, T) * b3;
   } else if (bc == DVM_BC1D_ZEROGRAD) {  // apply_zero_gradient_flow :915-962
-    const double* src = a.fconv + static_cast<size_t>(e == 0 ? 1 : a.nxs - 2) * nv;
+    const double* src = a.fconv + static_cast<size_t>(row0 + (e == 0 ? 1 : a.nxs - 2)) * nv;
     fc[l] = src[l];
   }
 }
 
 cudaError_t launch_bc1d_nodes(const Convect1DArgs& a, cudaStream_t s) {
-  dim3 grid((a.g.nv + 255) / 256, 2);
+  dim3 grid((a.g.nv + 255) / 256, 2 * a.rows);
   k_bc1d_nodes<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
@@ -2281,8 +2283,9 @@ constexpr int kBc1dThreads = 1024;
 __global__ void __launch_bounds__(kBc1dThreads) k_bc1d(Convect1DArgs a) {
   __shared__ double s_red[2 * 32];
   const GridInfo& g = a.g;
-  const int e = blockIdx.x;  // 0 left, 1 right
-  const int nx = (e == 0) ? 0 : a.nxs - 1;
+  const int e = blockIdx.x & 1;  // 0 left, 1 right
+  const int row0 = (blockIdx.x >> 1) * a.nxs;
+  const int nx = row0 + ((e == 0) ? 0 : a.nxs - 1);
   const int bc = a.bc[e];
   const int nv = g.nv, NX = g.nx, NXY = g.nx * g.ny;
   const double* f = a.f + static_cast<size_t>(nx) * nv;
@@ -2290,7 +2293,7 @@ __global__ void __launch_bounds__(kBc1dThreads) k_bc1d(Convect1DArgs a) {
   const double* W = a.wall[e];
   if (bc == DVM_BC1D_DIFFUSE) {  // apply_diffuse_reflection :566-781
     const double T = W[DVM_WP_TEMP], u = W[DVM_WP_U], v = W[DVM_WP_V], w = W[DVM_WP_W];
-    const double* f2 = a.f + static_cast<size_t>(e == 0 ? 1 : a.nxs - 2) * nv;
+    const double* f2 = a.f + static_cast<size_t>(row0 + (e == 0 ? 1 : a.nxs - 2)) * nv;
     const double mc = maxwell_coeff(a.mass, T, a.pi);
     double acc2[2] = {0.0, 0.0};  // incoming density, computed outgoing density
     for (int l = threadIdx.x; l < nv; l += blockDim.x) {
@@ -2348,7 +2351,7 @@ __global__ void __launch_bounds__(kBc1dThreads) k_bc1d(Convect1DArgs a) {
 }
 
 cudaError_t launch_bc1d(const Convect1DArgs& a, cudaStream_t s) {
-  k_bc1d<<<2, kBc1dThreads, 0, s>>>(a);
+  k_bc1d<<<2 * a.rows, kBc1dThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -108,7 +108,8 @@ typedef struct dvm_vgrid {
 typedef struct dvm_params {
   int32_t geometry;        /* DVM_GEOM_*                                           */
   int32_t nx_space;        /* cells in x (1 for 0-D)                               */
-  int32_t ny_space;        /* cells in y (1 for 0-D and 1-D)                       */
+  int32_t ny_space;        /* cells in y (2-D); 1-D: independent rows of nx_space  */
+                           /* cells, each with both ends (1 = one 1-D domain)      */
   int32_t coll_method;     /* iColl                                                */
   int32_t conv_method;     /* iConv                                                */
   int32_t num_repl;        /* NRepl (replenishing_collisions.f90:134-354)          */
@@ -213,9 +214,12 @@ int dvm_checkpoint_size(dvm_ctx* ctx, uint64_t* bytes);
 int dvm_checkpoint_save(dvm_ctx* ctx, uint64_t ntime, void* buf, uint64_t bytes);
 int dvm_checkpoint_load(dvm_ctx* ctx, const void* buf, uint64_t bytes, uint64_t* ntime);
 
-/* ---- batched homogeneous instances --------------------------------------------------- */
+/* ---- batched instances ----------------------------------------------------------------- */
 /* Many independent 0-D relaxations (the reference's homogeneous case, nx_space = ny_space =
- * 1, run for many initial states and grids at once). No reference counterpart. Instances on
+ * 1, run for many initial states and grids at once), or, with params->geometry =
+ * DVM_GEOM_1D, many 1-D solves of params->nx_space cells each, all with the end conditions
+ * of params (each instance is one row of a multi-row 1-D context). No reference
+ * counterpart. Instances on
  * the same velocity grid form one group (one context whose cells are the instances). One
  * step of every instance is one launch each of the CDF build, the sample plan, the
  * persistent collision kernel (the precision form adds the projection) and the moments, over
@@ -230,11 +234,12 @@ int dvm_batch_create(const dvm_params* params, const dvm_vgrid* grids, int ngrid
                      const int32_t* instance_grid, int ninstances,
                      const int64_t* samples_per_grid, dvm_batch** out);
 int dvm_batch_destroy(dvm_batch* b);
-/* f of one instance ([Nv] of its grid); properties are computed at the next step. */
+/* f of one instance ([Nv] of its grid; 1-D: [nx_space][Nv]); properties are computed at
+ * the next step. */
 int dvm_batch_upload_f(dvm_batch* b, int instance, const double* f);
 int dvm_batch_download_f(dvm_batch* b, int instance, double* f);
 int dvm_batch_step(dvm_batch* b, int nsteps);
-/* props[ninstances][DVM_NPROP] */
+/* props[ninstances][DVM_NPROP] (1-D: [ninstances][nx_space][DVM_NPROP]) */
 int dvm_batch_get_properties(dvm_batch* b, double* props);
 /* Device time of nsteps graph replays (ms) and the samples they drew. */
 int dvm_batch_time_steps(dvm_batch* b, int nsteps, double* ms, int64_t* collisions);

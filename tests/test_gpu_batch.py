@@ -200,3 +200,106 @@ def test_batch_configuration4_grids_single_grouped_launch(gpulib, pkg, prec):
             fb = batch.download_f(i)
             assert np.abs(fb - fs[c]).max() <= ftol * np.abs(fs[c]).max(), (q, i)
     batch.close()
+
+
+def _row_states(ph, g, rows, nxs, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(rows):
+        f, _, _ = ph.shock_profile(g, nxs, 0.5, 1.6 + 0.3 * r, 1.5)
+        out.append(f * (1.0 + 0.05 * rng.random(f.shape)))
+    return out
+
+
+@pytest.mark.parametrize("bc", [("INOUT", "INOUT"), ("DIFFUSE", "SPECULAR"),
+                                ("ZEROGRAD", "DIFFUSE")])
+def test_1d_rows_equal_single_row_contexts(gpulib, pkg, bc):
+    """A 1-D context of several rows (ny_space > 1) is that many independent 1-D domains,
+    each with both end conditions: three convection steps of a three-row context equal three
+    single-row contexts to 1e-12 (partial accommodation, so the diffuse end's specular remap
+    runs too)."""
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(10, -5.0, 5.0)
+    nxs, rows = 6, 3
+    f0 = _row_states(ph, g, rows, nxs, 1)
+    code = {"INOUT": pkg.DVM_BC1D_INOUT, "DIFFUSE": pkg.DVM_BC1D_DIFFUSE,
+            "SPECULAR": pkg.DVM_BC1D_SPECULAR, "ZEROGRAD": pkg.DVM_BC1D_ZEROGRAD}
+    walls = ((1.5, -0.8, 0.0, 0.0, 1.4), (1.0, -1.6, 0.0, 0.0, 1.0), (1, 0, 0, 0, 1.0),
+             (1, 0, 0, 0, 1.0))
+
+    def cfg(ny):
+        return pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=nxs, ny_space=ny, dx=0.5,
+                             deltat=0.05, iColl=pkg.DVM_COLL_NONE, iConv=pkg.DVM_CONV_UPWIND1,
+                             bc=(code[bc[0]], code[bc[1]], 0, 0), walls=walls, acc_coeff=0.7)
+
+    multi = pkg.DVMSolver(cfg(rows), g)
+    multi.initialize_dist_func(np.concatenate(f0))
+    multi.solve(3)
+    fm, pm = multi.phi(), multi.properties()
+    assert multi.error_word() == 0
+    for r in range(rows):
+        s = pkg.DVMSolver(cfg(1), g)
+        s.initialize_dist_func(f0[r])
+        s.solve(3)
+        fs, ps = s.phi(), s.properties()
+        s.close()
+        rr = slice(r * nxs, (r + 1) * nxs)
+        assert np.abs(fm[rr] - fs).max() <= 1e-12 * np.abs(fs).max(), r
+        assert np.abs(pm[rr, :17] - ps[:, :17]).max() <= 1e-11 * max(1.0, np.abs(ps).max())
+    multi.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_batch_1d_instances(gpulib, pkg, prec):
+    """1-D instances join the batch: five 8-cell shock instances on two grids (inflow ends,
+    VR collisions), one grouped launch of each collision kernel plus the convection of each
+    grid per step. Three steps (both placements of f, so both of the batch's graphs) equal
+    the multi-row contexts of each grid's instances: FP64 to 1e-12; FP32 one step to the
+    FP32 rounding of the increment."""
+    ph = pkg.physics
+    prec = pkg.DVM_PREC_FP64 if prec == "fp64" else pkg.DVM_PREC_FP32
+    grids = [ph.VelocityGrid.uniform(12, -6.0, 6.0), ph.VelocityGrid.uniform(14, -6.0, 6.0)]
+    samples = [3000, 4000]
+    gid = np.array([0, 1, 0, 1, 1], dtype=np.int32)
+    nxs = 8
+    f0 = [_row_states(ph, grids[q], 1, nxs, 10 + i)[0] for i, q in enumerate(gid)]
+    _, up, dn = ph.shock_profile(grids[0], nxs, 0.5, 1.6, 1.5)
+    walls = ((dn["n"], dn["u"], 0.0, 0.0, dn["T"]), (up["n"], up["u"], 0.0, 0.0, up["T"]),
+             (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0))
+
+    def cfg(ny=1, fixed=None):
+        c = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=nxs, ny_space=ny, dx=0.5,
+                          deltat=0.05, iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                          bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), walls=walls,
+                          seed=21, precision=prec)
+        if fixed is not None:
+            c.samples_mode = pkg.DVM_SAMPLES_FIXED
+            c.samples_per_step = fixed
+        return c
+
+    batch = pkg.DVMBatch(cfg(), grids, gid, samples)
+    for i, f in enumerate(f0):
+        batch.upload_f(i, f)
+    nsteps = 3 if prec == pkg.DVM_PREC_FP64 else 1
+    batch.step(nsteps)
+    shape = batch.launch_shape()
+    assert shape["launches_per_step"] == (4 if prec == pkg.DVM_PREC_FP64 else 5) + 2 * 2 + 1
+    pb = batch.properties()
+    assert pb.shape == (len(gid), nxs, pkg.DVM_NPROP)
+    for q, g in enumerate(grids):
+        members = np.flatnonzero(gid == q)
+        s = pkg.DVMSolver(cfg(len(members), samples[q]), g)
+        s.initialize_dist_func(np.concatenate([f0[i] for i in members]))
+        s.solve(nsteps)
+        fs, ps = s.phi(), s.properties()
+        assert s.error_word() == 0
+        s.close()
+        ftol = 1e-12 if prec == pkg.DVM_PREC_FP64 else 1e-5
+        for c, i in enumerate(members):
+            rr = slice(c * nxs, (c + 1) * nxs)
+            fb = batch.download_f(i)
+            assert fb.shape == (nxs, g.nv)
+            assert np.abs(fb - fs[rr]).max() <= ftol * np.abs(fs[rr]).max(), (q, i)
+            if prec == pkg.DVM_PREC_FP64:
+                assert np.abs(pb[i, :, :17] - ps[rr, :17]).max() <= 1e-11 * max(1.0, np.abs(ps).max())
+    batch.close()

@@ -514,6 +514,84 @@ def run_batch(pkg, args):
     return out
 
 
+BATCH1D_INSTANCES = 64
+BATCH1D_CELLS = 100
+BATCH1D_SAMPLES = 20000  # per cell-step
+
+
+def run_batch_1d(pkg, args):
+    """1-D instances batched: 64 shock solves of 100 cells on 24^3 and 28^3 grids (Mach
+    U[1.5,3] tanh profiles, one shared pair of inflow ends, 2e4 VR samples per cell-step),
+    FP32+projection batched against the plain FP64 path (one context per instance, one
+    dvm_step call per instance-step)."""
+    import dataclasses
+    ph = pkg.physics
+    rng = np.random.default_rng(SEED + 1)
+    grids = [ph.VelocityGrid.uniform(n, -8.0, 8.0) for n in (24, 28)]
+    gid = rng.integers(0, len(grids), BATCH1D_INSTANCES).astype(np.int32)
+    mol = ph.molecule("Ar", ph.CSECTION_VHS)
+    f0 = []
+    for i in range(BATCH1D_INSTANCES):
+        f, up, dn = ph.shock_profile(grids[gid[i]], BATCH1D_CELLS, 0.5, rng.uniform(1.5, 3.0), 10.0)
+        f0.append(f)
+    _, up, dn = ph.shock_profile(grids[0], 3, 0.5, 2.0, 10.0)
+    walls = ((dn["n"], dn["u"], 0.0, 0.0, dn["T"]), (up["n"], up["u"], 0.0, 0.0, up["T"]),
+             (1.0, 0.0, 0.0, 0.0, 1.0), (1.0, 0.0, 0.0, 0.0, 1.0))
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=BATCH1D_CELLS, dx=0.5, deltat=0.04,
+                        Kn=1.0, mass=mol["mass"], omega=mol["omega"], alpha=mol["alpha"],
+                        sigma=ph.cross_section(mol, ph.CSECTION_BIRD), iColl=pkg.DVM_COLL_VR,
+                        iConv=pkg.DVM_CONV_UPWIND1, samples_mode=pkg.DVM_SAMPLES_FIXED,
+                        samples_per_step=BATCH1D_SAMPLES,
+                        bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), walls=walls, seed=SEED)
+    per_step = BATCH1D_INSTANCES * BATCH1D_CELLS * BATCH1D_SAMPLES
+    out = {"workload": "%d 1-D shocks of %d cells on 24^3/28^3 grids on [-8,8], VHS, Mach "
+                       "U[1.5,3], inflow ends, %d VR samples per cell-step"
+                       % (BATCH1D_INSTANCES, BATCH1D_CELLS, BATCH1D_SAMPLES),
+           "collisions_per_step": per_step}
+    b = pkg.DVMBatch(dataclasses.replace(cfg, precision=pkg.DVM_PREC_FP32), grids, gid,
+                     [BATCH1D_SAMPLES] * len(grids))
+    for i, f in enumerate(f0):
+        b.upload_f(i, f)
+    b.step(args.warmup + 1)
+    ms_dev, colls = b.time_steps(2 * args.steps)
+    t0 = time.perf_counter()
+    b.step(2 * args.steps)
+    b.properties()
+    wall = time.perf_counter() - t0
+    out["fp32_batched"] = {"value": colls / (ms_dev * 1e-3), "unit": "collisions/s",
+                           "ms_per_step": ms_dev / (2 * args.steps),
+                           "wall_collisions_per_s": per_step * 2 * args.steps / wall,
+                           "cell_updates_per_s": BATCH1D_INSTANCES * BATCH1D_CELLS * 2 *
+                           args.steps / wall, "launch_shape": b.launch_shape()}
+    b.close()
+    solvers = []
+    for i, f in enumerate(f0):
+        s = pkg.DVMSolver(cfg, grids[gid[i]])
+        s.initialize_dist_func(f)
+        solvers.append(s)
+    for s in solvers:
+        s.solve(1)
+    for s in solvers:
+        s.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for s in solvers:
+            s.solve(1)
+    for s in solvers:
+        s.synchronize()
+    wall = time.perf_counter() - t0
+    out["fp64_plain"] = {"value": per_step * args.steps / wall, "unit": "collisions/s",
+                         "cell_updates_per_s": BATCH1D_INSTANCES * BATCH1D_CELLS * args.steps /
+                         wall}
+    bad = sum(int(s.error_word() != 0) for s in solvers)
+    for s in solvers:
+        s.close()
+    out["fp64_plain"]["instances_with_error"] = bad
+    out["speedup_fp32_batched_vs_fp64_plain"] = (out["fp32_batched"]["wall_collisions_per_s"] /
+                                                 out["fp64_plain"]["value"])
+    return out
+
+
 SERVE_REQUESTS = 200
 SERVE_RATE = 50.0        # Poisson arrivals per second
 SERVE_MAX_STEPS = 40
@@ -821,6 +899,7 @@ def run_gpu(args):
     if ws == 1 and not args.no_forms:
         line["forms"] = run_forms(pkg, args, value)
         line["forms"]["batched"] = run_batch(pkg, args)
+        line["forms"]["batched_1d"] = run_batch_1d(pkg, args)
         line["forms"]["served"] = run_serving(pkg, args)
     if ws == 1 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -838,7 +917,8 @@ def run_gpu(args):
 def run_case(args):
     """One form alone (for profiling and quick checks): prints its JSON object."""
     pkg = importlib.import_module("2d_dvm_microflows_gb300")
-    fn = {"cavity": run_cavity, "batch": run_batch, "served": run_serving}[args.case]
+    fn = {"cavity": run_cavity, "batch": run_batch, "batch1d": run_batch_1d,
+          "served": run_serving}[args.case]
     print(json.dumps({"case": args.case, "result": fn(pkg, args)}))
     return 0
 
@@ -854,7 +934,7 @@ def main():
                     help="skip the precision-form and cavity measurements")
     ap.add_argument("--cells", type=int, default=None,
                     help="smaller case of the same workload (profiling only)")
-    ap.add_argument("--case", default=None, choices=["cavity", "batch", "served"],
+    ap.add_argument("--case", default=None, choices=["cavity", "batch", "batch1d", "served"],
                     help="run one form alone and print its result (profiling)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gpu":

@@ -224,6 +224,19 @@ class DVMSolver:
         _check(self.lib.dvm_step(self.ctx, C.c_uint64(self.ntime), int(nsteps)), "dvm_step")
         self.ntime += nsteps
 
+    def step_host(self, f_in, nsteps=1, f_out=None):
+        """dvm_step_host: f_in (host, [cells, nv]) in, nsteps steps, f out (into f_out, which
+        may be f_in itself; a new array if None). Page-locked buffers move by the kernels."""
+        f_in = np.ascontiguousarray(f_in, dtype=np.float64)
+        if f_out is None:
+            f_out = np.empty_like(f_in)
+        if f_out.dtype != np.float64 or not f_out.flags["C_CONTIGUOUS"]:
+            raise ValueError("f_out must be a contiguous float64 array")
+        _check(self.lib.dvm_step_host(self.ctx, C.c_uint64(self.ntime), int(nsteps),
+                                      _dptr(f_in), _dptr(f_out)), "dvm_step_host")
+        self.ntime += nsteps
+        return f_out
+
     def collision_count(self):
         v = C.c_int64()
         _check(self.lib.dvm_last_collision_count(self.ctx, C.byref(v)), "dvm_last_collision_count")

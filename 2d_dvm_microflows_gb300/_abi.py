@@ -133,6 +133,8 @@ ENTRY_POINTS = {
     "dvm_checkpoint_size": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "dvm_checkpoint_save": (C.c_int, [_P, C.c_uint64, C.c_void_p, C.c_uint64]),
     "dvm_checkpoint_load": (C.c_int, [_P, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "dvm_step_host": (C.c_int, [_P, C.c_uint64, C.c_int, C.POINTER(C.c_double),
+                                C.POINTER(C.c_double)]),
     "dvm_batch_create": (C.c_int, [C.POINTER(dvm_params), C.POINTER(dvm_vgrid), C.c_int,
                                    C.POINTER(C.c_int32), C.c_int, C.POINTER(C.c_int64),
                                    C.POINTER(_P)]),

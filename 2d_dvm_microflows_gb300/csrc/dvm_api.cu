@@ -607,7 +607,8 @@ int dvm_download_f(dvm_ctx* c, double* f) {
 
 int dvm_calculate_physical_properties(dvm_ctx* c) {
   if (!c) return DVM_ERR_PARAM;
-  MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, c->d_residual};
+  MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, c->d_residual,
+               nullptr};
   int st = cuda_status(cudaMemsetAsync(c->d_residual, 0, sizeof(unsigned long long), c->stream));
   if (st) return st;
   return launch(c, DVM_K_MOMENTS, [&] { return launch_moments(a, c->stream); });
@@ -769,6 +770,52 @@ int dvm_step(dvm_ctx* c, uint64_t first_step, int nsteps) {
     if (st) return st;
   }
   return DVM_OK;
+}
+
+int dvm_step_host(dvm_ctx* c, uint64_t first_step, int nsteps, const double* f_in,
+                  double* f_out) {
+  if (!c || !f_in || !f_out || nsteps < 1) return DVM_ERR_PARAM;
+  // the device's view of a page-locked host buffer (null if the device cannot reach it)
+  auto device_view = [](const void* p) -> void* {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    if (at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged) return at.devicePointer;
+    return nullptr;
+  };
+  const double* din = static_cast<const double*>(device_view(f_in));
+  double* dout = static_cast<double*>(device_view(f_out));
+  int st = DVM_OK;
+  if (din) {
+    // the moments of the new state, read from host memory, write the device's copy of f
+    MomentArgs a{c->g, c->ncells, c->p.mass, din, c->d_props, c->d_err, c->d_residual, c->d_f};
+    st = cuda_status(cudaMemsetAsync(c->d_residual, 0, sizeof(unsigned long long), c->stream));
+    if (!st) st = launch(c, DVM_K_MOMENTS, [&] { return launch_moments(a, c->stream); });
+  } else {
+    st = dvm_upload_f(c, f_in);
+  }
+  for (int s = 0; s < nsteps && !st; ++s) {
+    st = dvm_compute_collision_integral(c, first_step + static_cast<uint64_t>(s), nullptr);
+    if (!st) st = dvm_compute_convection(c);
+    if (st) break;
+    if (s + 1 < nsteps || !dout) {
+      st = dvm_calculate_physical_properties(c);
+    } else {
+      // the last moments write the result to host memory as they read it
+      MomentArgs a{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, c->d_residual,
+                   dout};
+      st = cuda_status(cudaMemsetAsync(c->d_residual, 0, sizeof(unsigned long long), c->stream));
+      if (!st) st = launch(c, DVM_K_MOMENTS, [&] { return launch_moments(a, c->stream); });
+    }
+  }
+  if (!st && !dout) {
+    const size_t bytes = static_cast<size_t>(c->ncells) * c->g.nv * sizeof(double);
+    st = cuda_status(cudaMemcpyAsync(f_out, c->d_f, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (st) return st;
+  return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
 int dvm_last_collision_count(dvm_ctx* c, int64_t* count) {
@@ -1099,7 +1146,8 @@ void grouped_records(const dvm_batch* b, int g0, int ng, int bps, GroupedStep& g
     gs.col.tf[k] = c->tabs_f;
     gs.col.df[k] = c->d_df;
     gs.proj.a[k] = ProjectArgs{c->g, c->ncells, c->d_f, c->d_df, c->d_props};
-    gs.mom.a[k] = MomentArgs{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err, nullptr};
+    gs.mom.a[k] = MomentArgs{c->g, c->ncells, c->p.mass, c->d_f, c->d_props, c->d_err,
+                             nullptr, nullptr};
     work[k] = b->group_cost.size() == b->groups.size()
                   ? b->group_cost[g0 + k]
                   : static_cast<double>(c->ncells) * static_cast<double>(c->p.samples_per_step);

@@ -207,6 +207,9 @@ struct MomentArgs {
   // max over cells of the relative change of n, u and T since the previous moments
   // (the convergence residual); nonnegative doubles, compared as integers
   unsigned long long* residual;
+  // if set, every value of f the kernel reads is also written here (the same layout): the
+  // device copy of an f read from host memory, or the host copy of the device's f
+  double* mirror;
 };
 
 // Grouped launches: the instances of a batch on up to kMaxGroups velocity grids advance in

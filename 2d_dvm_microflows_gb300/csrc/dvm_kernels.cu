@@ -2382,7 +2382,7 @@ constexpr int kMomAhead = 4;  // column nodes read ahead of the sums
 // first CTA, which adds them in rank order and forms the properties.
 constexpr int kMomSplitMax = 4;
 
-template <bool kSplit, class Src>
+template <bool kSplit, class Src, bool kMirror = false>
 __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, Src& src) {
   __shared__ float2 s_red[kMomAcc * 32];
   __shared__ dfl s_ax[4 * kMaxAxis];  // x', x'^2, y', y'^2
@@ -2431,6 +2431,7 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
     double fb[kMomAhead];
 #pragma unroll
     for (int u = 0; u < kMomAhead; ++u) fb[u] = (u < NZ) ? src.raw(u) : 0.0;
+    double* mir = kMirror ? a.mirror + static_cast<size_t>(cell) * g.nv + col : nullptr;
     for (int k0 = 0; k0 < NZ; k0 += kMomAhead) {
       double fn[kMomAhead];
 #pragma unroll
@@ -2440,6 +2441,7 @@ __device__ __forceinline__ void moments_of_cell(const MomentArgs& a, int cell, S
       for (int u = 0; u < kMomAhead; ++u) {
         const int k = k0 + u;
         if (k >= NZ) break;
+        if constexpr (kMirror) mir[NXY * k] = fb[u];
         const dfl fv = dfl_from_double(fb[u]);
         dacc_add(G0, fv);
         dacc_fma(G1, fv, s_z[k]);
@@ -2575,17 +2577,19 @@ struct MomSourceF {
   __device__ double raw(int k) const { return __ldg(f + col + NXY * k); }
 };
 
+template <bool kMirror>
 __global__ void __launch_bounds__(kMomThreads, 3) k_moments(MomentArgs a) {
   const int cell = blockIdx.x;
   MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
-  moments_of_cell<false>(a, cell, src);
+  moments_of_cell<false, MomSourceF, kMirror>(a, cell, src);
 }
 
 // Launched in clusters of 2 or 4 CTAs per cell.
+template <bool kMirror>
 __global__ void __launch_bounds__(kMomThreads, 3) k_moments_split(MomentArgs a) {
   const int cell = static_cast<int>(blockIdx.x / cooperative_groups::this_cluster().num_blocks());
   MomSourceF src{a.f + static_cast<size_t>(cell) * a.g.nv, a.g.nx * a.g.ny, 0};
-  moments_of_cell<true>(a, cell, src);
+  moments_of_cell<true, MomSourceF, kMirror>(a, cell, src);
 }
 
 
@@ -2593,8 +2597,10 @@ cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
   // CTAs per cell: enough that a launch of few cells still covers the SMs twice over
   int split = 1;
   while (split < kMomSplitMax && a.ncells * split < 2 * sm_count()) split *= 2;
+  const bool mirror = a.mirror != nullptr;
   if (split == 1) {
-    k_moments<<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
+    if (mirror) k_moments<true><<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
+    else k_moments<false><<<a.ncells, column_threads(a.g, kMomThreads), 0, s>>>(a);
     return cudaGetLastError();
   }
   GridInfo gs = a.g;  // the columns one CTA walks
@@ -2613,7 +2619,8 @@ cudaError_t launch_moments(const MomentArgs& a, cudaStream_t s) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_moments_split, a);
+  return mirror ? cudaLaunchKernelEx(&cfg, k_moments_split<true>, a)
+                : cudaLaunchKernelEx(&cfg, k_moments_split<false>, a);
 }
 
 // ----------------------------------------------------------------------------------------

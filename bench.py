@@ -823,7 +823,7 @@ def run_gpu(args):
     colls_all = dist_reduce(dist, colls, "sum")
     value = colls_all / (t_max * 1e-3)
 
-    # end to end through the C ABI: f in pinned host memory, copied in and out every step
+    # end to end through the C ABI: f in pinned host memory, moved in and out every step
     host = torch.empty((NCELLS, nv), dtype=torch.float64, pin_memory=True)
     hnp = host.numpy()
     hnp[:] = s.phi()
@@ -833,12 +833,11 @@ def run_gpu(args):
     t0 = time.perf_counter()
     e2e_colls = 0
     for k in range(args.steps):
-        if lib.dvm_upload_f(s.ctx, ptr):
-            raise RuntimeError("upload failed")
-        if lib.dvm_step(s.ctx, C.c_uint64(10000 + k), 1):
+        # f from pinned host memory in, one step, f back out to the same host buffer
+        # (dvm_step_host: the device reads and writes the page-locked buffer in its moments
+        # passes)
+        if lib.dvm_step_host(s.ctx, C.c_uint64(10000 + k), 1, ptr, ptr):
             raise RuntimeError("step failed")
-        if lib.dvm_download_f(s.ctx, ptr):
-            raise RuntimeError("download failed")
         e2e_colls += cfg.samples_per_step * NCELLS
     t_e2e = time.perf_counter() - t0
     t_e2e = dist_reduce(dist, t_e2e, "max")

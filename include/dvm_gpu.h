@@ -188,6 +188,15 @@ int dvm_set_properties(dvm_ctx* ctx, const double* props);
 /* One solve() iteration per step: collisions, convection, moments
  * (solver/dvm_solver.f90:299-357). first_step is the Philox step counter of the first. */
 int dvm_step(dvm_ctx* ctx, uint64_t first_step, int nsteps);
+/* No reference counterpart: dvm_upload_f(f_in), dvm_step(first_step, nsteps) and
+ * dvm_download_f(f_out) in one call, for a host that keeps f in its own memory between
+ * steps (the reference's phi). When f_in / f_out are page-locked (cudaHostAlloc,
+ * cudaHostRegister), the device reads f_in in the moments pass that starts the call (which
+ * writes the device's copy as it goes) and writes f_out in the moments pass that ends it,
+ * instead of separate copies; other host memory goes through copies. f_in and f_out may be
+ * the same buffer. Returns after f_out is written. */
+int dvm_step_host(dvm_ctx* ctx, uint64_t first_step, int nsteps, const double* f_in,
+                  double* f_out);
 /* Collision samples drawn by the last collision call, summed over cells (tot_colls). */
 int dvm_last_collision_count(dvm_ctx* ctx, int64_t* count);
 /* Scatter adds into f made by the last collision call, counted by the collide kernel: two

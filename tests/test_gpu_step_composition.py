@@ -73,3 +73,40 @@ def test_step_with_collisions(gpulib, pkg):
     fa, fb = a.phi(), b.phi()
     assert np.abs(fa - fb).max() <= 1e-13 * np.abs(fa).max()
     assert np.abs(a.properties()[:, :17] - b.properties()[:, :17]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_host_equals_upload_step_download(gpulib, pkg, pinned):
+    """dvm_step_host (host f in, steps, host f out in one call) gives what dvm_upload_f,
+    dvm_step and dvm_download_f give: with page-locked buffers the device reads and writes
+    them in its moments passes, with pageable ones through copies. Same Philox steps, so the
+    results agree to the FP64 atomics' ordering (1e-12), moments included, and the buffer
+    may be both input and output."""
+    import torch
+
+    ph = pkg.physics
+    g = ph.VelocityGrid.uniform(14, -6.0, 6.0)
+    f0, up, dn = ph.shock_profile(g, 12, 0.5, 2.0, 2.0)
+    walls = ((dn["n"], dn["u"], 0.0, 0.0, dn["T"]), (up["n"], up["u"], 0.0, 0.0, up["T"]),
+             (1, 0, 0, 0, 1.0), (1, 0, 0, 0, 1.0))
+    cfg = pkg.DVMConfig(geometry=pkg.DVM_GEOM_1D, nx_space=12, dx=0.5, deltat=0.05,
+                        iColl=pkg.DVM_COLL_VR, iConv=pkg.DVM_CONV_UPWIND1,
+                        samples_mode=pkg.DVM_SAMPLES_FIXED, samples_per_step=5000,
+                        bc=(pkg.DVM_BC1D_INOUT, pkg.DVM_BC1D_INOUT, 0, 0), walls=walls, seed=3)
+    ref = pkg.DVMSolver(cfg, g)
+    ref.initialize_dist_func(f0)
+    ref.solve(3)
+    fr, pr = ref.phi(), ref.properties()
+    ref.close()
+    if pinned:
+        buf = torch.empty(f0.shape, dtype=torch.float64, pin_memory=True).numpy()
+    else:
+        buf = np.empty_like(f0)
+    buf[:] = f0
+    s = pkg.DVMSolver(cfg, g)
+    s.step_host(buf, 3, f_out=buf)
+    ps = s.properties()
+    assert s.error_word() == 0
+    s.close()
+    assert np.abs(buf - fr).max() <= 1e-12 * np.abs(fr).max()
+    assert np.abs(ps[:, :17] - pr[:, :17]).max() <= 1e-11 * max(1.0, np.abs(pr).max())

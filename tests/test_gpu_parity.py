@@ -31,6 +31,13 @@ def prop_scales(p):
     return np.array(sc)
 
 
+def node_rel_err(a, b, floor=1e-30):
+    """Largest error of a node relative to the node's own value (values below floor times
+    the largest are judged on that floor): the tails of f are checked, not only the peak."""
+    scale = np.maximum(np.abs(b), floor * np.abs(b).max())
+    return (np.abs(a - b) / scale).max()
+
+
 def props_err(a, b):
     return (np.abs(a[:, :17] - b[:, :17]).max(0) / prop_scales(b)).max()
 
@@ -245,6 +252,8 @@ def test_cavity_convection(gpulib, pkg, oracle, acc, grid_n, lr):
         gpu.compute_convection()
         cpu.compute_convection()
         assert rel_err(gpu.phi(), cpu.phi()) <= REL
+        # deterministic: every node, tails included, to its own value
+        assert node_rel_err(gpu.phi(), cpu.phi()) <= 1e-11
     assert gpu.error_word() == 0
 
 
@@ -262,6 +271,7 @@ def test_1d_convection(gpulib, pkg, oracle, bc):
         gpu.compute_convection()
         cpu.compute_convection()
         assert rel_err(gpu.phi(), cpu.phi()) <= REL
+        assert node_rel_err(gpu.phi(), cpu.phi()) <= 1e-11
 
 
 def test_cavity_full_steps(gpulib, pkg, oracle):

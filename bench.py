@@ -602,7 +602,7 @@ SERVE_QUANTUM = 16   # steps per turn at most (the turn's graph loops on the dev
                      # stops at convergence; measured on 120 requests: 7.58e9 collisions/s
                      # at 16, 7.43e9 at 8, 6.80e9 at 40)
 SERVE_PREEMPT = 0    # turns before a request yields its slot to a waiting one (0: never)
-SERVE_ENS = 4        # seeds per precision in the ensemble accuracy comparison
+SERVE_ENS = 8        # seeds per precision in the ensemble accuracy comparison
 SERVE_ENS_REQ = 3    # requests of each kind in that comparison
 
 

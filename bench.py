@@ -282,7 +282,7 @@ ENS_SEEDS = 4  # independent seeds per precision in the ensemble accuracy compar
 
 
 def ensemble_error(pkg, make, steps, seeds=ENS_SEEDS):
-    """Accuracy of the precision form as the benchmark spec states it, at matched ensembles:
+    """Accuracy of the precision form against FP64 at matched ensembles:
     `make(precision, seed)` returns a stepped-ready solver (or batch); after `steps` steps the
     means over `seeds` independent seeds of each precision are compared per moment field
     (moment_error), beside the FP64 ensemble's own standard error on the same scale."""

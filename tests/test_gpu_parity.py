@@ -679,8 +679,8 @@ CONSERVED = ("dens", "u", "v", "w", "temp", "species_temp", "pressure")
 def test_ensemble_relaxation_configuration_all_fields(gpulib, pkg, oracle):
     """Configuration 1 (24^3, two Maxwellians, 1e5 samples per step, dt 0.01), 20 steps,
     16 independent Philox seeds on each side: the fields every collision conserves (n, u,
-    T, p) agree to round-off, and the ensemble means of every other field the benchmark spec
-    names (mean speed, heat flux q_x, q_y, q_z, stress tau_xx ... tau_yz) agree within
+    T, p) agree to round-off, and the ensemble means of every other moment field (mean
+    speed, heat flux q_x, q_y, q_z, stress tau_xx ... tau_yz) agree within
     3 standard errors (physical_props.f90:879-1087, 1914-2071)."""
     from concurrent.futures import ThreadPoolExecutor
 
@@ -716,8 +716,8 @@ def test_precision_form_ensemble_cavity(gpulib, pkg):
     """The precision form against FP64 at configuration 3's settings (hard sphere, Kn 0.1,
     lid 0.3, reference-formula samples with ColnRMS 0.001) on a 16 x 16 cavity: after 20
     steps, the ensemble means over 8 seeds of every moment field agree with the FP64
-    ensemble's within 1e-3 of the field's scale in every cell (the benchmark spec's accuracy
-    bar), and their cavity averages within 1e-4."""
+    ensemble's within 1e-3 of the field's scale in every cell (the precision form's
+    accuracy bar), and their cavity averages within 1e-4."""
     import copy
 
     bench = _bench_module()

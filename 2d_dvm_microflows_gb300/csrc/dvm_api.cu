@@ -36,7 +36,6 @@ struct dvm_ctx {
   double* d_eq_cache = nullptr;
   long long* d_cum_eq = nullptr;   // fixed-point CDFs
   long long* d_cum_dev = nullptr;
-  float* d_kin = nullptr;
   int2* d_ref_eq = nullptr;
   int2* d_ref_dev = nullptr;
   CellPlan* d_plan = nullptr;
@@ -184,7 +183,7 @@ void release(dvm_ctx* c) {
   harvest(c);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
   void* bufs[] = {c->d_axes, c->d_speed, c->d_f, c->d_fconv, c->d_props, c->d_eq_cache,
-                  c->d_cum_eq, c->d_cum_dev, c->d_kin, c->d_ref_eq, c->d_ref_dev, c->d_plan,
+                  c->d_cum_eq, c->d_cum_dev, c->d_ref_eq, c->d_ref_dev, c->d_plan,
                   c->d_chunk_off, c->d_total_samples, c->d_ghost, c->d_err, c->d_flush,
                   c->d_axis_tab, c->d_gtab, c->d_trig, c->d_df, c->d_axis_tab_f,
                   c->d_gtab_f, c->d_trig_f, c->d_residual, c->d_cfl};
@@ -479,7 +478,7 @@ int create_context(const dvm_params* params, const dvm_vgrid* vg, cudaStream_t s
   if (params->coll_method != DVM_COLL_NONE) {
     if ((st = dalloc(c, &c->d_eq_cache, C * kEqCache)) ||
         (st = dalloc(c, &c->d_cum_eq, C * (nv + 1))) || (st = dalloc(c, &c->d_cum_dev, C * (nv + 1))) ||
-        (st = dalloc(c, &c->d_kin, C * (nv + 1))) || (st = dalloc(c, &c->d_ref_eq, C * kNRef)) ||
+        (st = dalloc(c, &c->d_ref_eq, C * kNRef)) ||
         (st = dalloc(c, &c->d_ref_dev, C * kNRef)) || (st = dalloc(c, &c->d_plan, C)) ||
         (st = dalloc(c, &c->d_chunk_off, 3 * C + 1)) || (st = dalloc(c, &c->d_total_samples, 2))) {
       release(c);
@@ -677,7 +676,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     CdfArgs ca{};
     ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
     ca.f = c->d_f; ca.props = c->d_props; ca.eq_cache = c->d_eq_cache;
-    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
+    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev;
     ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan;
     ca.pairs = pd; ca.err = c->d_err;
     st = launch(c, DVM_K_CDF, [&] { return launch_cdf(ca, c->stream); });
@@ -693,7 +692,7 @@ int dvm_compute_collision_integral(dvm_ctx* c, uint64_t step, const dvm_pairlist
     a.g = c->g; a.cp = coll_params(c); a.t = c->tabs; a.ncells = c->ncells;
     a.step = static_cast<uint32_t>(step);
     a.step_dev = c->step_dev;
-    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
+    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
     a.chunk_off = c->d_chunk_off; a.pairs = pd; a.err = c->d_err;
     // d_total_samples[1]: the adds into f (df) of this call
@@ -1130,7 +1129,7 @@ void grouped_records(const dvm_batch* b, int g0, int ng, int bps, GroupedStep& g
     CdfArgs& ca = gs.cdf.a[k];
     ca.g = c->g; ca.cp = coll_params(c); ca.ncells = c->ncells;
     ca.f = c->d_f; ca.props = c->d_props; ca.eq_cache = c->d_eq_cache;
-    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev; ca.kin = c->d_kin;
+    ca.cum_eq = c->d_cum_eq; ca.cum_dev = c->d_cum_dev;
     ca.ref_eq = c->d_ref_eq; ca.ref_dev = c->d_ref_dev; ca.plan = c->d_plan; ca.err = c->d_err;
     gs.plan.ncells[k] = c->ncells;
     gs.plan.plan[k] = c->d_plan;
@@ -1139,7 +1138,7 @@ void grouped_records(const dvm_batch* b, int g0, int ng, int bps, GroupedStep& g
     CollideArgs a{};
     a.g = c->g; a.cp = coll_params(c); a.t = c->tabs; a.ncells = c->ncells;
     a.step_dev = c->step_dev;
-    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev; a.kin = c->d_kin;
+    a.f = c->d_f; a.cum_eq = c->d_cum_eq; a.cum_dev = c->d_cum_dev;
     a.ref_eq = c->d_ref_eq; a.ref_dev = c->d_ref_dev; a.plan = c->d_plan;
     a.chunk_off = c->d_chunk_off; a.err = c->d_err;
     gs.col.a[k] = collide_consts(a);
@@ -1360,8 +1359,8 @@ size_t context_bytes(const dvm_params* p, const dvm_vgrid* vg) {
              + sizeof(uint32_t) + nv * sizeof(float2)       // error word, speeds
              + sizeof(unsigned long long);                  // residual
   if (p->coll_method != DVM_COLL_NONE) {
-    b += 2 * C * (nv + 1) * d + C * (nv + 1) * sizeof(float)  // cum_eq, cum_dev, kin,
-         + C * kEqCache * d;                                  // equilibrium cache
+    b += 2 * C * (nv + 1) * d   // cum_eq, cum_dev
+         + C * kEqCache * d;      // equilibrium cache
     b += 2 * C * kNRef * sizeof(int2) + C * sizeof(CellPlan) +
          (3 * C + 1) * sizeof(long long) + 2 * sizeof(long long);
     const size_t nmax = std::max(vg->nx, std::max(vg->ny, vg->nz));

@@ -68,9 +68,10 @@ struct CdfArgs {
   const double* f;          // [C][nv]
   const double* props;      // [C][DVM_NPROP]
   double* eq_cache;         // [C][kEqCache] dens, u, v, temp, w of the cached equilibrium
-  long long* cum_eq;        // [C][nv+1] cumulative f_eq, fixed point (see k_cdf)
-  long long* cum_dev;       // [C][nv+1] cumulative |f - f_eq| (FMC: |f|), fixed point
-  float* kin;               // [C][nv+1] (VR: f - f_eq; FMC: f), read for its sign
+  // [C][nv+1] cumulative sums c(p) through node p - 1, fixed point (see k_cdf), stored as
+  // 2 c(p) + s(p): s(p) = 1 when node p - 1 is negative (VR: f - f_eq < 0; FMC: f < 0)
+  long long* cum_eq;        // f_eq (s = 0)
+  long long* cum_dev;       // |f - f_eq| (FMC: |f|)
   int2* ref_eq;             // [C][1000]
   int2* ref_dev;            // [C][1000]
   CellPlan* plan;           // [C]
@@ -145,7 +146,6 @@ struct CollideArgs {
   double* f;
   const long long* cum_eq;
   const long long* cum_dev;
-  const float* kin;
   const int2* ref_eq;
   const int2* ref_dev;
   const CellPlan* plan;

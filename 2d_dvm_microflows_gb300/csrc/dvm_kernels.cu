@@ -33,7 +33,7 @@ namespace dvm {
 // reference's running sum. The partner search (k_collide) then compares integers only.
 constexpr int kCdfPer = 4;
 constexpr int kCdfPitch = kCdfPer + 1;  // padded row of a lane's values in the transpose
-constexpr int kCdfTrWarp = 2 * 32 * kCdfPitch + (32 * kCdfPitch + 1) / 2;  // words per warp
+constexpr int kCdfTrWarp = 2 * 32 * kCdfPitch;  // words per warp
 constexpr int kCdfCoarseMax = 512;   // entries of the shared-memory coarse index per table
 
 // compute_num_coll_pairs, collisions/collision_utilities.f90:106-140 (n = m); ct is
@@ -125,12 +125,6 @@ __device__ __forceinline__ void node_ijk(int l, int NX, int NXY, float rNX, floa
   i = r - j * NX;
 }
 
-// Sign of v as +-1.0f (the collision kernels read only the sign bit of kin).
-__device__ __forceinline__ float sign_float(double v) {
-  const uint32_t hi = static_cast<uint32_t>(__double_as_longlong(v) >> 32);
-  return __int_as_float(static_cast<int>((hi & 0x80000000u) | 0x3f800000u));
-}
-
 static int sm_count() {
   static int n = 0;
   if (n == 0) {
@@ -188,13 +182,12 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
   __shared__ dfl s_fac[3 * kMaxAxis];
   __shared__ long long s_coarse[2][kCdfCoarseMax + 1];
   __shared__ int s_right[2][kNRef];  // bucket boundaries right(r) of the two tables
-  // per warp: its 4 x 32 cumulative values of both CDFs and signs, transposed so that every
+  // per warp: its 4 x 32 cumulative values of both CDFs (signs in the low bits), transposed so that every
   // store instruction writes 32 consecutive positions
   extern __shared__ __align__(16) long long s_tr[];  // (T / 32) * kCdfTrWarp words
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   long long* tr_e = s_tr + warp * kCdfTrWarp;
   long long* tr_d = tr_e + 32 * kCdfPitch;
-  float* tr_k = reinterpret_cast<float*>(tr_d + 32 * kCdfPitch);
   const GridInfo& g = a.g;
   const int nv = g.nv;
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
@@ -202,7 +195,6 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
   const double* P = a.props + static_cast<size_t>(cell) * DVM_NPROP;
   long long* ce = a.cum_eq + cs;
   long long* cd = a.cum_dev + cs;
-  float* kin = a.kin + cs;
   const bool vr = (a.cp.method == DVM_COLL_VR);
   const int NX = g.nx, NXY = g.nx * g.ny;
   // coarse index: every cstep-th cumulative value, cstep a power of two
@@ -313,6 +305,7 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
     int ii = 0, jj = 0, kk = 0;
     if (vr && l0 < nv) node_ijk(l0, NX, NXY, rNX, rNXY, ii, jj, kk);
     long long pe[kCdfPer], ad[kCdfPer];
+    int sgn = 0;  // bit r: the sign of node l0 + r
 #pragma unroll
     for (int r = 0; r < kCdfPer; ++r) {
       const int l = l0 + r;
@@ -327,11 +320,11 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
                         : to_fixed_f(ev.hi, ke, bad) + to_fixed_f(ev.lo, ke, bad);
           if (recompute) te = E;
           const long long d = F - E;
-          tr_k[lane * kCdfPitch + r] = d < 0 ? -1.f : 1.f;
+          sgn |= (d < 0 ? 1 : 0) << r;
           td = d < 0 ? -d : d;
           if (++ii == NX) { ii = 0; if (++jj == NY) { jj = 0; ++kk; } }
         } else {
-          tr_k[lane * kCdfPitch + r] = sign_float(fv[r]);
+          sgn |= static_cast<int>(static_cast<unsigned long long>(__double_as_longlong(fv[r])) >> 63) << r;
           td = F < 0 ? -F : F;
         }
       }
@@ -344,12 +337,13 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
     block_scan2_i64(oe, od, te, td, &s_scan[0][0]);
     oe += carry_e;
     od += carry_d;
-    // the cumulative sums at positions p = node + 1 and the signs, through the warp's
+    // the cumulative sums at positions p = node + 1 as 2 c + s (s = 1: the node is negative,
+    // the sign that picks the sign of a partner's contribution), through the warp's
     // transpose, and the coarse index
 #pragma unroll
     for (int r = 0; r < kCdfPer; ++r) {
-      tr_e[lane * kCdfPitch + r] = oe + pe[r];
-      tr_d[lane * kCdfPitch + r] = od + ad[r];
+      tr_e[lane * kCdfPitch + r] = (oe + pe[r]) << 1;
+      tr_d[lane * kCdfPitch + r] = ((od + ad[r]) << 1) | ((sgn >> r) & 1);
     }
     __syncwarp();
     const int wbase = base + warp * 32 * kCdfPer;
@@ -362,10 +356,9 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
         const long long ve = tr_e[idx], vd = tr_d[idx];
         if (recompute) ce[p] = ve;
         cd[p] = vd;
-        kin[p] = tr_k[idx];
         if ((p & (cstep - 1)) == 0) {
-          s_coarse[0][p / cstep] = ve;
-          s_coarse[1][p / cstep] = vd;
+          s_coarse[0][p / cstep] = ve >> 1;
+          s_coarse[1][p / cstep] = vd >> 1;
         }
       }
     }
@@ -377,10 +370,12 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
   }
   if (threadIdx.x == 0) {
     if (recompute) ce[0] = 0;
-    cd[0] = 0; kin[0] = 0.f;
+    cd[0] = 0;
     s_coarse[0][0] = 0;
     s_coarse[1][0] = 0;
-    if (carry_e < 0 || carry_d < 0) bad |= DVM_EW_NONFINITE;  // the scale did not hold
+    // the scale did not hold: a sum at or above 2^62 leaves no room for the sign bit
+    if (carry_e < 0 || carry_d < 0 || carry_e >= (1ll << 62) || carry_d >= (1ll << 62))
+      bad |= DVM_EW_NONFINITE;
   }
   __syncthreads();
 
@@ -429,7 +424,7 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
         if (plo[j] < phi[j]) {
           open = true;
           const int mid = (plo[j] + phi[j]) >> 1;
-          if (tg[j] > cum[mid]) plo[j] = mid + 1; else phi[j] = mid;
+          if (tg[j] > (cum[mid] >> 1)) plo[j] = mid + 1; else phi[j] = mid;
         }
       }
       if (!open) break;
@@ -460,7 +455,7 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
     const double qk = ldexp(1.0, -k);
     if (vr) {
       const double dens = P[DVM_P_DENS], temp = P[DVM_P_SPECIES_TEMP];
-      const long long te = recompute ? carry_e : ce[nv];
+      const long long te = recompute ? carry_e : (ce[nv] >> 1);
       const double eq_dens = static_cast<double>(te) * ldexp(1.0, -ke);
       const double neq_dens = static_cast<double>(carry_d) * ldexp(1.0, -ke);
       const double fc = cp.dt * 0.5 / cp.Kn;  // n = m: factor_coeff = dt*0.5/Kn
@@ -647,7 +642,9 @@ __device__ __forceinline__ unsigned long long u53_bits(double R) {
 // of bisection on the wide tail buckets that set a warp's pace. The reference's test
 // cum(idx) < target <= cum(idx+1) is made on the bucket's ends instead, loaded beside the
 // first round: every step keeps cum(lo) < target <= cum(hi) and the sums never decrease,
-// so the test on the ends holds exactly when it holds on the result.
+// so the test on the ends holds exactly when it holds on the result. The stored values
+// are 2 cum + s (s the sign bit of k_cdf); against the doubled target every comparison
+// has the outcome it has on cum itself, so the sign bits change no step.
 // R enters as m = R 2^53 truncated and the test R < tol, made by the caller (on m for the
 // Philox uniforms, on the double for recorded ones).
 __device__ __forceinline__ int referenced_search_fixed(const long long* __restrict__ cum,
@@ -660,8 +657,10 @@ __device__ __forceinline__ int referenced_search_fixed(const long long* __restri
   const int2 lr = __ldg(ref + i - 1);
   const int left = lr.x, right = lr.y;
   if (left == right) return left < n ? left : n - 1;
-  const unsigned long long T = static_cast<unsigned long long>(__ldg(cum + n));
-  const long long adj = static_cast<long long>((__umul64hi(m, T) << 11) | ((m * T) >> 53));
+  const unsigned long long T = static_cast<unsigned long long>(__ldg(cum + n) >> 1);
+  // the target floor(R T), doubled: 2 t > 2 c + s exactly when t > c (s = 0 or 1)
+  const long long adj =
+      static_cast<long long>((__umul64hi(m, T) << 11) | ((m * T) >> 53)) << 1;
   // cum(lo) < adj <= cum(hi) holds for a valid bucket; each step keeps it
   int lo = left, hi = right;
   if (lo >= 0 && hi <= n && lo < hi) {
@@ -1106,10 +1105,12 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
       if (gg < kDoubleTol) continue;
       g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
     }
-    // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old
-    const float* kc = a.kin + cs;
-    const bool negA = (vr && q == 0) ? false : signbit(__ldg(kc + lA + 1));
-    const bool negB = (vr && q == 1) ? false : signbit(__ldg(kc + lB + 1));
+    // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old. The low bit of
+    // the value closing the partner's interval, next to the last values the search read
+    const bool negA =
+        (vr && q == 0) ? false : (__ldg(a.cum_dev + cs + lA + 1) & 1) != 0;
+    const bool negB =
+        (vr && q == 1) ? false : (__ldg(a.cum_dev + cs + lB + 1) & 1) != 0;
     // vr_depletion_routine elastic part (variance_reduction.f90:1157-1166): kin_depl(1) =
     // kin_depl(2) = sA sB factor g^(2-2 omega)
     const double fg = factor * g_sigma;
@@ -1591,9 +1592,8 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
     if (gg < 1e-13f) return;
     g_sigma = (c.vhs == 1.f) ? gg : powf(gg, c.vhs);
   }
-  const float* kc = a.kin + cs;
-  const float sA = (vr && q == 0) ? 1.f : (signbit(__ldg(kc + lA + 1)) ? -1.f : 1.f);
-  const float sB = (vr && q == 1) ? 1.f : (signbit(__ldg(kc + lB + 1)) ? -1.f : 1.f);
+  const float sA = (vr && q == 0) ? 1.f : ((__ldg(a.cum_dev + cs + lA + 1) & 1) ? -1.f : 1.f);
+  const float sB = (vr && q == 1) ? 1.f : ((__ldg(a.cum_dev + cs + lB + 1) & 1) ? -1.f : 1.f);
   const float kin = sA * sB * factor * g_sigma;
   atomicAdd(df + lA, -kin);
   atomicAdd(df + lB, -kin);

@@ -20,10 +20,10 @@
 // error word, which accumulates until a call that waits for its result reads and clears
 // it. Calls that overlap on the GPU (other streams, other host threads) race on the array.
 //
-// Size: 20*(Nv+1) + 16112 bytes per cell (two 64-bit cumulative sums and one FP32 sign
-// array per node, two 1000-entry bucket tables, the equilibrium cache, plan and chunk
-// offsets) plus the grid tables (under 0.2 MB), in 32 MiB: 341 cells of 16^3, 114 of
-// 24^3, 49 of 32^3, 25 of 40^3.
+// Size: 16*(Nv+1) + 16112 bytes per cell (two 64-bit cumulative sums per node, the signs
+// in their low bits, two 1000-entry bucket tables, the equilibrium cache, plan and chunk
+// offsets) plus the grid tables (under 0.2 MB), in 32 MiB: 410 cells of 16^3, 141 of
+// 24^3, 61 of 32^3, 32 of 40^3.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -50,7 +50,7 @@ size_t align256(size_t v) { return (v + 255) & ~static_cast<size_t>(255); }
 // Offsets of every buffer inside the scratch array. The error word comes first, at a fixed
 // offset, so that calls of any size find the bits earlier calls left there.
 struct Layout {
-  size_t err, axes, tabs, gtab, trig, eq_cache, cum_eq, cum_dev, kin, ref_eq, ref_dev, plan,
+  size_t err, axes, tabs, gtab, trig, eq_cache, cum_eq, cum_dev, ref_eq, ref_dev, plan,
       chunk_off, total, end;
 };
 
@@ -68,7 +68,6 @@ Layout layout(int nx, int ny, int nz, int ncells, int gtab_n) {
   L.eq_cache = o; o = align256(o + sizeof(double) * C * kEqCache);
   L.cum_eq = o; o = align256(o + sizeof(double) * C * nv1);
   L.cum_dev = o; o = align256(o + sizeof(double) * C * nv1);
-  L.kin = o; o = align256(o + sizeof(float) * C * nv1);
   L.ref_eq = o; o = align256(o + sizeof(int2) * C * kNRef);
   L.ref_dev = o; o = align256(o + sizeof(int2) * C * kNRef);
   L.plan = o; o = align256(o + sizeof(CellPlan) * C);
@@ -281,7 +280,6 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   ca.eq_cache = d_eq_cache;
   ca.cum_eq = reinterpret_cast<long long*>(base + L.cum_eq);
   ca.cum_dev = reinterpret_cast<long long*>(base + L.cum_dev);
-  ca.kin = reinterpret_cast<float*>(base + L.kin);
   ca.ref_eq = reinterpret_cast<int2*>(base + L.ref_eq);
   ca.ref_dev = reinterpret_cast<int2*>(base + L.ref_dev);
   ca.plan = reinterpret_cast<CellPlan*>(base + L.plan);
@@ -304,7 +302,7 @@ extern "C" int dvm_collide_noalloc(const dvm_params* p, const dvm_vgrid* vg, dou
   a.t.phi_scale = 2.0 * pi / kPiExact;
   a.t.trig = d_trig;
   a.t.two_pi = 2.0 * pi;
-  a.f = f; a.cum_eq = ca.cum_eq; a.cum_dev = ca.cum_dev; a.kin = ca.kin;
+  a.f = f; a.cum_eq = ca.cum_eq; a.cum_dev = ca.cum_dev;
   a.ref_eq = ca.ref_eq; a.ref_dev = ca.ref_dev; a.plan = ca.plan; a.chunk_off = d_chunk;
   a.err = d_err;
   if ((e = launch_collide(a, grid_blocks * collide_blocks_per_sm(collide_smem_bytes(g, a.t)), s)) !=

@@ -393,8 +393,8 @@ int dvm_vis_format_e(double x, int w, int d, char* out, int out_len);
  * memory, f[ncells][Nv] (updated in place) and props[ncells][DVM_NPROP] (the cell
  * properties, e.g. from dvm_get_properties); every intermediate lives in one fixed 32 MiB
  * device array that the library holds on each GPU that loads it, until exit.
- *   Limit: the grid tables (under 0.2 MB) plus 20*(Nv+1) + 16112 bytes per cell must fit
- *   in 32 MiB: at most 341 cells of 16^3, 114 of 24^3, 49 of 32^3 or 25 of 40^3; larger
+ *   Limit: the grid tables (under 0.2 MB) plus 16*(Nv+1) + 16112 bytes per cell must fit
+ *   in 32 MiB: at most 410 cells of 16^3, 141 of 24^3, 61 of 32^3 or 32 of 40^3; larger
  *   problems get DVM_ERR_TOO_LARGE before anything is launched.
  *   The first call on a device looks up that array's address (cudaGetSymbolAddress) with
  *   the device current and keeps it; make that first call before any stream capture, and

@@ -964,7 +964,18 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   return L;
 }
 
-// One CTA of the persistent collide launch: CTA bid of the nblk that walk this grid's chunks.
+// The common configuration: Philox uniforms (no recorded list), one replica, isotropic
+// scattering (alpha = 1) and the tabulated relative speeds of a cubic uniform grid. The
+// collide kernels are also compiled for it alone (kFast): without the other branches they
+// hold fewer registers live (the FP64 kernel spills 52 instead of 136 bytes per thread).
+static bool collide_fast(const CollideArgs& a) {
+  return !a.pairs.active && a.cp.num_repl == 1 && a.t.gtab != nullptr &&
+         !(fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol);
+}
+
+// One CTA of the persistent collide launch: CTA bid of the nblk that walk this grid's
+// chunks; kFast: the configuration of collide_fast.
+template <bool kFast>
 __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
@@ -1027,11 +1038,11 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
   const long long total = a.chunk_off[nent] & kRunMask;
   const int runlen = static_cast<int>(a.chunk_off[nent] >> kRunShift);
   const bool vr = (a.cp.method == DVM_COLL_VR);
-  const int NR = a.cp.num_repl;
+  const int NR = kFast ? 1 : a.cp.num_repl;
   const double vhs = 2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega));
   const double alpha = 0.5 * (a.cp.alpha + a.cp.alpha);
   const double ralpha = 1.0 / alpha;
-  const bool vss = fabs(ralpha - 1.0) > kDoubleTol;
+  const bool vss = kFast ? false : (fabs(ralpha - 1.0) > kDoubleTol);
   const uint32_t step = a.step_dev ? *a.step_dev : a.step;
   uint32_t bad = 0;
   uint32_t nat = 0;  // FP64 adds into f by this thread
@@ -1064,7 +1075,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
 
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
     unsigned long long mA = 0, mB = 0;
-    const bool rec = a.pairs.active;
+    const bool rec = kFast ? false : a.pairs.active;
     if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
@@ -1091,7 +1102,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     node_ijk(lB, NX, NXY, a.rnx, a.rnxy, iB, jB, kB);
     // compute_relative_velocity (collision_utilities.f90:188-218) and g^(2-2 omega)
     double gg, g_sigma;
-    if (gtab) {
+    if (kFast || gtab) {
       const int di = iB - iA, dj = jB - jA, dk = kB - kA;
       const int s2 = di * di + dj * dj + dk * dk;
       if (s2 == 0) continue;  // g < double_tol, variance_reduction.f90:697
@@ -1226,8 +1237,9 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
   add_scatter_count(a.scatter_count, nat);
 }
 
+template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
-  collide_cta(a, blockIdx.x, gridDim.x);
+  collide_cta<kFast>(a, blockIdx.x, gridDim.x);
 }
 
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
@@ -1237,9 +1249,9 @@ size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
 int collide_blocks_per_sm(size_t smem) {
   int n = 0;
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_collide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_collide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(smem));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide, kCollideChunk, smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide<false>, kCollideChunk, smem) !=
       cudaSuccess)
     n = 1;
   cudaGetLastError();  // a refused query must not surface at the next launch
@@ -1264,12 +1276,17 @@ CollideArgs collide_consts(const CollideArgs& a) { return with_collide_consts(a)
 
 cudaError_t launch_collide(const CollideArgs& a, int grid, cudaStream_t s) {
   const size_t smem = collide_smem_bytes(a.g, a.t);
+  const bool fast = collide_fast(a);
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(
-        k_collide, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaError_t e = cudaFuncSetAttribute(
+        k_collide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_collide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
-  k_collide<<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a));
+  if (fast) k_collide<true><<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a));
+  else k_collide<false><<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a));
   return cudaGetLastError();
 }
 
@@ -1541,6 +1558,7 @@ __device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const Co
 }
 
 // One sample of sub-integral q of a cell in FP32, scattered into df (global or shared).
+template <bool kFast>
 __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const CollTablesF& tf,
                                                    const F32Ctx& c, int cell, int q, long long i,
                                                    float factor, float* df, uint32_t& bad,
@@ -1551,7 +1569,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   const size_t cs = static_cast<size_t>(cell) * (nv + 1);
   const bool vr = c.vr;
   unsigned long long mA = 0, mB = 0;
-  const bool rec = a.pairs.active;
+  const bool rec = kFast ? false : a.pairs.active;
   if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, c.step, q, 0u, mA, mB);
   int lA, lB;
   if (rec && a.pairs.glA[q]) {
@@ -1579,7 +1597,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   const float xA = A.v[0][iA], yA = A.v[1][jA], zA = A.v[2][kA];
   const float xB = A.v[0][iB], yB = A.v[1][jB], zB = A.v[2][kB];
   float gg, g_sigma;
-  if (c.gtab) {
+  if (kFast || c.gtab) {
     const int di = iB - iA, dj = jB - jA, dk = kB - kA;
     const int s2 = di * di + dj * dj + dk * dk;
     if (s2 == 0) return;
@@ -1598,8 +1616,8 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   atomicAdd(df + lA, -kin);
   atomicAdd(df + lB, -kin);
   nat += 2u;
-  const int NR = c.NR;
-  const float kr = kin / static_cast<float>(NR);
+  const int NR = kFast ? 1 : c.NR;
+  const float kr = kFast ? kin : kin / static_cast<float>(NR);
   const float vc0 = 0.5f * (xA + xB), vc1 = 0.5f * (yA + yB), vc2 = 0.5f * (zA + zB);
   const float hg = 0.5f * gg;
   for (int r = 0; r < NR; ++r) {
@@ -1628,7 +1646,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
       sphi = cs2.y * ct + cs2.x * st;
     }
     float ux, uy, uz;
-    if (c.vss) {
+    if (!kFast && c.vss) {
       const float ur = fabsf(xA - vc0) + fabsf(xB - vc0);
       const float vr_ = fabsf(yA - vc1) + fabsf(yB - vc1);
       const float wr = fabsf(zA - vc2) + fabsf(zB - vc2);
@@ -1664,6 +1682,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
 }
 
 // One CTA of the persistent FP32 collide launch (as collide_cta).
+template <bool kFast>
 __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const CollTablesF& tf,
                                                 float* __restrict__ dfs, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -1693,7 +1712,7 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
     for (int rr = 0; rr < runlen; ++rr) {
       const long long i = i0 + rr * kChunkSamples;
       if (i >= pl.num[q]) break;
-      collide_sample_f32(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
+      collide_sample_f32<kFast>(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
                          dfs + static_cast<size_t>(cell) * nv, bad, nat);
     }
   }
@@ -1703,19 +1722,20 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
 
 // Three CTAs per SM: 80 registers hold the FP32 sample without spilling (3.25 against
 // 3.32 ms at four CTAs and 64 registers on the benchmark shock).
+template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32(CollideArgs a, CollTablesF tf,
                                                                 float* __restrict__ dfs) {
-  collide_f32_cta(a, tf, dfs, blockIdx.x, gridDim.x);
+  collide_f32_cta<kFast>(a, tf, dfs, blockIdx.x, gridDim.x);
 }
 
 int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
   const int gtab_smem = (t.gtab && static_cast<size_t>(t.gtab_n) * sizeof(float2) <= 48 * 1024) ? 1 : 0;
   const size_t smem = collide_f32_smem_layout(g, t, gtab_smem).total;
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_collide_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_collide_f32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(smem));
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide_f32, kCollideChunk, smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide_f32<false>, kCollideChunk, smem) !=
       cudaSuccess)
     n = 1;
   cudaGetLastError();
@@ -1725,12 +1745,18 @@ int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
 cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, float* df, int grid,
                                cudaStream_t s) {
   const size_t smem = collide_f32_smem_layout(a.g, a.t, tf.gtab_smem).total;
+  const bool fast = collide_fast(a);
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(
-        k_collide_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaError_t e = cudaFuncSetAttribute(k_collide_f32<false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_collide_f32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
-  k_collide_f32<<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a), tf, df);
+  if (fast) k_collide_f32<true><<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a), tf, df);
+  else k_collide_f32<false><<<grid, kCollideChunk, smem, s>>>(with_collide_consts(a), tf, df);
   return cudaGetLastError();
 }
 
@@ -2727,16 +2753,34 @@ cudaError_t launch_plan_grouped(const GroupedPlan& m, cudaStream_t s) {
 // Groups own consecutive CTAs (first[g] <= blockIdx.x < first[g+1]). Three CTAs per SM:
 // the per-group arguments are read by index and need the registers that 80 per thread
 // leave (at 64 the FP64 kernel spills three times as much and runs 25 % slower).
+// kFast when every group has the configuration of collide_fast.
+template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_grouped(const __grid_constant__ GroupedCollide m) {
   const int b = static_cast<int>(blockIdx.x);
   const int gi = group_of(m.first, m.ngroups, b);
-  collide_cta(m.a[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+  collide_cta<kFast>(m.a[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
 }
 
+template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32_grouped(const __grid_constant__ GroupedCollide m) {
   const int b = static_cast<int>(blockIdx.x);
   const int gi = group_of(m.first, m.ngroups, b);
-  collide_f32_cta(m.a[gi], m.tf[gi], m.df[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+  collide_f32_cta<kFast>(m.a[gi], m.tf[gi], m.df[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+}
+
+static bool grouped_fast(const GroupedCollide& m) {
+  for (int gi = 0; gi < m.ngroups; ++gi)
+    if (!collide_fast(m.a[gi])) return false;
+  return true;
+}
+
+static const void* grouped_collide_fn(const GroupedCollide& m, bool fp32) {
+  const bool fast = grouped_fast(m);
+  if (fp32)
+    return fast ? reinterpret_cast<const void*>(k_collide_f32_grouped<true>)
+                : reinterpret_cast<const void*>(k_collide_f32_grouped<false>);
+  return fast ? reinterpret_cast<const void*>(k_collide_grouped<true>)
+              : reinterpret_cast<const void*>(k_collide_grouped<false>);
 }
 
 static size_t collide_grouped_smem(const GroupedCollide& m, bool fp32) {
@@ -2751,8 +2795,7 @@ static size_t collide_grouped_smem(const GroupedCollide& m, bool fp32) {
 
 int collide_grouped_blocks_per_sm(const GroupedCollide& m, bool fp32) {
   const size_t smem = collide_grouped_smem(m, fp32);
-  const void* fn = fp32 ? reinterpret_cast<const void*>(k_collide_f32_grouped)
-                        : reinterpret_cast<const void*>(k_collide_grouped);
+  const void* fn = grouped_collide_fn(m, fp32);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int n = 0;
@@ -2768,16 +2811,21 @@ cudaError_t launch_collide_grouped(const GroupedCollide& m, bool fp32, cudaStrea
   for (int gi = 0; gi < m.ngroups; ++gi)
     if (m.first[gi + 1] <= m.first[gi]) return cudaErrorInvalidValue;  // every group owns a CTA
   const size_t smem = collide_grouped_smem(m, fp32);
-  const void* fn = fp32 ? reinterpret_cast<const void*>(k_collide_f32_grouped)
-                        : reinterpret_cast<const void*>(k_collide_grouped);
+  const void* fn = grouped_collide_fn(m, fp32);
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(smem));
     if (e != cudaSuccess) return e;
   }
   const unsigned grid = static_cast<unsigned>(m.first[m.ngroups]);
-  if (fp32) k_collide_f32_grouped<<<grid, kCollideChunk, smem, s>>>(m);
-  else k_collide_grouped<<<grid, kCollideChunk, smem, s>>>(m);
+  const bool fast = grouped_fast(m);
+  if (fp32) {
+    if (fast) k_collide_f32_grouped<true><<<grid, kCollideChunk, smem, s>>>(m);
+    else k_collide_f32_grouped<false><<<grid, kCollideChunk, smem, s>>>(m);
+  } else {
+    if (fast) k_collide_grouped<true><<<grid, kCollideChunk, smem, s>>>(m);
+    else k_collide_grouped<false><<<grid, kCollideChunk, smem, s>>>(m);
+  }
   return cudaGetLastError();
 }
 

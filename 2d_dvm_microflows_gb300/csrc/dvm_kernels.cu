@@ -756,17 +756,28 @@ __device__ __forceinline__ int round_small(float x) {
 }
 
 // Nearest node, as nearest() but on pair keys.
+// kUniform (a uniform axis): x = factor (u.hi - vmin) is u's position in node units up to
+// a few FP32 roundings (of u.hi - vmin, of the factor, of the product) and the dropped
+// u.lo, each relative to values below about 4 n in node units: under 2e-4 for the longest
+// axis (128 nodes). When x lies within 0.499 of the node it rounds to, no midpoint is
+// nearer and the exact check is skipped; a position clamped to an end node is that node.
+// The other positions (0.2 % of them) are checked on the keys as on any axis.
+template <bool kUniform>
 __device__ __forceinline__ int nearest_d(const SmemAxesD& A, int ax, dfl u, float vmin,
                                          float factor, int& corner, int& bad) {
   const int mx = A.n[ax] - 1;
-  const long long* mid = A.mid[ax];
-  const long long vk = dkey(u);
-  int o = round_small(factor * (u.hi - vmin));
+  const float x = factor * (u.hi - vmin);
+  int o = round_small(x);
+  const bool check = !kUniform || !(fabsf(x - static_cast<float>(o)) < 0.499f);
   o = o < 0 ? 0 : (o > mx ? mx : o);
   if (u.hi != u.hi) bad |= 1;
-  int it = 0;
-  while (o > 0 && vk <= mid[o - 1] && it++ < kMaxAxis) --o;
-  while (o < mx && vk > mid[o] && it++ < kMaxAxis) ++o;
+  if (check) {
+    const long long* mid = A.mid[ax];
+    const long long vk = dkey(u);
+    int it = 0;
+    while (o > 0 && vk <= mid[o - 1] && it++ < kMaxAxis) --o;
+    while (o < mx && vk > mid[o] && it++ < kMaxAxis) ++o;
+  }
   if (o >= mx) { o = mx; corner++; }
   else if (o <= 0) { o = 0; corner++; }
   return o;
@@ -809,14 +820,15 @@ __device__ __forceinline__ void axis_ext(const SmemAxesD& A, int ax, int o, int 
 // compute_remapping_quantities (collisions/remapping.f90:92-394), f_off = 1, in pairs,
 // with the replenishment scatter of the contribution w8 (apply_phi_replenishment,
 // replenishing_collisions.f90:356-434) into f.
+template <bool kUniform>
 __device__ __forceinline__ int remap_scatter_dfl(const GridInfo& g, const SmemAxesD& A, dfl u,
                                                  dfl v, dfl w, float xmin, float ymin,
                                                  float zmin, float xfac, float yfac, float zfac,
                                                  double* f, dfl w8, uint32_t& nat) {
   int corner = 0, bad = 0;
-  int o_i = nearest_d(A, 0, u, xmin, xfac, corner, bad);
-  int o_j = nearest_d(A, 1, v, ymin, yfac, corner, bad);
-  int o_k = nearest_d(A, 2, w, zmin, zfac, corner, bad);
+  int o_i = nearest_d<kUniform>(A, 0, u, xmin, xfac, corner, bad);
+  int o_j = nearest_d<kUniform>(A, 1, v, ymin, yfac, corner, bad);
+  int o_k = nearest_d<kUniform>(A, 2, w, zmin, zfac, corner, bad);
   const int i_max = g.nx - 1, j_max = g.ny - 1, k_max = g.nz - 1;
   if (corner == 3) {
     o_i -= isign1(o_i - 1);
@@ -1221,12 +1233,12 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
       // the second velocity is formed before the first scatter, so that only it (not the
       // centre of mass and the relative half-velocity) stays live across that scatter
       const dfl pB0 = dfl_sub(vc0, ux), pB1 = dfl_sub(vc1, uy), pB2 = dfl_sub(vc2, uz);
-      int rb = remap_scatter_dfl(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
+      int rb = remap_scatter_dfl<kFast>(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
                                  a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0], a.vfac[1],
                                  a.vfac[2], f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_scatter_dfl(g, A, pB0, pB1, pB2, a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0],
+      rb = remap_scatter_dfl<kFast>(g, A, pB0, pB1, pB2, a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0],
                              a.vfac[1], a.vfac[2], f, kr, nat);
       if (rb & 2) bad |= DVM_EW_REMAP;
       if (rb & 1) bad |= DVM_EW_SEARCH;

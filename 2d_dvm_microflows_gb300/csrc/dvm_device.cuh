@@ -45,14 +45,40 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t
                                               uint32_t k0, uint32_t k1, uint32_t out[4]) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
-    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    const uint64_t p0 = static_cast<uint64_t>(0xD2511F53u) * c0;
+    const uint64_t p1 = static_cast<uint64_t>(0xCD9E8D57u) * c2;
+    const uint32_t n0 = static_cast<uint32_t>(p1 >> 32) ^ c1 ^ k0;
+    const uint32_t n2 = static_cast<uint32_t>(p0 >> 32) ^ c3 ^ k1;
+    c0 = n0; c1 = static_cast<uint32_t>(p1); c2 = n2; c3 = static_cast<uint32_t>(p0);
     k0 += 0x9E3779B9u;
     k1 += 0xBB67AE85u;
   }
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// philox4x32_10 with the key schedule given: rk[2 r], rk[2 r + 1] are the keys of round r
+// (k0 + r 0x9E3779B9, k1 + r 0xBB67AE85), formed once on the host; kernels that hold rk
+// in their launch parameters read each key as an operand instead of adding it up.
+__device__ __forceinline__ void philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2,
+                                                 uint32_t c3, const uint32_t (&rk)[20],
+                                                 uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = static_cast<uint64_t>(0xD2511F53u) * c0;
+    const uint64_t p1 = static_cast<uint64_t>(0xCD9E8D57u) * c2;
+    const uint32_t n0 = static_cast<uint32_t>(p1 >> 32) ^ c1 ^ rk[2 * r];
+    const uint32_t n2 = static_cast<uint32_t>(p0 >> 32) ^ c3 ^ rk[2 * r + 1];
+    c0 = n0; c1 = static_cast<uint32_t>(p1); c2 = n2; c3 = static_cast<uint32_t>(p0);
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// The key schedule of a seed (k0, k1 = its low and high words).
+__host__ __device__ inline void philox_key_schedule(uint64_t seed, uint32_t (&rk)[20]) {
+  for (int r = 0; r < 10; ++r) {
+    rk[2 * r] = static_cast<uint32_t>(seed) + static_cast<uint32_t>(r) * 0x9E3779B9u;
+    rk[2 * r + 1] = static_cast<uint32_t>(seed >> 32) + static_cast<uint32_t>(r) * 0xBB67AE85u;
+  }
 }
 
 // m 2^-53 for a 53-bit integer m, built from the bits (exact; no FP64 op).
@@ -76,6 +102,17 @@ __device__ __forceinline__ void philox_u53x2(uint64_t seed, uint32_t sample, uin
   uint32_t o[4];
   philox4x32_10(sample, cell, step, (sub & 3u) | (call << 2), static_cast<uint32_t>(seed),
                 static_cast<uint32_t>(seed >> 32), o);
+  m0 = ((static_cast<uint64_t>(o[1]) << 32) | o[0]) >> 11;
+  m1 = ((static_cast<uint64_t>(o[3]) << 32) | o[2]) >> 11;
+}
+
+// philox_u53x2 from a key schedule.
+__device__ __forceinline__ void philox_u53x2_rk(const uint32_t (&rk)[20], uint32_t sample,
+                                                uint32_t cell, uint32_t step, uint32_t sub,
+                                                uint32_t call, unsigned long long& m0,
+                                                unsigned long long& m1) {
+  uint32_t o[4];
+  philox4x32_10_rk(sample, cell, step, (sub & 3u) | (call << 2), rk, o);
   m0 = ((static_cast<uint64_t>(o[1]) << 32) | o[0]) >> 11;
   m1 = ((static_cast<uint64_t>(o[3]) << 32) | o[2]) >> 11;
 }

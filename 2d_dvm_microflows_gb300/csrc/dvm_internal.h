@@ -157,6 +157,7 @@ struct CollideArgs {
   // the kernels read them as parameters rather than hold them in registers
   float vmin[3], vfac[3];  // axis minima and nearest-node factors
   float rnx, rnxy;         // 1 / NX and 1 / (NX NY)
+  uint32_t rk[20];         // Philox key schedule of cp.seed (philox_key_schedule)
 };
 
 // 2-D wall ghost slabs: one per (wall side, position along the wall).

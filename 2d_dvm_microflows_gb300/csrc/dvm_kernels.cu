@@ -985,9 +985,20 @@ static bool collide_fast(const CollideArgs& a) {
          !(fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol);
 }
 
+// The two 53-bit Philox integers of a sample's counter: from the key schedule in the
+// launch parameters (kKeys; the single-context kernels, where each key is an operand) or
+// from the seed (the grouped kernels, whose per-group parameters are read by index).
+template <bool kKeys>
+__device__ __forceinline__ void sample_u53x2(const CollideArgs& a, uint32_t i, uint32_t cell,
+                                             uint32_t step, uint32_t q, uint32_t call,
+                                             unsigned long long& m0, unsigned long long& m1) {
+  if (kKeys) philox_u53x2_rk(a.rk, i, cell, step, q, call, m0, m1);
+  else philox_u53x2(a.cp.seed, i, cell, step, q, call, m0, m1);
+}
+
 // One CTA of the persistent collide launch: CTA bid of the nblk that walk this grid's
-// chunks; kFast: the configuration of collide_fast.
-template <bool kFast>
+// chunks; kFast: the configuration of collide_fast; kKeys: as sample_u53x2.
+template <bool kFast, bool kKeys>
 __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   const GridInfo& g = a.g;
@@ -1088,7 +1099,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
     unsigned long long mA = 0, mB = 0;
     const bool rec = kFast ? false : a.pairs.active;
-    if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
+    if (!rec) sample_u53x2<kKeys>(a, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
       lA = a.pairs.glA[q][i];
@@ -1167,7 +1178,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
         rcos_rec = a.pairs.rcos[q][i * NR + r];
         mphi = u53_bits(rphi_rec);
       } else {
-        philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
+        sample_u53x2<kKeys>(a, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
       }
       dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
       if (vss) {
@@ -1251,7 +1262,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
 
 template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
-  collide_cta<kFast>(a, blockIdx.x, gridDim.x);
+  collide_cta<kFast, true>(a, blockIdx.x, gridDim.x);
 }
 
 size_t collide_smem_bytes(const GridInfo& g, const CollTables& t) {
@@ -1281,6 +1292,7 @@ static CollideArgs with_collide_consts(const CollideArgs& a) {
   b.vfac[2] = static_cast<float>(a.g.zv_factor);
   b.rnx = 1.f / static_cast<float>(a.g.nx);
   b.rnxy = 1.f / static_cast<float>(a.g.nx * a.g.ny);
+  philox_key_schedule(a.cp.seed, b.rk);
   return b;
 }
 
@@ -1570,7 +1582,7 @@ __device__ __forceinline__ F32Ctx load_f32_tables(const CollideArgs& a, const Co
 }
 
 // One sample of sub-integral q of a cell in FP32, scattered into df (global or shared).
-template <bool kFast>
+template <bool kFast, bool kKeys>
 __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const CollTablesF& tf,
                                                    const F32Ctx& c, int cell, int q, long long i,
                                                    float factor, float* df, uint32_t& bad,
@@ -1582,7 +1594,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
   const bool vr = c.vr;
   unsigned long long mA = 0, mB = 0;
   const bool rec = kFast ? false : a.pairs.active;
-  if (!rec) philox_u53x2(a.cp.seed, static_cast<uint32_t>(i), cell, c.step, q, 0u, mA, mB);
+  if (!rec) sample_u53x2<kKeys>(a, static_cast<uint32_t>(i), cell, c.step, q, 0u, mA, mB);
   int lA, lB;
   if (rec && a.pairs.glA[q]) {
     lA = a.pairs.glA[q][i];
@@ -1640,8 +1652,13 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
     } else {
       // the top 24 bits of the two uniforms the FP64 form draws from this counter
       uint32_t o[4];
-      philox4x32_10(static_cast<uint32_t>(i), cell, c.step, (q & 3u) | ((1u + r) << 2),
-                    static_cast<uint32_t>(a.cp.seed), static_cast<uint32_t>(a.cp.seed >> 32), o);
+      if (kKeys)
+        philox4x32_10_rk(static_cast<uint32_t>(i), cell, c.step, (q & 3u) | ((1u + r) << 2),
+                         a.rk, o);
+      else
+        philox4x32_10(static_cast<uint32_t>(i), cell, c.step, (q & 3u) | ((1u + r) << 2),
+                      static_cast<uint32_t>(a.cp.seed), static_cast<uint32_t>(a.cp.seed >> 32),
+                      o);
       rphi = static_cast<float>(o[1] >> 8) * 0x1.0p-24f;
       rcos = static_cast<float>(o[3] >> 8) * 0x1.0p-24f;
     }
@@ -1694,7 +1711,7 @@ __device__ __forceinline__ void collide_sample_f32(const CollideArgs& a, const C
 }
 
 // One CTA of the persistent FP32 collide launch (as collide_cta).
-template <bool kFast>
+template <bool kFast, bool kKeys>
 __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const CollTablesF& tf,
                                                 float* __restrict__ dfs, int bid, int nblk) {
   extern __shared__ __align__(16) unsigned char s_raw[];
@@ -1724,7 +1741,7 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
     for (int rr = 0; rr < runlen; ++rr) {
       const long long i = i0 + rr * kChunkSamples;
       if (i >= pl.num[q]) break;
-      collide_sample_f32<kFast>(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
+      collide_sample_f32<kFast, kKeys>(a, tf, c, cell, q, i, static_cast<float>(pl.factor[q]),
                          dfs + static_cast<size_t>(cell) * nv, bad, nat);
     }
   }
@@ -1737,7 +1754,7 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
 template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32(CollideArgs a, CollTablesF tf,
                                                                 float* __restrict__ dfs) {
-  collide_f32_cta<kFast>(a, tf, dfs, blockIdx.x, gridDim.x);
+  collide_f32_cta<kFast, true>(a, tf, dfs, blockIdx.x, gridDim.x);
 }
 
 int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
@@ -2770,14 +2787,14 @@ template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_grouped(const __grid_constant__ GroupedCollide m) {
   const int b = static_cast<int>(blockIdx.x);
   const int gi = group_of(m.first, m.ngroups, b);
-  collide_cta<kFast>(m.a[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+  collide_cta<kFast, false>(m.a[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
 }
 
 template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32_grouped(const __grid_constant__ GroupedCollide m) {
   const int b = static_cast<int>(blockIdx.x);
   const int gi = group_of(m.first, m.ngroups, b);
-  collide_f32_cta<kFast>(m.a[gi], m.tf[gi], m.df[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
+  collide_f32_cta<kFast, false>(m.a[gi], m.tf[gi], m.df[gi], b - m.first[gi], m.first[gi + 1] - m.first[gi]);
 }
 
 static bool grouped_fast(const GroupedCollide& m) {

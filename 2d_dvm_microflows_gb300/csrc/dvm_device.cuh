@@ -117,6 +117,17 @@ __device__ __forceinline__ void philox_u53x2_rk(const uint32_t (&rk)[20], uint32
   m1 = ((static_cast<uint64_t>(o[3]) << 32) | o[2]) >> 11;
 }
 
+// An out-of-line copy of philox_u53x2_rk, for a kernel that draws from two places in its
+// sample loop: one copy of the ten rounds in its code instead of two inlined ones (the
+// FP64 collide kernel waits on instruction fetch otherwise).
+static __device__ __noinline__ void philox_u53x2_rk_call(const uint32_t (&rk)[20],
+                                                         uint32_t sample, uint32_t cell,
+                                                         uint32_t step, uint32_t sub,
+                                                         uint32_t call, unsigned long long& m0,
+                                                         unsigned long long& m1) {
+  philox_u53x2_rk(rk, sample, cell, step, sub, call, m0, m1);
+}
+
 // u < kDoubleTol for u = m 2^-53 exactly when m < kTolU53 = ceil(kDoubleTol 2^53).
 constexpr double kTolScaled = kDoubleTol * 9007199254740992.0;
 constexpr unsigned long long kTolU53 =

@@ -987,12 +987,14 @@ static bool collide_fast(const CollideArgs& a) {
 
 // The two 53-bit Philox integers of a sample's counter: from the key schedule in the
 // launch parameters (kKeys; the single-context kernels, where each key is an operand) or
-// from the seed (the grouped kernels, whose per-group parameters are read by index).
-template <bool kKeys>
+// from the seed (the grouped kernels, whose per-group parameters are read by index);
+// kCall: through the out-of-line copy of the rounds.
+template <bool kKeys, bool kCall = false>
 __device__ __forceinline__ void sample_u53x2(const CollideArgs& a, uint32_t i, uint32_t cell,
                                              uint32_t step, uint32_t q, uint32_t call,
                                              unsigned long long& m0, unsigned long long& m1) {
-  if (kKeys) philox_u53x2_rk(a.rk, i, cell, step, q, call, m0, m1);
+  if (kKeys && kCall) philox_u53x2_rk_call(a.rk, i, cell, step, q, call, m0, m1);
+  else if (kKeys) philox_u53x2_rk(a.rk, i, cell, step, q, call, m0, m1);
   else philox_u53x2(a.cp.seed, i, cell, step, q, call, m0, m1);
 }
 
@@ -1099,7 +1101,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     // partners: pick_collision_partner x2 (collision_utilities.f90:142-186)
     unsigned long long mA = 0, mB = 0;
     const bool rec = kFast ? false : a.pairs.active;
-    if (!rec) sample_u53x2<kKeys>(a, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
+    if (!rec) sample_u53x2<kKeys, true>(a, static_cast<uint32_t>(i), cell, step, q, 0u, mA, mB);
     int lA, lB;
     if (rec && a.pairs.glA[q]) {
       lA = a.pairs.glA[q][i];
@@ -1178,7 +1180,7 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
         rcos_rec = a.pairs.rcos[q][i * NR + r];
         mphi = u53_bits(rphi_rec);
       } else {
-        sample_u53x2<kKeys>(a, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
+        sample_u53x2<kKeys, true>(a, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
       }
       dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
       if (vss) {
@@ -1241,18 +1243,21 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
         uy = dfl_mul(hs, sphi);
         uz = dfl_mul(hg, ct);
       }
-      // the second velocity is formed before the first scatter, so that only it (not the
-      // centre of mass and the relative half-velocity) stays live across that scatter
+      // both velocities are formed before the first scatter (the centre of mass and the
+      // relative half-velocity are not live across it) and go through one copy of the
+      // remap in a two-pass loop: two inlined copies made the kernel wait on instruction
+      // fetch
+      dfl q0 = dfl_add(vc0, ux), q1 = dfl_add(vc1, uy), q2 = dfl_add(vc2, uz);
       const dfl pB0 = dfl_sub(vc0, ux), pB1 = dfl_sub(vc1, uy), pB2 = dfl_sub(vc2, uz);
-      int rb = remap_scatter_dfl<kFast>(g, A, dfl_add(vc0, ux), dfl_add(vc1, uy), dfl_add(vc2, uz),
-                                 a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0], a.vfac[1],
-                                 a.vfac[2], f, kr, nat);
-      if (rb & 2) bad |= DVM_EW_REMAP;
-      if (rb & 1) bad |= DVM_EW_SEARCH;
-      rb = remap_scatter_dfl<kFast>(g, A, pB0, pB1, pB2, a.vmin[0], a.vmin[1], a.vmin[2], a.vfac[0],
-                             a.vfac[1], a.vfac[2], f, kr, nat);
-      if (rb & 2) bad |= DVM_EW_REMAP;
-      if (rb & 1) bad |= DVM_EW_SEARCH;
+#pragma unroll 1
+      for (int side = 0; side < 2; ++side) {
+        const int rb = remap_scatter_dfl<kFast>(g, A, q0, q1, q2, a.vmin[0], a.vmin[1],
+                                                a.vmin[2], a.vfac[0], a.vfac[1], a.vfac[2], f,
+                                                kr, nat);
+        if (rb & 2) bad |= DVM_EW_REMAP;
+        if (rb & 1) bad |= DVM_EW_SEARCH;
+        q0 = pB0; q1 = pB1; q2 = pB2;
+      }
     }
     }  // the run's chunks
   }

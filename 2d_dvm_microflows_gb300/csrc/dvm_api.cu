@@ -354,7 +354,9 @@ int build_collision_tables(dvm_ctx* c) {
     const size_t n = static_cast<size_t>(c->ncells) * c->g.nv;
     if ((st = dalloc(c, &c->d_df, n))) return st;
     cudaMemsetAsync(c->d_df, 0, n * sizeof(float), c->stream);
-    c->collide_f32_grid = c->num_sms * collide_f32_blocks_per_sm(c->g, c->tabs);
+    const bool fast = c->p.num_repl == 1 && c->tabs.gtab != nullptr &&
+                      !(std::fabs(1.0 / (0.5 * (c->p.alpha + c->p.alpha)) - 1.0) > kDoubleTol);
+    c->collide_f32_grid = c->num_sms * collide_f32_blocks_per_sm(c->g, c->tabs, fast);
   }
   // the host tables above are staged before they go out of scope
   return cuda_status(cudaStreamSynchronize(c->stream));

@@ -263,7 +263,9 @@ cudaError_t launch_collide_f32(const CollideArgs& a, const CollTablesF& tf, floa
                                cudaStream_t s);
 cudaError_t launch_project(const ProjectArgs& a, cudaStream_t s);
 
-int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t);
+// CTAs per SM of the FP32 collide kernel; fast: of its copy for the common configuration
+// (collide_fast without the recorded-list test, which the test hooks switch per call).
+int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t, bool fast);
 cudaError_t launch_wall_flux(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_wall_specular(const WallArgs& a, cudaStream_t s);
 cudaError_t launch_convect2d(const Convect2DArgs& a, int ncells, cudaStream_t s);

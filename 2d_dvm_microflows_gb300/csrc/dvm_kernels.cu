@@ -1754,23 +1754,25 @@ __device__ __forceinline__ void collide_f32_cta(const CollideArgs& a, const Coll
   add_scatter_count(a.scatter_count, nat);
 }
 
-// Three CTAs per SM: 80 registers hold the FP32 sample without spilling (3.25 against
-// 3.32 ms at four CTAs and 64 registers on the benchmark shock).
+// The general kernel at three CTAs per SM: 80 registers hold the FP32 sample without
+// spilling (3.25 against 3.32 ms at four CTAs and 64 registers on the benchmark shock).
+// The common configuration's copy at four: 3.09 ms on the shock either way, 0.231 against
+// 0.252 ms on the cavity, whose collide waits on DRAM and needs the warps.
 template <bool kFast>
-__global__ void __launch_bounds__(kCollideChunk, 3) k_collide_f32(CollideArgs a, CollTablesF tf,
+__global__ void __launch_bounds__(kCollideChunk, kFast ? 4 : 3) k_collide_f32(CollideArgs a, CollTablesF tf,
                                                                 float* __restrict__ dfs) {
   collide_f32_cta<kFast, true>(a, tf, dfs, blockIdx.x, gridDim.x);
 }
 
-int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t) {
+int collide_f32_blocks_per_sm(const GridInfo& g, const CollTables& t, bool fast) {
   const int gtab_smem = (t.gtab && static_cast<size_t>(t.gtab_n) * sizeof(float2) <= 48 * 1024) ? 1 : 0;
   const size_t smem = collide_f32_smem_layout(g, t, gtab_smem).total;
+  const void* fn = fast ? reinterpret_cast<const void*>(k_collide_f32<true>)
+                        : reinterpret_cast<const void*>(k_collide_f32<false>);
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_collide_f32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(smem));
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_collide_f32<false>, kCollideChunk, smem) !=
-      cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kCollideChunk, smem) != cudaSuccess)
     n = 1;
   cudaGetLastError();
   return n > 0 ? n : 1;

@@ -1265,6 +1265,10 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
   add_scatter_count(a.scatter_count, nat);
 }
 
+// Four CTAs per SM (64 registers): the kernel needs the warps more than the registers
+// (three CTAs at 80 registers measured 5.55 against 5.47 ms for the general kernel, 4.34
+// against 4.19 ms for the common configuration's copy on the benchmark shock; five at 48
+// registers 5.22 against 5.05 ms).
 template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 4) k_collide(CollideArgs a) {
   collide_cta<kFast, true>(a, blockIdx.x, gridDim.x);
@@ -2788,8 +2792,10 @@ cudaError_t launch_plan_grouped(const GroupedPlan& m, cudaStream_t s) {
 
 // Groups own consecutive CTAs (first[g] <= blockIdx.x < first[g+1]). Three CTAs per SM:
 // the per-group arguments are read by index and need the registers that 80 per thread
-// leave (at 64 the FP64 kernel spills three times as much and runs 25 % slower).
-// kFast when every group has the configuration of collide_fast.
+// leave (at 64 the general FP64 kernel spills three times as much and runs 25 % slower;
+// the common configuration's copies at four measured 9.04 against 7.96 ms (FP64) and
+// 6.2 against 5.3 ms (FP32) per batch step). kFast when every group has the
+// configuration of collide_fast.
 template <bool kFast>
 __global__ void __launch_bounds__(kCollideChunk, 3) k_collide_grouped(const __grid_constant__ GroupedCollide m) {
   const int b = static_cast<int>(blockIdx.x);

@@ -190,6 +190,142 @@ __device__ __forceinline__ double dfl_mul_to_double(dfl a, dfl b) {
   return static_cast<double>(p) + dbl_from_normal_float(e);
 }
 
+__device__ __forceinline__ dfl dfl_scale(dfl a, float s) {  // s a power of two
+  return dfl_make(a.hi * s, a.lo * s);
+}
+
+// Division with one correction step (Karp-Markstein style): q1 = a/b in FP32, the
+// remainder a - q1 b formed exactly by FMA, divided again (about 2^-45 relative).
+__device__ __forceinline__ dfl dfl_div(dfl a, dfl b) {
+  const float rb = rcp_approx(b.hi);
+  const float q1 = __fmul_rn(a.hi, rb);
+  const float p = __fmul_rn(q1, b.hi);
+  const float e = __fmaf_rn(q1, b.hi, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), __fmaf_rn(q1, b.lo, e)), a.lo);
+  const float q2 = __fmul_rn(r, rb);
+  return dfl_norm(q1, q2);
+}
+
+// Square root from the reciprocal square root estimate y: s = a y, then s + (a - s^2) y / 2.
+__device__ __forceinline__ dfl dfl_sqrt(dfl a) {
+  if (!(a.hi > 0.f)) return dfl_make(0.f, 0.f);
+  const float y = rsqrt_approx(a.hi);
+  const float s = __fmul_rn(a.hi, y);
+  const float p = __fmul_rn(s, s);
+  const float e = __fmaf_rn(s, s, -p);
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
+  return dfl_norm(s, __fmul_rn(r, 0.5f * y));
+}
+
+// ---- x^q for a positive pair: x^q = 2^(q log2 x) ------------------------------------------
+// The relative speed's g^(2 - 2 omega) on grids without a speed table: an FP64 pow per
+// sample costs the collide kernel as much as the rest of its work together, the FP64 pipe
+// issuing at 1/64 of the FP32 rate. Methods (from the mathematics, not from any library):
+//   log2 x = e + log2 m: x = 2^e m with m in [sqrt(1/2), sqrt(2)); ln m = 2 atanh s,
+//     s = (m - 1)/(m + 1), |s| <= 0.1716, t = s^2 <= 0.0295, ln m = 2 s (1 + t/3 + t^2/5 +
+//     ... + t^9/19); the terms from t^4 on (below 7e-8 of the sum) in FP32, the others in
+//     pairs.
+//   q log2 x = q e + q log2 m: q is held as three floats (all 53 bits of the double), so
+//     q e is formed exactly by error-free products and only its fraction and q log2 m
+//     (each below 1 in size) go through pair arithmetic.
+//   2^y: y = n + j/32 + u with integer n, j in [-16, 16] and |u| <= 1/64; 2^y =
+//     2^n 2^(j/32) e^v, v = u ln 2, |v| <= 0.0109, 2^(j/32) from a 33-entry pair table and
+//     e^v by its Taylor series to v^6 (v^4 on in FP32) -- the table-driven reduction of
+//     P. T. P. Tang, ACM Trans. Math. Softw. 15 (1989) 144-157.
+// Each pair step rounds at about 2^-48 of a value below 1 in size: the result is within a
+// few 1e-15 relative whatever the size of q log2 x.
+constexpr int kExp2TabN = 33;  // 2^(j/32), j = -16 .. 16
+
+// Entry t of the table (2^((t - 16)/32) as a normalised pair) from the FP64 exp2.
+__device__ __forceinline__ float2 exp2_table_entry(int t) {
+  const dfl v = dfl_from_double(exp2(static_cast<double>(t - 16) * 0.03125));
+  const dfl n = dfl_norm(v.hi, v.lo);
+  return make_float2(n.hi, n.lo);
+}
+
+// A double as three floats whose sum is the double (exactly, for normal results).
+struct flt3 {
+  float hi, mid, lo;
+};
+
+__device__ __forceinline__ flt3 flt3_from_double(double q) {
+  flt3 r;
+  r.hi = __double2float_rn(q);
+  const double r1 = q - static_cast<double>(r.hi);
+  r.mid = __double2float_rn(r1);
+  r.lo = __double2float_rn(r1 - static_cast<double>(r.mid));
+  return r;
+}
+
+__device__ __forceinline__ float pow2f_exact(int a) {  // 2^a, -126 <= a <= 127
+  return __int_as_float((a + 127) << 23);
+}
+
+// log2 m of a pair x with a positive normal hi, x = 2^e m, m in [sqrt(1/2), sqrt(2)).
+__device__ __forceinline__ dfl dfl_log2_split(dfl x, int& e) {
+  const int bits = __float_as_int(x.hi);
+  e = ((bits >> 23) & 0xff) - 127;
+  const float mh = __int_as_float((bits & 0x007fffff) | 0x3f800000);  // in [1, 2)
+  if (mh > 1.41421354f) e += 1;                                       // m < sqrt(2)
+  const float sc = pow2f_exact(-e);
+  const dfl m = dfl_make(x.hi * sc, x.lo * sc);                       // exact
+  const dfl one = dfl_make(1.f, 0.f);
+  const dfl s = dfl_div(dfl_sub(m, one), dfl_add(m, one));
+  const dfl t = dfl_mul(s, s);
+  const float th = t.hi;
+  // 1/9 + t/11 + ... + t^5/19 in FP32
+  const float r4 = fmaf(th, fmaf(th, fmaf(th, fmaf(th, fmaf(th, 1.f / 19.f, 1.f / 17.f),
+                                                   1.f / 15.f), 1.f / 13.f), 1.f / 11.f),
+                        1.f / 9.f);
+  const dfl c3 = dfl_make(0x1.555556p-2f, -0x1.555556p-27f);
+  const dfl c5 = dfl_make(0x1.99999ap-3f, -0x1.99999ap-29f);
+  const dfl c7 = dfl_make(0x1.24924ap-3f, -0x1.b6db6ep-28f);
+  const dfl inv_ln2 = dfl_make(0x1.715476p+0f, 0x1.4ae0c0p-26f);
+  const dfl A = dfl_add(c7, dfl_mul(t, dfl_make(r4, 0.f)));
+  const dfl B = dfl_add(c5, dfl_mul(t, A));
+  const dfl P = dfl_add(c3, dfl_mul(t, B));
+  const dfl s2 = dfl_scale(s, 2.f);
+  const dfl lnm = dfl_add(s2, dfl_mul(dfl_mul(s2, t), P));
+  return dfl_mul(lnm, inv_ln2);
+}
+
+// 2^(n + y) for an integer n and a pair |y| below a few units, n + y within [-126, 127].
+__device__ __forceinline__ dfl dfl_exp2_split(int n, dfl y, const float2* tab) {
+  const float ny = rintf(y.hi);
+  const dfl f = dfl_sub(y, dfl_make(ny, 0.f));
+  const float j = rintf(f.hi * 32.f);
+  const dfl u = dfl_sub(f, dfl_make(j * 0.03125f, 0.f));
+  const dfl v = dfl_mul(u, dfl_make(0x1.62e430p-1f, -0x1.05c610p-29f));  // u ln 2
+  const dfl v2 = dfl_mul(v, v);
+  const float vh = v.hi;
+  const float tail = v2.hi * v2.hi * fmaf(vh, fmaf(vh, 1.f / 720.f, 1.f / 120.f), 1.f / 24.f);
+  const dfl v3s = dfl_mul(dfl_mul(v2, v), dfl_make(0x1.555556p-3f, -0x1.555556p-28f));  // v^3/6
+  const dfl ev = dfl_add(dfl_add(dfl_make(1.f, 0.f), v),
+                         dfl_add(dfl_scale(v2, 0.5f), dfl_add(v3s, dfl_make(tail, 0.f))));
+  const int ji = min(max(static_cast<int>(j) + 16, 0), kExp2TabN - 1);
+  const float2 T = tab[ji];
+  const dfl R = dfl_mul(dfl_make(T.x, T.y), ev);
+  const float sc = pow2f_exact(n + static_cast<int>(ny));
+  return dfl_make(R.hi * sc, R.lo * sc);
+}
+
+// x^q for a pair x with a positive normal hi and q given as three floats.
+__device__ __forceinline__ dfl dfl_pow(dfl x, flt3 q, const float2* tab) {
+  int e;
+  const dfl lm = dfl_log2_split(x, e);
+  // q e exactly: hi and mid products with their FMA error terms, lo e below 2^-70 of q e
+  const float fe = static_cast<float>(e);
+  const float p1 = q.hi * fe, e1 = fmaf(q.hi, fe, -p1);
+  const float p2 = q.mid * fe, e2 = fmaf(q.mid, fe, -p2);
+  const float n1 = rintf(p1);  // |p1| < 2^24: p1 - n1 is exact
+  dfl y = dfl_make(p1 - n1, 0.f);
+  y = dfl_add(y, dfl_make(p2, 0.f));
+  y = dfl_add(y, dfl_make(e1, 0.f));
+  y = dfl_add(y, dfl_make(e2 + q.lo * fe, 0.f));
+  y = dfl_add(y, dfl_mul(lm, dfl_norm(q.hi, q.mid)));
+  return dfl_exp2_split(static_cast<int>(n1), y, tab);
+}
+
 // A running sum, renormalised after every term so that lo stays within half an ulp of hi
 // and each term adds at most about 2^-48 of the sum in rounding.
 struct dacc {

@@ -719,33 +719,6 @@ __device__ __forceinline__ int dfl_isgn(dfl a) {
   return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? -1 : 1;
 }
 
-__device__ __forceinline__ dfl dfl_scale(dfl a, float s) {  // s a power of two
-  return dfl_make(a.hi * s, a.lo * s);
-}
-
-// Division with one correction step (Karp-Markstein style): q1 = a/b in FP32, the
-// remainder a - q1 b formed exactly by FMA, divided again (about 2^-45 relative).
-__device__ __forceinline__ dfl dfl_div(dfl a, dfl b) {
-  const float rb = rcp_approx(b.hi);
-  const float q1 = __fmul_rn(a.hi, rb);
-  const float p = __fmul_rn(q1, b.hi);
-  const float e = __fmaf_rn(q1, b.hi, -p);
-  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), __fmaf_rn(q1, b.lo, e)), a.lo);
-  const float q2 = __fmul_rn(r, rb);
-  return dfl_norm(q1, q2);
-}
-
-// Square root from the reciprocal square root estimate y: s = a y, then s + (a - s^2) y / 2.
-__device__ __forceinline__ dfl dfl_sqrt(dfl a) {
-  if (!(a.hi > 0.f)) return dfl_make(0.f, 0.f);
-  const float y = rsqrt_approx(a.hi);
-  const float s = __fmul_rn(a.hi, y);
-  const float p = __fmul_rn(s, s);
-  const float e = __fmaf_rn(s, s, -p);
-  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
-  return dfl_norm(s, __fmul_rn(r, 0.5f * y));
-}
-
 // Nearest integer (ties to even) of x, as __float2int_rn for |x| <= 2^22, by the FP32 adder:
 // x + 1.5 2^23 lies in [2^23, 2^24], where the float spacing is 1 and the even offset keeps
 // the parity of the tie rule. Larger |x| (and NaN) are clamped to +-2^22 first; the callers
@@ -959,7 +932,7 @@ struct ChunkWalk {
 };
 
 struct CollideSmem {
-  size_t axes, axes_d, keys, tabs, gtab, trig, total;
+  size_t axes, axes_d, keys, tabs, gtab, trig, exp2tab, total;
 };
 
 __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, const CollTables& t) {
@@ -972,7 +945,10 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   L.gtab = L.tabs + 3 * static_cast<size_t>(t.nmax) * sizeof(AxisEntryD);
   L.gtab = (L.gtab + 15) & ~static_cast<size_t>(15);  // double2 needs 16-byte alignment
   L.trig = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
-  L.total = L.trig + static_cast<size_t>(kTrigN) * sizeof(float4);
+  L.exp2tab = L.trig + static_cast<size_t>(kTrigN) * sizeof(float4);
+  // without a speed table: 2^(j/32) and, after it, the exponent (2 - 2 omega)/2 as three
+  // floats
+  L.total = L.exp2tab + (t.gtab ? 0 : static_cast<size_t>(kExp2TabN + 2) * sizeof(float2));
   return L;
 }
 
@@ -1042,6 +1018,18 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     const dfl c = dfl_from_double(cs.x), sn = dfl_from_double(cs.y);
     const dfl cn = dfl_norm(c.hi, c.lo), snn = dfl_norm(sn.hi, sn.lo);
     strig[t] = make_float4(cn.hi, cn.lo, snn.hi, snn.lo);
+  }
+  float2* sexp2 = reinterpret_cast<float2*>(s_raw + L.exp2tab);
+  if (!kFast && !a.t.gtab) {
+    for (int t = threadIdx.x; t <= kExp2TabN; t += blockDim.x) {
+      if (t < kExp2TabN) {
+        sexp2[t] = exp2_table_entry(t);
+      } else {
+        const flt3 q = flt3_from_double(0.5 * (2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega))));
+        sexp2[t] = make_float2(q.hi, q.mid);
+        sexp2[t + 1] = make_float2(q.lo, 0.f);
+      }
+    }
   }
   __syncthreads();
   SmemAxesD A;
@@ -1135,11 +1123,23 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
       gg = e.x;
       g_sigma = e.y;
     } else {
-      const double gx = A.vd[0][iB] - A.vd[0][iA], gy = A.vd[1][jB] - A.vd[1][jA];
-      const double gz = A.vd[2][kB] - A.vd[2][kA];
-      gg = sqrt(gx * gx + gy * gy + gz * gz);
+      // |g|^2 from the nodes as pairs, |g| by the pair square root and g^(2 - 2 omega) as
+      // (|g|^2)^((2 - 2 omega)/2) by dfl_pow: the FP64 sqrt and pow they replace took half
+      // of the kernel's time on grids without a speed table
+      const dfl gxp = dfl_sub(A.v[0][iB], A.v[0][iA]), gyp = dfl_sub(A.v[1][jB], A.v[1][jA]);
+      const dfl gzp = dfl_sub(A.v[2][kB], A.v[2][kA]);
+      const dfl g2 = dfl_add(dfl_add(dfl_mul(gxp, gxp), dfl_mul(gyp, gyp)), dfl_mul(gzp, gzp));
+      const dfl gp = dfl_sqrt(g2);
+      gg = dfl_to_double(gp);
       if (gg < kDoubleTol) continue;
-      g_sigma = (vhs == 1.0) ? gg : pow(gg, vhs);
+      if (vhs == 1.0) {
+        g_sigma = gg;
+      } else {
+        const float2 qa = sexp2[kExp2TabN], qb = sexp2[kExp2TabN + 1];
+        flt3 q;
+        q.hi = qa.x; q.mid = qa.y; q.lo = qb.x;
+        g_sigma = dfl_to_double(dfl_pow(g2, q, sexp2));
+      }
     }
     // signs of the deviation partners (cdf_neq%sign); FMC: sign of phi_old. The low bit of
     // the value closing the partner's interval, next to the last values the search read

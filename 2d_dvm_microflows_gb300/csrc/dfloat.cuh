@@ -153,6 +153,10 @@ __device__ __forceinline__ dfl dfl_neg(dfl a) { return dfl_make(-a.hi, -a.lo); }
 
 __device__ __forceinline__ dfl dfl_sub(dfl a, dfl b) { return dfl_add(a, dfl_neg(b)); }
 
+__device__ __forceinline__ dfl dfl_abs(dfl a) {
+  return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? dfl_neg(a) : a;
+}
+
 // FP32 reciprocal and reciprocal square root estimates (MUFU, about 1 ulp); the callers
 // correct them with an exactly formed remainder.
 __device__ __forceinline__ float rcp_approx(float x) {

@@ -946,9 +946,9 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
   L.gtab = (L.gtab + 15) & ~static_cast<size_t>(15);  // double2 needs 16-byte alignment
   L.trig = L.gtab + (t.gtab_smem ? static_cast<size_t>(t.gtab_n) * sizeof(double2) : 0);
   L.exp2tab = L.trig + static_cast<size_t>(kTrigN) * sizeof(float4);
-  // without a speed table: 2^(j/32) and, after it, the exponent (2 - 2 omega)/2 as three
-  // floats
-  L.total = L.exp2tab + (t.gtab ? 0 : static_cast<size_t>(kExp2TabN + 2) * sizeof(float2));
+  // for the general kernel's powers: 2^(j/32), then the exponents (2 - 2 omega)/2 and
+  // 1/alpha as three floats each (two float2 slots each)
+  L.total = L.exp2tab + static_cast<size_t>(kExp2TabN + 4) * sizeof(float2);
   return L;
 }
 
@@ -1020,14 +1020,18 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
     strig[t] = make_float4(cn.hi, cn.lo, snn.hi, snn.lo);
   }
   float2* sexp2 = reinterpret_cast<float2*>(s_raw + L.exp2tab);
-  if (!kFast && !a.t.gtab) {
-    for (int t = threadIdx.x; t <= kExp2TabN; t += blockDim.x) {
+  if (!kFast) {
+    for (int t = threadIdx.x; t < kExp2TabN + 2; t += blockDim.x) {
       if (t < kExp2TabN) {
         sexp2[t] = exp2_table_entry(t);
       } else {
-        const flt3 q = flt3_from_double(0.5 * (2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega))));
-        sexp2[t] = make_float2(q.hi, q.mid);
-        sexp2[t + 1] = make_float2(q.lo, 0.f);
+        const double e = (t == kExp2TabN)
+                             ? 0.5 * (2.0 - 2.0 * (0.5 * (a.cp.omega + a.cp.omega)))
+                             : 1.0 / (0.5 * (a.cp.alpha + a.cp.alpha));
+        const flt3 q = flt3_from_double(e);
+        const int o = kExp2TabN + 2 * (t - kExp2TabN);
+        sexp2[o] = make_float2(q.hi, q.mid);
+        sexp2[o + 1] = make_float2(q.lo, 0.f);
       }
     }
   }
@@ -1182,37 +1186,11 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
       } else {
         sample_u53x2<kKeys, true>(a, static_cast<uint32_t>(i), cell, step, q, 1u + r, mphi, mcos);
       }
-      dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
-      if (vss) {
-        // VSS branch (pick_random_velocity_on_sphere :314-328) in FP64
-        const double rphi = rec ? rphi_rec : u53m(mphi), rcos = rec ? rcos_rec : u53m(mcos);
-        const double xA = A.vd[0][iA], yA = A.vd[1][jA], zA = A.vd[2][kA];
-        const double xB = A.vd[0][iB], yB = A.vd[1][jB], zB = A.vd[2][kB];
-        const double v0 = 0.5 * xA + 0.5 * xB, v1 = 0.5 * yA + 0.5 * yB, v2 = 0.5 * zA + 0.5 * zB;
-        const double sphi = sin(a.t.two_pi * rphi), cphi = cos(a.t.two_pi * rphi);
-        const double ur = fabs(xA - v0) + fabs(xB - v0);
-        const double vr_ = fabs(yA - v1) + fabs(yB - v1);
-        const double wr = fabs(zA - v2) + fabs(zB - v2);
-        const double ct = 2.0 * pow(rcos, ralpha) - 1.0;
-        const double stt = sqrt(1.0 - ct * ct);
-        const double den = sqrt(vr_ * vr_ + wr * wr);
-        double rx, ry, rz;
-        if (den > kDoubleTol * gg) {
-          rx = ct * ur + stt * sphi * den;
-          ry = ct * vr_ + stt * (gg * wr * cphi - ur * vr_ * sphi) / den;
-          rz = ct * wr - stt * (gg * vr_ * cphi + ur * wr * sphi) / den;
-        } else {
-          rx = ct * ur;
-          ry = stt * cphi * ur;
-          rz = stt * sphi * ur;
-        }
-        const dfl tx = dfl_from_double(0.5 * rx), ty = dfl_from_double(0.5 * ry);
-        const dfl tz = dfl_from_double(0.5 * rz);
-        ux = dfl_norm(tx.hi, tx.lo); uy = dfl_norm(ty.hi, ty.lo); uz = dfl_norm(tz.hi, tz.lo);
-      } else {
-        // phi = 2 pi R (pick_random_velocity_on_sphere :284-352): R = k/kTrigN + t, cos and
-        // sin of 2 pi k/kTrigN from the table, of th = 2 pi t (< 0.0062) by Taylor series
-        // (the dropped terms are below 1e-17), then the angle-addition formulas
+      // phi = 2 pi R (pick_random_velocity_on_sphere :284-352): R = k/kTrigN + t, cos and
+      // sin of 2 pi k/kTrigN from the table, of th = 2 pi t (< 0.0062) by Taylor series
+      // (the dropped terms are below 1e-17), then the angle-addition formulas
+      dfl cphi, sphi;
+      {
         int k;
         const dfl th = dfl_mul(two_pi, angle_fraction(mphi, k));
         const dfl t2 = dfl_mul(th, th);
@@ -1225,8 +1203,47 @@ __device__ __forceinline__ void collide_cta(const CollideArgs& a, int bid, int n
         const dfl cth = dfl_sub(dfl_make(1.f, 0.f), cc1);
         const float4 tb = strig[min(max(k, 0), kTrigN - 1)];
         const dfl C = dfl_make(tb.x, tb.y), S = dfl_make(tb.z, tb.w);
-        const dfl cphi = dfl_sub(dfl_mul(C, cth), dfl_mul(S, sth));
-        const dfl sphi = dfl_add(dfl_mul(S, cth), dfl_mul(C, sth));
+        cphi = dfl_sub(dfl_mul(C, cth), dfl_mul(S, sth));
+        sphi = dfl_add(dfl_mul(S, cth), dfl_mul(C, sth));
+      }
+      dfl ux, uy, uz;  // r / 2: half the post-collision relative velocity
+      if (vss) {
+        // VSS branch (pick_random_velocity_on_sphere :314-328) in pairs: cos theta =
+        // 2 R^(1/alpha) - 1 by dfl_pow; |x_A - v0| + |x_B - v0| = |x_A - x_B| for the midpoint
+        // v0 of a like-species pair
+        const dfl ur = dfl_abs(dfl_sub(A.v[0][iA], A.v[0][iB]));
+        const dfl vr_ = dfl_abs(dfl_sub(A.v[1][jA], A.v[1][jB]));
+        const dfl wr = dfl_abs(dfl_sub(A.v[2][kA], A.v[2][kB]));
+        dfl ct = dfl_make(-1.f, 0.f);  // R = 0
+        {
+          const double rc = rec ? rcos_rec : u53m(mcos);
+          if (rc > 0.0) {
+            const dfl r = dfl_from_double(rc);
+            const float2 qa = sexp2[kExp2TabN + 2], qb = sexp2[kExp2TabN + 3];
+            flt3 q;
+            q.hi = qa.x; q.mid = qa.y; q.lo = qb.x;
+            ct = dfl_sub(dfl_scale(dfl_pow(dfl_norm(r.hi, r.lo), q, sexp2), 2.f),
+                         dfl_make(1.f, 0.f));
+          }
+        }
+        const dfl one = dfl_make(1.f, 0.f);
+        const dfl stt = dfl_sqrt(dfl_sub(one, dfl_mul(ct, ct)));
+        const dfl den = dfl_sqrt(dfl_add(dfl_mul(vr_, vr_), dfl_mul(wr, wr)));
+        const dfl gp = dfl_scale(hg, 2.f);  // |g|
+        dfl rx, ry, rz;
+        if (den.hi > static_cast<float>(kDoubleTol) * gp.hi) {
+          rx = dfl_add(dfl_mul(ct, ur), dfl_mul(dfl_mul(stt, sphi), den));
+          const dfl ny = dfl_sub(dfl_mul(dfl_mul(gp, wr), cphi), dfl_mul(dfl_mul(ur, vr_), sphi));
+          const dfl nz = dfl_add(dfl_mul(dfl_mul(gp, vr_), cphi), dfl_mul(dfl_mul(ur, wr), sphi));
+          ry = dfl_add(dfl_mul(ct, vr_), dfl_div(dfl_mul(stt, ny), den));
+          rz = dfl_sub(dfl_mul(ct, wr), dfl_div(dfl_mul(stt, nz), den));
+        } else {
+          rx = dfl_mul(ct, ur);
+          ry = dfl_mul(dfl_mul(stt, cphi), ur);
+          rz = dfl_mul(dfl_mul(stt, sphi), ur);
+        }
+        ux = dfl_scale(rx, 0.5f); uy = dfl_scale(ry, 0.5f); uz = dfl_scale(rz, 0.5f);
+      } else {
         // cos theta = 2 R - 1 (exact in FP64), sin theta = sqrt(1 - cos^2)
         dfl ct;
         {

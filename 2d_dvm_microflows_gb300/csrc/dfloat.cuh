@@ -236,8 +236,8 @@ __device__ __forceinline__ dfl dfl_sqrt(dfl a) {
 //     2^n 2^(j/32) e^v, v = u ln 2, |v| <= 0.0109, 2^(j/32) from a 33-entry pair table and
 //     e^v by its Taylor series to v^6 (v^4 on in FP32) -- the table-driven reduction of
 //     P. T. P. Tang, ACM Trans. Math. Softw. 15 (1989) 144-157.
-// Each pair step rounds at about 2^-48 of a value below 1 in size: the result is within a
-// few 1e-15 relative whatever the size of q log2 x.
+// Each pair step rounds at about 2^-48 of a value below 1 in size: the result is within
+// about 1e-14 relative whatever the size of q log2 x.
 constexpr int kExp2TabN = 33;  // 2^(j/32), j = -16 .. 16
 
 // Entry t of the table (2^((t - 16)/32) as a normalised pair) from the FP64 exp2.
@@ -274,7 +274,11 @@ __device__ __forceinline__ dfl dfl_log2_split(dfl x, int& e) {
   const float sc = pow2f_exact(-e);
   const dfl m = dfl_make(x.hi * sc, x.lo * sc);                       // exact
   const dfl one = dfl_make(1.f, 0.f);
-  const dfl s = dfl_div(dfl_sub(m, one), dfl_add(m, one));
+  const dfl num = dfl_sub(m, one), den = dfl_add(m, one);
+  dfl s = dfl_div(num, den);
+  // one more correction of the quotient: s + (num - s den)/den (dfl_div alone holds about
+  // 2^-45 of s, the leading term of ln m)
+  s = dfl_add(s, dfl_make(__fmul_rn(dfl_sub(num, dfl_mul(s, den)).hi, rcp_approx(den.hi)), 0.f));
   const dfl t = dfl_mul(s, s);
   const float th = t.hi;
   // 1/9 + t/11 + ... + t^5/19 in FP32
@@ -304,11 +308,12 @@ __device__ __forceinline__ dfl dfl_exp2_split(int n, dfl y, const float2* tab) {
   const float vh = v.hi;
   const float tail = v2.hi * v2.hi * fmaf(vh, fmaf(vh, 1.f / 720.f, 1.f / 120.f), 1.f / 24.f);
   const dfl v3s = dfl_mul(dfl_mul(v2, v), dfl_make(0x1.555556p-3f, -0x1.555556p-28f));  // v^3/6
-  const dfl ev = dfl_add(dfl_add(dfl_make(1.f, 0.f), v),
-                         dfl_add(dfl_scale(v2, 0.5f), dfl_add(v3s, dfl_make(tail, 0.f))));
+  // e^v - 1, below 0.011 in size, so that 2^(j/32) e^v = T + T (e^v - 1) rounds only the
+  // small correction and the final sum
+  const dfl em1 = dfl_add(v, dfl_add(dfl_scale(v2, 0.5f), dfl_add(v3s, dfl_make(tail, 0.f))));
   const int ji = min(max(static_cast<int>(j) + 16, 0), kExp2TabN - 1);
-  const float2 T = tab[ji];
-  const dfl R = dfl_mul(dfl_make(T.x, T.y), ev);
+  const dfl T = dfl_make(tab[ji].x, tab[ji].y);
+  const dfl R = dfl_add(T, dfl_mul(T, em1));
   const float sc = pow2f_exact(n + static_cast<int>(ny));
   return dfl_make(R.hi * sc, R.lo * sc);
 }

@@ -41,7 +41,10 @@ int main() {
   cudaMalloc(&dx, n * sizeof(double));
   cudaMalloc(&de, n * sizeof(double));
   cudaMemcpy(dx, x.data(), n * sizeof(double), cudaMemcpyHostToDevice);
-  const double qs[] = {0.5 * (2.0 - 2.0 * 0.81), 0.5 * (2.0 - 2.0 * 0.74), 0.25, 0.5 * 0.1, 0.45};
+  // (2 - 2 omega)/2 for VHS omega 0.81, 0.74, 0.75, 0.95, 0.55, and 1/alpha for VSS alpha
+  // 1.4 and 1.01
+  const double qs[] = {0.5 * (2.0 - 2.0 * 0.81), 0.5 * (2.0 - 2.0 * 0.74), 0.25, 0.5 * 0.1,
+                       0.45, 1.0 / 1.4, 1.0 / 1.01};
   bool ok = true;
   std::printf("ok");
   for (double q : qs) {

@@ -28,8 +28,9 @@ def test_dfloat_accuracy(gpulib, tmp_path):
 
 def test_pair_power_accuracy(tmp_path):
     """dfl_pow, the pair x^q the collide kernel uses for g^(2 - 2 omega) on grids without a
-    speed table, against the FP64 pow: within 2e-14 relative for squared relative speeds
-    from 1e-20 to 1e5 and the exponents of the molecular models (HS to VHS omega 0.95)."""
+    speed table and for the VSS polar angle, against the FP64 pow: within 2e-14 relative for
+    arguments from 1e-20 to 1e5 and the exponents of the molecular models ((2 - 2 omega)/2
+    for VHS omega 0.55 to 0.95, 1/alpha for VSS alpha 1.01 and 1.4)."""
     exe = tmp_path / "dfl_pow_selftest"
     subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
                     "-I", CSRC, os.path.join(HERE, "csrc", "dfl_pow_selftest.cu"), "-o", str(exe)],
@@ -37,5 +38,5 @@ def test_pair_power_accuracy(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120).stdout.split()
     assert out[0] == "ok", out
     errs = [float(v) for v in out[1:]]
-    assert len(errs) == 5
+    assert len(errs) == 7
     assert max(errs) <= 2e-14, errs

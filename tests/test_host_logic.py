@@ -120,3 +120,33 @@ def test_oracle_cavity_conserves_mass_with_diffuse_walls(pkg, oracle):
     for _ in range(4):
         s.compute_convection()
     assert abs(s.phi().sum() - m0) < 1e-12 * m0
+
+
+def test_pair_constants_in_the_kernels():
+    """The hi + lo float pairs written as hex literals in the device code are the pair
+    splits of the constants they stand for: hi the float nearest the value, |lo| at most
+    half an ulp of hi, hi + lo within 2^-48 of the value."""
+    import math
+    import os
+    import re
+    from fractions import Fraction
+
+    import numpy as np
+
+    root = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..",
+                        "2d_dvm_microflows_gb300", "csrc")
+    src = open(os.path.join(root, "dfloat.cuh")).read() + open(
+        os.path.join(root, "dvm_kernels.cu")).read()
+    pair = re.compile(r"dfl_make\((-?0x[0-9a-f.]+p[-+]?\d+)f, (-?0x[0-9a-f.]+p[-+]?\d+)f\)")
+    found = {}
+    for name, value in (("c3 ", 1 / 3), ("c5 ", 1 / 5), ("c7 ", 1 / 7), ("inv_ln2", 1 / math.log(2)),
+                        ("u ln 2", math.log(2)), ("v^3/6", 1 / 6), ("one_sixth", 1 / 6)):
+        line = next(ln for ln in src.splitlines() if name in ln and "dfl_make(0x" in ln)
+        hi_s, lo_s = pair.search(line).groups()
+        hi, lo = float.fromhex(hi_s), float.fromhex(lo_s)
+        found[name] = (hi, lo)
+        assert np.float32(hi) == hi and np.float32(lo) == lo  # both are floats
+        assert float(np.float32(value)) == hi  # hi rounds the value to nearest
+        assert abs(lo) <= float(np.spacing(np.float32(abs(hi)))) / 2
+        assert abs(Fraction(hi) + Fraction(lo) - Fraction(value)) <= Fraction(value) * Fraction(1, 2 ** 48)
+    assert len(found) == 7

@@ -955,7 +955,8 @@ __host__ __device__ inline CollideSmem collide_smem_layout(const GridInfo& g, co
 // The common configuration: Philox uniforms (no recorded list), one replica, isotropic
 // scattering (alpha = 1) and the tabulated relative speeds of a cubic uniform grid. The
 // collide kernels are also compiled for it alone (kFast): without the other branches they
-// hold fewer registers live (the FP64 kernel spills 52 instead of 136 bytes per thread).
+// hold fewer registers live (the FP64 kernel's copy spills 24 bytes per thread, the general
+// kernel 116).
 static bool collide_fast(const CollideArgs& a) {
   return !a.pairs.active && a.cp.num_repl == 1 && a.t.gtab != nullptr &&
          !(fabs(1.0 / (0.5 * (a.cp.alpha + a.cp.alpha)) - 1.0) > kDoubleTol);

@@ -88,8 +88,6 @@ __device__ __forceinline__ long long to_fixed_f(float v, int k, uint32_t& bad) {
   return (b >> 31) ? -static_cast<long long>(r) : static_cast<long long>(r);
 }
 
-// 2^a as a float, for -126 <= a <= 127.
-__device__ __forceinline__ float pow2f(int a) { return __int_as_float((a + 127) << 23); }
 
 // to_fixed_f through the FP32 multiplier, for a scale 2^k = s1 s2 with s1, s2 normal
 // powers of two: v s1 s2 is exact (flushing to zero drops only values below 2^-126, whose
@@ -277,7 +275,8 @@ __device__ __forceinline__ void cdf_cta(const CdfArgs& a, const int cell) {
   // the equilibrium's scale 2^ke as two float factors (every cell of a sane density; the
   // bit-operation conversion covers the rest)
   const bool mul_scale = (ke >= -252 && ke <= 252);
-  const float s1 = mul_scale ? pow2f(ke / 2) : 1.f, s2 = mul_scale ? pow2f(ke - ke / 2) : 1.f;
+  const float s1 = mul_scale ? pow2f_exact(ke / 2) : 1.f;
+  const float s2 = mul_scale ? pow2f_exact(ke - ke / 2) : 1.f;
   const int NY = g.ny;
   const float rNX = 1.f / static_cast<float>(NX), rNXY = 1.f / static_cast<float>(NXY);
   const bool pairs = (reinterpret_cast<uintptr_t>(f) & 15u) == 0;
